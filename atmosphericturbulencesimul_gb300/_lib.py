@@ -1,0 +1,119 @@
+"""ctypes binding of libatmwfs.so (the C ABI declared in include/atmwfs.h).
+
+The library is the only compute path: if it is missing or cannot be loaded
+this module raises; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libatmwfs.so"
+
+OK = 0
+STATUS_NAMES = {0: "OK", 1: "ERR_INVALID", 2: "ERR_NOMEM", 3: "ERR_CUDA", 4: "ERR_IO", 5: "ERR_TIMEOUT",
+                6: "ERR_STATE", 7: "ERR_NODEVICE"}
+MODE_REF, MODE_SCI, MODE_PHASE = 0, 1, 2
+
+
+class AtmwfsError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Instance(C.Structure):
+    _fields_ = [
+        ("lambda_", C.c_double),
+        ("mode", C.c_int),
+        ("src_x", C.c_float),
+        ("src_y", C.c_float),
+        ("wf_raw_size", C.c_long),
+        ("wf_size", C.c_long),
+        ("scoeff", C.POINTER(C.c_float)),
+        ("roffset", C.POINTER(C.c_double)),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("nlayers", C.c_int),
+        ("alt", C.POINTER(C.c_double)),
+        ("cn2", C.POINTER(C.c_double)),
+        ("speed", C.POINTER(C.c_double)),
+        ("dir", C.POINTER(C.c_double)),
+        ("fresnel_bin", C.c_double),
+        ("zangle", C.c_float),
+        ("pupil_scale", C.c_float),
+        ("time_step", C.c_float),
+        ("master_size", C.c_long),
+        ("amplitude", C.c_int),
+        ("fresnel", C.c_int),
+        ("realtime", C.c_int),
+        ("realtime_factor", C.c_double),
+        ("ninst", C.c_int),
+        ("inst", C.POINTER(Instance)),
+        ("ring", C.c_int),
+    ]
+
+
+class Sink(C.Structure):
+    _fields_ = [("pha", C.POINTER(C.c_float)), ("amp", C.POINTER(C.c_float)), ("nslots", C.c_long)]
+
+
+# (name, restype, argtypes) of every exported entry point
+_ctx = C.c_void_p
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+SIGNATURES = [
+    ("atmwfs_create", C.c_int, [C.POINTER(Params), C.POINTER(_ctx)]),
+    ("atmwfs_destroy", None, [_ctx]),
+    ("atmwfs_load_screen", C.c_int, [_ctx, C.c_int, _fp, C.c_long]),
+    ("atmwfs_load_screen_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_long]),
+    ("atmwfs_normalize_screens", C.c_int, [_ctx, C.c_float, C.c_float, _dp]),
+    ("atmwfs_run", C.c_int, [_ctx, C.c_long, C.POINTER(Sink)]),
+    ("atmwfs_frame_dev", C.c_int, [_ctx, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    ("atmwfs_frame_floats", C.c_size_t, [_ctx]),
+    ("atmwfs_frame_offset", C.c_size_t, [_ctx, C.c_int]),
+    ("atmwfs_last_iters", C.c_int, [_ctx, C.c_int]),
+    ("atmwfs_steps_done", C.c_long, [_ctx]),
+    ("atmwfs_num_planes", C.c_int, [_ctx]),
+    ("atmwfs_plane_info", C.c_int, [_ctx, _ip, _ip, _dp]),
+    ("atmwfs_positions", C.c_int, [_ctx, C.c_int, _dp, _dp]),
+    ("atmwfs_stream", C.c_void_p, [_ctx]),
+    ("atmwfs_num_classes", C.c_int, [_ctx]),
+    ("atmwfs_time_pass", C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip]),
+    ("atmwfs_fresnel", C.c_int, [_fp, _fp, C.c_long, C.c_double, C.c_double, C.c_double]),
+    ("atmwfs_fresnel_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_double,
+                                     C.c_void_p]),
+    ("atmwfs_fft2d", C.c_int, [_fp, _fp, C.c_long, C.c_int]),
+    ("atmwfs_fft2d_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
+    ("atmwfs_master_screen", C.c_int, [C.c_uint64, C.c_uint32, C.c_long, C.c_double, C.c_double, _fp, _fp, _dp]),
+    ("atmwfs_last_error", C.c_char_p, []),
+]
+
+_lib = None
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load (once) and return the library with every signature declared."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} is missing: build it with atmosphericturbulencesimul_gb300.build.build()")
+    lib = C.CDLL(str(p))
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        raise AtmwfsError(status, load().atmwfs_last_error().decode(errors="replace"))

@@ -1,0 +1,344 @@
+// aux_kernels.cu -- setup and per-step helper kernels of the engine.
+#include "aux_kernels.cuh"
+#include "pass_impl.cuh"
+
+namespace atmwfs {
+
+// ---------------------------------------------------------------------------
+// halo-padded periodic screen copies (one-time setup)
+//   orient 0: P[yp][xp] = S[(yp - kPadY) mod M][(xp - kPadX) mod M]
+//   orient 1: P[yp][xp] = S[(xp - kPadX) mod M][(yp - kPadY) mod M]
+// ---------------------------------------------------------------------------
+__global__ void k_pad_screen(const float* __restrict__ S, int M, float* __restrict__ P, int Wp, int Hp, int orient)
+{
+    __shared__ float tileT[32][33];
+    const int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+    if (orient == 0) {
+        for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+            const int yp = by + r, xp = bx + threadIdx.x;
+            if (yp < Hp && xp < Wp) {
+                const int a = ((yp - kPadY) % M + M) % M, b = ((xp - kPadX) % M + M) % M;
+                P[(size_t)yp * Wp + xp] = S[(size_t)a * M + b];
+            }
+        }
+        return;
+    }
+    // transposed: read a 32 x 32 block of S coalesced, write it transposed
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int xp = bx + r, yp = by + threadIdx.x;  // element (yp, xp) = S[(xp-4)][(yp-1)]
+        const int a = ((xp - kPadX) % M + M) % M, b = ((yp - kPadY) % M + M) % M;
+        tileT[r][threadIdx.x] = S[(size_t)a * M + b];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        const int yp = by + r, xp = bx + threadIdx.x;
+        if (yp < Hp && xp < Wp) P[(size_t)yp * Wp + xp] = tileT[threadIdx.x][r];
+    }
+}
+
+cudaError_t pad_screen(const float* S, int M, float* P, int Wp, int Hp, int orient, cudaStream_t st)
+{
+    dim3 grid((Wp + 31) / 32, (Hp + 31) / 32), block(32, 8);
+    k_pad_screen<<<grid, block, 0, st>>>(S, M, P, Wp, Hp, orient);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// r0 measurement: sum over ii < M - dpix, all jj of (S[jj][ii] - S[jj][ii+dpix])^2
+// (AtmosphericTurbulence.c:2246-2263); float per thread, double per block.
+// ---------------------------------------------------------------------------
+__global__ void k_lagsq(const float* __restrict__ S, int M, int dpix, double* acc)
+{
+    double local = 0.0;
+    const long n = (long)M * M;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int ii = (int)(i % M);
+        if (ii < M - dpix) {
+            const double d = (double)S[i] - (double)S[i + dpix];
+            local += d * d;
+        }
+    }
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = local;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) atomicAdd(acc, v);
+    }
+}
+
+cudaError_t lag_sumsq(const float* S, int M, int dpix, double* acc, cudaStream_t st)
+{
+    k_lagsq<<<4 * 152, 256, 0, st>>>(S, M, dpix, acc);
+    return cudaGetLastError();
+}
+
+// S[i] = (float)((double)S[i] * f)  (the reference's float *= double)
+__global__ void k_scale(float* __restrict__ S, long n, double f)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        S[i] = (float)((double)S[i] * f);
+}
+
+cudaError_t scale_screen(float* S, long n, double f, cudaStream_t st)
+{
+    k_scale<<<4 * 152, 256, 0, st>>>(S, n, f);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// science-output unwrap: bin relaxation (AtmosphericTurbulence.c:3629-3941
+// float branch).  One CTA per science instance.  The twelve sweeps vote
+// +-0.2 (8-neighbourhood) or +-0.15 (distance-2 ring) into a float change
+// map; votes reach each bin in the reference's loop order so that the float
+// rounding of the accumulation is reproduced.
+// ---------------------------------------------------------------------------
+struct Sweep {
+    int dx, dy, ox, oy;
+    double c;
+};
+__constant__ Sweep c_sweeps[12] = {
+    {+1, 0, 0, 0, 0.2},   {0, +1, 0, 0, 0.2},   {+1, +1, 0, 0, 0.2},  {+1, -1, 0, 1, 0.2},
+    {+2, 0, 0, 0, 0.15},  {0, -2, 0, 2, 0.15},  {-1, -2, 1, 2, 0.15}, {+1, -2, 0, 2, 0.15},
+    {-2, -2, 2, 2, 0.15}, {+2, -2, 0, 2, 0.15}, {+2, -1, 0, 1, 0.15}, {-2, -1, 2, 1, 0.15},
+};
+
+__device__ __forceinline__ float vote_acc(float ch, double c) { return __double2float_rn((double)ch + c); }
+
+__device__ float bin_votes(const float* pb, int nb, int bx, int by)
+{
+    const double kPi = 3.14159265358979323846;
+    float ch = 0.0f;
+    const double pv = (double)pb[by * nb + bx];
+    for (int s = 0; s < 12; s++) {
+        const Sweep w = c_sweeps[s];
+        // role A: this bin is index1, partner index2 = (bx + dx, by + dy)
+        // role B: this bin is index2, partner index1 = (bx - dx, by - dy)
+        const int ax = bx + w.dx, ay = by + w.dy;
+        const int bxp = bx - w.dx, byp = by - w.dy;
+        const bool va = ax >= 0 && ax < nb && ay >= 0 && ay < nb;
+        const bool vb = bxp >= 0 && bxp < nb && byp >= 0 && byp < nb;
+        const bool a_first = (w.dx < 0) || (w.dx == 0 && w.dy < 0);
+        for (int k = 0; k < 2; k++) {
+            const bool doA = (k == 0) == a_first;
+            if (doA && va) {
+                const double pv2 = (double)pb[ay * nb + ax];
+                if (pv2 > pv + kPi) ch = vote_acc(ch, w.c);
+                if (pv > pv2 + kPi) ch = vote_acc(ch, -w.c);
+            }
+            if (!doA && vb) {
+                const double pv1 = (double)pb[byp * nb + bxp];
+                if (pv > pv1 + kPi) ch = vote_acc(ch, -w.c);
+                if (pv1 > pv + kPi) ch = vote_acc(ch, w.c);
+            }
+        }
+    }
+    return ch;
+}
+
+__global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restrict__ list, unsigned* status,
+                         int* iters_out)
+{
+    const InstDev& I = insts[list[blockIdx.x]];
+    const int nb = I.nb;
+    if (nb <= 0) return;
+    const int n = nb * nb;
+    extern __shared__ float sh[];
+    float* pb = sh;
+    float* ch = sh + n;
+    __shared__ unsigned s_max;
+    __shared__ int s_cnt;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        pb[i] = (float)atan2((double)I.bins[n + i], (double)I.bins[i]);
+        I.bins[i] = 0.0f;
+        I.bins[n + i] = 0.0f;
+    }
+    if (threadIdx.x == 0) { s_max = 0u; s_cnt = 0; }
+    __syncthreads();
+    int chiter = 0, chcnt0cnt = 0;
+    double plim = 1.0;
+    const double kTwoPi = 2.0 * 3.14159265358979323846;
+    while (plim > 0.51 && chiter < 1000 && chcnt0cnt < 5) {
+        chiter++;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const float c = bin_votes(pb, nb, i % nb, i / nb);
+            ch[i] = c;
+            atomicMax(&s_max, __float_as_uint(fabsf(c)));
+        }
+        __syncthreads();
+        plim = (double)__uint_as_float(s_max) - 0.001;
+        if (plim < 0.5) plim = 0.5;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const int bx = i % nb, by = i / nb;
+            const bool interior = bx > 1 && by > 1 && bx < nb - 2 && by < nb - 2;
+            const double c = (double)ch[i];
+            if (c > plim) {
+                if (interior) atomicAdd(&s_cnt, 1);
+                pb[i] = (float)((double)pb[i] + kTwoPi);
+            }
+            if (c < -plim) {
+                if (interior) atomicAdd(&s_cnt, 1);
+                pb[i] = (float)((double)pb[i] - kTwoPi);
+            }
+        }
+        __syncthreads();
+        const int chcnt = s_cnt;
+        __syncthreads();
+        if (threadIdx.x == 0) { s_max = 0u; s_cnt = 0; }
+        if (chcnt == 0) chcnt0cnt++;
+        else chcnt0cnt = 0;
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) I.peak[i] = pb[i];
+    if (threadIdx.x == 0 && iters_out) iters_out[list[blockIdx.x]] = chiter;
+}
+
+cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int maxnb, unsigned* status, int* iters,
+                        cudaStream_t st)
+{
+    if (nsci <= 0) return cudaSuccess;
+    const size_t sm = (size_t)2 * maxnb * maxnb * sizeof(float);
+    if (sm > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_unwrap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    k_unwrap<<<nsci, 512, sm, st>>>(insts, list, status, iters);
+    return cudaGetLastError();
+}
+
+// final science phase: pha + 2 pi round((phasum - pha - peak[bin]) / 2 pi)
+// (AtmosphericTurbulence.c:3918-3941)
+__global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __restrict__ list, const int* d_step)
+{
+    const InstDev& I = insts[list[blockIdx.y]];
+    const int Nout = I.Nout, nb = I.nb;
+    const long n = (long)Nout * Nout;
+    const int step = d_step ? *d_step : 0;
+    float* pha = I.out_pha + (size_t)(step % I.ring) * n;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int jj = (int)(i / Nout), ii = (int)(i % Nout);
+        const float peak = nb > 0 ? I.peak[I.binx[jj] * nb + I.binx[ii]] : 0.0f;
+        const float p = pha[i];
+        float d1, e1, d2, e2;
+        two_sum(I.phisum[i], -p, d1, e1);
+        two_sum(d1, -peak, d2, e2);
+        pha[i] = add_2pi_multiple(p, round_2pi(d2, e1 + e2));
+    }
+}
+
+cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxnout, const int* d_step, cudaStream_t st)
+{
+    if (nsci <= 0) return cudaSuccess;
+    const long n = (long)maxnout * maxnout;
+    const int bx = (int)((n + 255) / 256 < 64 ? (n + 255) / 256 : 64);
+    k_sci_apply<<<dim3(bx, nsci), 256, 0, st>>>(insts, list, d_step);
+    return cudaGetLastError();
+}
+
+__global__ void k_step_advance(int* d_step) { *d_step += 1; }
+
+cudaError_t step_advance(int* d_step, cudaStream_t st)
+{
+    k_step_advance<<<1, 1, 0, st>>>(d_step);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// master-screen synthesis (AtmosphericTurbulence.c:643-855)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t lo0 = 0xD2511F53u * c[0], hi0 = __umulhi(0xD2511F53u, c[0]);
+        const uint32_t lo1 = 0xCD9E8D57u * c[2], hi1 = __umulhi(0xCD9E8D57u, c[2]);
+        const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+// Spectrum A(k) exp(i 2 pi u), written at its fftshifted position (the
+// reference applies permut() before the FFT, :782).
+__global__ void k_screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, double fi, float2* __restrict__ C)
+{
+    const long n = (long)M * M;
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
+        uint32_t c[4] = {(uint32_t)p, stream, 0u, 0u};
+        philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        const float u = (float)(c[0] >> 8) * (1.0f / 16777216.0f);
+        const float u1 = ((float)(c[1] >> 8) + 1.0f) * (1.0f / 16777216.0f);
+        const float u2 = (float)(c[2] >> 8) * (1.0f / 16777216.0f);
+        const float g = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+        const int ii = (int)(p % M), jj = (int)(p / M);
+        const float dx = (float)(ii - M / 2), dy = (float)(jj - M / 2);
+        const float r2 = dx * dx + dy * dy;
+        const float d = sqrtf(r2 + (float)(fo * fo));
+        const float gi = g * sqrtf(expf(-r2 / (float)fi / (float)fi));
+        float a = gi / powf(d, 11.0f / 6.0f);
+        if (ii == M / 2 && jj == M / 2) a = 0.0f;
+        float s, co;
+        sincospif(2.0f * u, &s, &co);
+        const int io = (ii + M / 2) % M, jo = (jj + M / 2) % M;
+        C[(size_t)jo * M + io] = make_float2(a * co, a * s);
+    }
+}
+
+cudaError_t screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, double fi, float2* C, cudaStream_t st)
+{
+    k_screen_spectrum<<<8 * 152, 256, 0, st>>>(seed, stream, M, fo, fi, C);
+    return cudaGetLastError();
+}
+
+// Structure function D(lx, ly) of the real and imaginary parts at lags
+// (1..2)^2, circular (fft_structure_function, info.c:1670-1690, from its
+// definition).  acc[8]: [part][lag] sums.
+__global__ void k_strf(const float2* __restrict__ F, int M, double* acc)
+{
+    double loc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const long n = (long)M * M;
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
+        const int x = (int)(p % M), y = (int)(p / M);
+        const float2 a = F[p];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int lx = 1 + (q & 1), ly = 1 + (q >> 1);
+            const float2 b = F[(size_t)((y + ly) % M) * M + (x + lx) % M];
+            const double dr = (double)a.x - (double)b.x, di = (double)a.y - (double)b.y;
+            loc[q] += dr * dr;
+            loc[4 + q] += di * di;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        double v = loc[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[q], v);
+    }
+}
+
+cudaError_t strf_lags(const float2* F, int M, double* acc, cudaStream_t st)
+{
+    k_strf<<<4 * 152, 256, 0, st>>>(F, M, acc);
+    return cudaGetLastError();
+}
+
+__global__ void k_split_scale(const float2* __restrict__ F, long n, double s1, double s2, float* o1, float* o2)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float2 v = F[i];
+        if (o1) o1[i] = (float)((double)v.x * s1);
+        if (o2) o2[i] = (float)((double)v.y * s2);
+    }
+}
+
+cudaError_t split_scale(const float2* F, long n, double s1, double s2, float* o1, float* o2, cudaStream_t st)
+{
+    k_split_scale<<<4 * 152, 256, 0, st>>>(F, n, s1, s2, o1, o2);
+    return cudaGetLastError();
+}
+
+}  // namespace atmwfs

@@ -1,0 +1,25 @@
+// aux_kernels.cuh -- host launchers of the setup / per-step helper kernels.
+#pragma once
+#include "engine.cuh"
+
+namespace atmwfs {
+
+cudaError_t pad_screen(const float* S, int M, float* P, int Wp, int Hp, int orient, cudaStream_t st);
+cudaError_t lag_sumsq(const float* S, int M, int dpix, double* acc, cudaStream_t st);
+cudaError_t scale_screen(float* S, long n, double f, cudaStream_t st);
+cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int maxnb, unsigned* status, int* iters,
+                        cudaStream_t st);
+cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxnout, const int* d_step, cudaStream_t st);
+cudaError_t step_advance(int* d_step, cudaStream_t st);
+cudaError_t screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, double fi, float2* C, cudaStream_t st);
+cudaError_t strf_lags(const float2* F, int M, double* acc, cudaStream_t st);
+cudaError_t split_scale(const float2* F, long n, double s1, double s2, float* o1, float* o2, cudaStream_t st);
+
+cudaError_t launch_pass_64(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
+cudaError_t launch_pass_128(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
+cudaError_t launch_pass_256(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
+cudaError_t launch_pass_512(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
+cudaError_t launch_pass_1024(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
+cudaError_t launch_pass_2048(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
+
+}  // namespace atmwfs

@@ -1,0 +1,995 @@
+// capi.cu -- C ABI of the wavefront-series engine: context set-up (the host
+// part of make_AtmosphericTurbulence_wavefront_series,
+// src/AtmosphericTurbulence/AtmosphericTurbulence.c:1433-2560), the per-step
+// launch graph, and the unit-level operators.
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "atmwfs.h"
+#include "aux_kernels.cuh"
+
+namespace atmwfs {
+
+static const double kPi = 3.14159265358979323846264338328;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static atmwfs_status fail(atmwfs_status s, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return s;
+}
+
+#define AW_CUDA(expr)                                                                                     \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return fail(ATMWFS_ERR_CUDA, "%s failed: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                        \
+    } while (0)
+
+#define AW_TRY(expr)                            \
+    do {                                        \
+        atmwfs_status s_ = (expr);              \
+        if (s_ != ATMWFS_OK) return s_;         \
+    } while (0)
+
+PassLauncher pass_launcher(int N)
+{
+    switch (N) {
+        case 64: return launch_pass_64;
+        case 128: return launch_pass_128;
+        case 256: return launch_pass_256;
+        case 512: return launch_pass_512;
+        case 1024: return launch_pass_1024;
+        case 2048: return launch_pass_2048;
+        default: return nullptr;
+    }
+}
+
+static bool pow2_in(long n, long lo, long hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; }
+
+// Twiddle table exp(-2 pi i k / N), k < N, evaluated in double.  One copy per
+// (device, N) for the life of the process.
+static const float2* twiddles(int N)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, float2*> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(dev, N);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    std::vector<float2> h(N);
+    for (int k = 0; k < N; k++) {
+        const double a = -2.0 * kPi * (double)k / (double)N;
+        h[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    float2* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float2) * N) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    cache[key] = d;
+    return d;
+}
+
+// 1-D Fresnel transfer table of one hop: H[k] = exp(-i c f_k^2) / N with
+// c = pi z lambda / (dx N)^2 (WFpropagate.c:91) and f_k the centred
+// frequency of unshifted index k (the permut() pair around the multiply,
+// WFpropagate.c:75, 143).  The product over the two axes is the reference's
+// exp(-i c ((i-N/2)^2 + (j-N/2)^2)) / N^2.  The angle is formed and reduced
+// to [-pi, pi] in double before the float rounding.
+static void transfer_table(float2* h, int N, double dx, double z, double lambda)
+{
+    const double coeff = kPi * z * lambda / (dx * (double)N) / (dx * (double)N);
+    for (int k = 0; k < N; k++) {
+        const long f = k < N / 2 ? k : k - N;
+        double ang = -coeff * (double)(f * f);
+        ang -= 2.0 * kPi * nearbyint(ang / (2.0 * kPi));
+        h[k] = make_float2((float)(cos(ang) / N), (float)(sin(ang) / N));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// super-layer grouping (AtmosphericTurbulence.c:2067-2132) and the layer ->
+// super-layer index (:2135-2147; the reference's read past the end of the
+// separator array is given the value +infinity, which leaves the result
+// unchanged).  cn2 is normalised.
+// ---------------------------------------------------------------------------
+static int group_superlayers(const std::vector<double>& alt, const std::vector<double>& cn2, double bin,
+                             std::vector<double>& salt, std::vector<int>& sidx)
+{
+    const int L = (int)alt.size();
+    salt = alt;
+    std::vector<double> scn2 = cn2;
+    int S = L;
+    for (;;) {
+        double mind = alt[L - 1];
+        int idx = 0;
+        for (int i = 0; i < S - 1; i++) {
+            const double v = salt[i + 1] - salt[i];
+            if (v < mind) { mind = v; idx = i; }
+        }
+        if (mind > bin || S == 1) break;
+        salt[idx] = (scn2[idx] * salt[idx] + scn2[idx + 1] * salt[idx + 1]) / (scn2[idx] + scn2[idx + 1]);
+        scn2[idx] += scn2[idx + 1];
+        for (int i = idx + 1; i < S - 1; i++) { salt[i] = salt[i + 1]; scn2[i] = scn2[i + 1]; }
+        S--;
+    }
+    salt.resize(S);
+    const int nsep = S - 1;
+    std::vector<double> sep(nsep + 1);
+    for (int i = 0; i < nsep; i++) sep[i] = 0.5 * (salt[i] + salt[i + 1]);
+    sep[nsep] = INFINITY;
+    sidx.assign(L, 0);
+    for (int l = 0; l < L; l++) {
+        int idx = 0;
+        for (int i = 0; i < nsep; i++)
+            if (sep[i] < alt[l] && sep[i + 1] > alt[l]) idx = i + 1;
+        if (nsep > 0 && alt[l] > sep[nsep - 1]) idx = nsep;
+        sidx[l] = idx;
+    }
+    return S;
+}
+
+struct Class {
+    int N = 0, Nout = 0, RR = 0;
+    std::vector<int> members;  // global instance indices
+    int base = 0;              // first slot in the class-ordered InstDev array
+    TmaSet maps;
+};
+
+}  // namespace atmwfs
+
+using namespace atmwfs;
+
+struct atmwfs_ctx {
+    // configuration
+    int L = 0, ninst = 0, ring = 1;
+    long M = 0;
+    float pupil = 0, zangle = 0, tstep = 0;
+    int amplitude = 1, fresnel = 1, realtime = 0;
+    double rtfactor = 1.0;
+    std::vector<double> alt, cn2, speed, dir;
+    std::vector<atmwfs_instance> inst;
+    std::vector<std::vector<float>> scoeff;
+    std::vector<std::vector<double>> roff;
+    // planes: runs of layers with one super-layer index, top first
+    std::vector<double> salt;
+    std::vector<int> sidx;
+    std::vector<int> plane_lo, plane_hi;  // layers [lo, hi)
+    std::vector<double> hop_z;            // hop i: plane i -> plane i + 1
+    // frozen-flow state [inst * L + layer]
+    std::vector<double> xpos, ypos, xpos0, ypos0, vx, vy;
+    std::vector<long> xcnt, ycnt;
+    long steps = 0;
+    // device
+    cudaStream_t st = nullptr;
+    int Nmax = 0, Wp = 0, Hp = 0;
+    std::vector<float*> d_screen;        // raw M x M per layer
+    std::vector<float*> d_pad[2];        // padded copies per layer and orientation
+    std::vector<char> loaded;
+    bool normalized = false, committed = false;
+    std::vector<Class> classes;
+    std::vector<InstDev> hinst;          // class order
+    std::vector<int> slot_of;            // global index -> class-order slot
+    InstDev* d_inst = nullptr;
+    std::vector<void*> allocs;
+    size_t frame_floats = 0;
+    std::vector<size_t> frame_off;       // per global instance
+    float* d_out_pha = nullptr;          // [ring][frame_floats]
+    float* d_out_amp = nullptr;
+    int* d_step = nullptr;
+    unsigned* d_status = nullptr;
+    int* d_iters = nullptr;
+    int* d_sci = nullptr;
+    int nsci = 0, maxnb = 0, maxnout = 0;
+    LayerPos* d_pos = nullptr;
+    int poscap = 256;
+    LayerPos* h_pos[2] = {nullptr, nullptr};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaGraphExec_t gexec = nullptr;
+};
+
+namespace {
+
+atmwfs_status dalloc(atmwfs_ctx* c, void** p, size_t bytes)
+{
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(ATMWFS_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    c->allocs.push_back(*p);
+    return ATMWFS_OK;
+}
+
+// Start positions, wind, source and refraction offsets (:2152-2197).
+void init_positions(atmwfs_ctx* c)
+{
+    const int L = c->L;
+    const size_t n = (size_t)c->ninst * L;
+    c->xpos.assign(n, 0); c->ypos.assign(n, 0); c->xpos0.assign(n, 0); c->ypos0.assign(n, 0);
+    c->vx.assign(n, 0); c->vy.assign(n, 0); c->xcnt.assign(n, 0); c->ycnt.assign(n, 0);
+    const float dx = c->pupil;  // PUPIL_SCALE / pfactor with pfactor = 1, a float
+    for (int i = 0; i < c->ninst; i++)
+        for (int l = 0; l < L; l++) {
+            const size_t k = (size_t)i * L + l;
+            const atmwfs_instance& I = c->inst[i];
+            c->xpos[k] = 0.05 * c->M;
+            c->ypos[k] = 0.05 * c->M;
+            c->ypos[k] += c->roff[i][l] / dx;
+            c->xpos[k] += I.src_x * c->alt[l] / dx;
+            c->ypos[k] += I.src_y * c->alt[l] / dx;
+            c->xpos0[k] = I.src_x * c->alt[l] / dx;
+            c->ypos0[k] = I.src_y * c->alt[l] / dx;
+            c->vx[k] = c->speed[l] * cos(c->dir[l]) / dx;
+            c->vy[k] = c->speed[l] * sin(c->dir[l]) / dx;
+        }
+}
+
+// One step of the frozen-flow update of every layer of every instance
+// (:2700-2756) and the per-window sample origin (the reference evaluates
+// fmod(pos + ii, M) per pixel; at ii = 0 this gives the window origin).
+void advance_positions(atmwfs_ctx* c, double tnow, LayerPos* out)
+{
+    const double Md = (double)c->M;
+    const size_t n = (size_t)c->ninst * c->L;
+    for (size_t k = 0; k < n; k++) {
+        if (c->realtime) {
+            c->xpos[k] = c->xpos0[k] + c->vx[k] * tnow + 1.0 * c->xcnt[k] * Md;
+            c->ypos[k] = c->ypos0[k] + c->vy[k] * tnow + 1.0 * c->ycnt[k] * Md;
+        } else {
+            c->xpos[k] += c->vx[k] * c->tstep;
+            c->ypos[k] += c->vy[k] * c->tstep;
+        }
+        while (c->xpos[k] < 0) { c->xpos[k] += Md; c->xcnt[k]++; }
+        while (c->xpos[k] > Md) { c->xpos[k] -= Md; c->xcnt[k]--; }
+        while (c->ypos[k] < 0) { c->ypos[k] += Md; c->ycnt[k]++; }
+        while (c->ypos[k] > Md) { c->ypos[k] -= Md; c->ycnt[k]--; }
+        const double fxm = fmod(c->xpos[k], Md), fym = fmod(c->ypos[k], Md);
+        LayerPos p;
+        p.ix = (int)(long)fxm;
+        p.iy = (int)(long)fym;
+        p.fx = (float)(fxm - (double)p.ix);
+        p.fy = (float)(fym - (double)p.iy);
+        out[k] = p;
+    }
+}
+
+atmwfs_status make_tma_map(CUtensorMap* m, float* base, int Wp, int Hp, int box_rows)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !p)
+            return fail(ATMWFS_ERR_CUDA, "cuTensorMapEncodeTiled entry point unavailable");
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)Wp, (cuuint64_t)Hp};
+    cuuint64_t strides[1] = {(cuuint64_t)Wp * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)kBoxW, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ATMWFS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return ATMWFS_OK;
+}
+
+// Orientation of pass k (1-based) of Q = P + 1 passes: the last pass is in
+// the screen's own orientation.
+int pass_orient(int k, int Q) { return (Q - k) & 1; }
+
+// Launch pass k (1-based) for grid class cl; optionally report the
+// algorithmic bytes of the launch.
+atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes)
+{
+    const int Q = (int)c->plane_lo.size();
+    const int P = Q - 1;
+    {
+        {
+            PassArgs a;
+            memset(&a, 0, sizeof a);
+            a.inst = c->d_inst + cl.base;
+            a.pos = c->d_pos;
+            a.d_step = c->d_step;
+            a.d_status = c->d_status;
+            a.L = c->L;
+            a.ninst_total = c->ninst;
+            a.poscap = c->poscap;
+            a.g_lo = c->plane_lo[k - 1];
+            a.g_hi = c->plane_hi[k - 1];
+            a.hop1 = k - 2;
+            a.hop2 = k - 1;
+            a.src = k & 1;
+            a.dst = (k + 1) & 1;
+            a.orient = pass_orient(k, Q);
+            int var;
+            if (P == 0) var = kVarSingle;
+            else if (k == 1) var = kVarFirst;
+            else if (k == Q) var = kVarLast;
+            else var = kVarMid;
+            int rows = cl.N;
+            a.row0 = 0;
+            if (var == kVarLast || var == kVarSingle) {
+                const int off = (cl.N - cl.Nout) / 2;
+                a.row0 = off / cl.RR * cl.RR;
+                rows = (off + cl.Nout - a.row0 + cl.RR - 1) / cl.RR * cl.RR;
+            }
+            dim3 grid(rows / cl.RR, (unsigned)cl.members.size());
+            if (bytes) {
+                // field read / transposed write (8 B/px each), one screen tile
+                // of the window per gathered layer (4 B/px), outputs
+                const double px = (double)cl.N * cl.N, npx = (double)rows * cl.N, cnt = (double)cl.members.size();
+                const int ng = (var & OP_EPI) ? c->L : a.g_hi - a.g_lo;
+                double b = 0;
+                if (var & OP_LOAD) b += 8.0 * npx;
+                if (var & OP_STORE_T) b += 8.0 * px;
+                b += 4.0 * npx * ng;
+                if (var & OP_EPI) {
+                    const int mode = c->inst[cl.members[0]].mode;
+                    b += (double)cl.Nout * cl.Nout * (mode == ATMWFS_MODE_SCI ? 12.0 : 8.0);
+                }
+                *bytes = b * cnt;
+            }
+            AW_CUDA(pass_launcher(cl.N)(var, grid, a, &cl.maps, twiddles(cl.N), c->st));
+        }
+    }
+    return ATMWFS_OK;
+}
+
+atmwfs_status launch_step(atmwfs_ctx* c)
+{
+    const int Q = (int)c->plane_lo.size();
+    for (int k = 1; k <= Q; k++)
+        for (Class& cl : c->classes) AW_TRY(launch_pass(c, k, cl, nullptr));
+    if (c->nsci > 0) {
+        AW_CUDA(unwrap_bins(c->d_inst, c->d_sci, c->nsci, c->maxnb, c->d_status, c->d_iters, c->st));
+        AW_CUDA(sci_apply(c->d_inst, c->d_sci, c->nsci, c->maxnout, c->d_step, c->st));
+    }
+    AW_CUDA(step_advance(c->d_step, c->st));
+    return ATMWFS_OK;
+}
+
+atmwfs_status commit(atmwfs_ctx* c)
+{
+    if (c->committed) return ATMWFS_OK;
+    for (int l = 0; l < c->L; l++)
+        if (!c->loaded[l]) return fail(ATMWFS_ERR_STATE, "screen of layer %d not loaded", l);
+    const int Q = (int)c->plane_lo.size();
+    // orientations needed: 0 for every layer (last pass sums all layers),
+    // 1 for the layers gathered by passes in the transposed orientation
+    std::vector<char> need1(c->L, 0);
+    for (int k = 1; k <= Q; k++)
+        if (pass_orient(k, Q) == 1)
+            for (int l = c->plane_lo[k - 1]; l < c->plane_hi[k - 1]; l++) need1[l] = 1;
+    const size_t padn = (size_t)c->Wp * c->Hp;
+    for (int l = 0; l < c->L; l++) {
+        for (int o = 0; o < 2; o++) {
+            if (o == 1 && !need1[l]) continue;
+            if (!c->d_pad[o][l]) AW_TRY(dalloc(c, (void**)&c->d_pad[o][l], padn * sizeof(float)));
+            AW_CUDA(pad_screen(c->d_screen[l], (int)c->M, c->d_pad[o][l], c->Wp, c->Hp, o, c->st));
+        }
+    }
+    for (Class& cl : c->classes) {
+        memset(&cl.maps, 0, sizeof cl.maps);
+        for (int o = 0; o < 2; o++)
+            for (int l = 0; l < c->L; l++)
+                if (c->d_pad[o][l]) AW_TRY(make_tma_map(&cl.maps.m[o][l], c->d_pad[o][l], c->Wp, c->Hp, cl.RR + 3));
+    }
+    AW_CUDA(cudaStreamSynchronize(c->st));
+    // capture one step
+    cudaGraph_t g = nullptr;
+    AW_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
+    atmwfs_status s = launch_step(c);
+    cudaError_t ec = cudaStreamEndCapture(c->st, &g);
+    if (s != ATMWFS_OK) {
+        if (g) cudaGraphDestroy(g);
+        return s;
+    }
+    AW_CUDA(ec);
+    AW_CUDA(cudaGraphInstantiate(&c->gexec, g, 0));
+    cudaGraphDestroy(g);
+    c->committed = true;
+    return ATMWFS_OK;
+}
+
+atmwfs_status check_status(atmwfs_ctx* c)
+{
+    unsigned st = 0;
+    AW_CUDA(cudaMemcpyAsync(&st, c->d_status, sizeof st, cudaMemcpyDeviceToHost, c->st));
+    AW_CUDA(cudaStreamSynchronize(c->st));
+    if (st & kStatTmaTimeout) return fail(ATMWFS_ERR_TIMEOUT, "a screen tile load did not complete within 1 s");
+    if (st) return fail(ATMWFS_ERR_CUDA, "device status 0x%x", st);
+    return ATMWFS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* atmwfs_last_error(void) { return g_err.c_str(); }
+
+atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
+{
+    if (!p || !out) return fail(ATMWFS_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (p->nlayers < 1 || p->nlayers > kMaxLayers) return fail(ATMWFS_ERR_INVALID, "nlayers must be 1..%d", kMaxLayers);
+    if (!p->alt || !p->cn2 || !p->speed || !p->dir) return fail(ATMWFS_ERR_INVALID, "profile arrays missing");
+    if (!pow2_in(p->master_size, 64, 1 << 16)) return fail(ATMWFS_ERR_INVALID, "master_size must be a power of two >= 64");
+    if (p->ninst < 1 || !p->inst) return fail(ATMWFS_ERR_INVALID, "no instances");
+    if (!(p->pupil_scale > 0)) return fail(ATMWFS_ERR_INVALID, "pupil_scale must be > 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(ATMWFS_ERR_NODEVICE, "no CUDA device");
+    for (int i = 0; i < p->ninst; i++) {
+        const atmwfs_instance& I = p->inst[i];
+        if (!pow2_in(I.wf_raw_size, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "instance %d: wf_raw_size must be a power of two in 64..2048", i);
+        if (I.wf_size < 1 || I.wf_size > I.wf_raw_size) return fail(ATMWFS_ERR_INVALID, "instance %d: wf_size must be 1..wf_raw_size", i);
+        if (I.mode < 0 || I.mode > 2) return fail(ATMWFS_ERR_INVALID, "instance %d: bad mode", i);
+        if (!(I.lambda > 0)) return fail(ATMWFS_ERR_INVALID, "instance %d: lambda must be > 0", i);
+    }
+    atmwfs_ctx* c = new atmwfs_ctx();
+    c->L = p->nlayers;
+    c->ninst = p->ninst;
+    c->ring = p->ring < 1 ? 1 : p->ring;
+    c->M = p->master_size;
+    c->pupil = p->pupil_scale;
+    c->zangle = p->zangle;
+    c->tstep = p->time_step;
+    c->amplitude = p->amplitude;
+    c->fresnel = p->amplitude ? p->fresnel : 0;  // :1395-1402
+    c->realtime = p->realtime;
+    c->rtfactor = p->realtime_factor;
+    c->alt.assign(p->alt, p->alt + c->L);
+    c->cn2.assign(p->cn2, p->cn2 + c->L);
+    c->speed.assign(p->speed, p->speed + c->L);
+    c->dir.assign(p->dir, p->dir + c->L);
+    // Cn2 normalised to a sum of 1 (:2009-2015)
+    double tot = 0.0;
+    for (double v : c->cn2) tot += v;
+    if (!(tot > 0)) { delete c; return fail(ATMWFS_ERR_INVALID, "sum of cn2 must be > 0"); }
+    for (double& v : c->cn2) v *= 1.0 / tot;
+    c->inst.assign(p->inst, p->inst + c->ninst);
+    c->scoeff.resize(c->ninst);
+    c->roff.resize(c->ninst);
+    for (int i = 0; i < c->ninst; i++) {
+        c->scoeff[i].assign(c->L, 1.0f);
+        c->roff[i].assign(c->L, 0.0);
+        if (p->inst[i].scoeff) c->scoeff[i].assign(p->inst[i].scoeff, p->inst[i].scoeff + c->L);
+        if (p->inst[i].roffset) c->roff[i].assign(p->inst[i].roffset, p->inst[i].roffset + c->L);
+        c->inst[i].scoeff = nullptr;
+        c->inst[i].roffset = nullptr;
+        if (c->inst[i].mode == ATMWFS_MODE_PHASE && c->amplitude) c->inst[i].mode = ATMWFS_MODE_REF;
+        if (!c->amplitude) c->inst[i].mode = ATMWFS_MODE_PHASE;
+    }
+    group_superlayers(c->alt, c->cn2, p->fresnel_bin, c->salt, c->sidx);
+    // planes: layer runs met while walking from the top layer down (:2649-2692)
+    if (c->amplitude && c->fresnel) {
+        int hi = c->L;
+        for (int l = c->L - 1; l >= 0; l--) {
+            if (l == 0 || c->sidx[l - 1] != c->sidx[l]) {
+                c->plane_lo.push_back(l);
+                c->plane_hi.push_back(hi);
+                if (l > 0) c->hop_z.push_back((c->salt[c->sidx[l]] - c->salt[c->sidx[l - 1]]) / cos((double)c->zangle));
+                hi = l;
+            }
+        }
+    } else {
+        c->plane_lo.push_back(0);
+        c->plane_hi.push_back(c->L);
+    }
+    const int P = (int)c->hop_z.size();
+    init_positions(c);
+
+    atmwfs_status s = ATMWFS_OK;
+#define CK(x)                                  \
+    do {                                       \
+        s = (x);                               \
+        if (s != ATMWFS_OK) goto fail_out;     \
+    } while (0)
+#define CKC(x)                                                                                            \
+    do {                                                                                                  \
+        cudaError_t e_ = (x);                                                                             \
+        if (e_ != cudaSuccess) {                                                                          \
+            s = fail(ATMWFS_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));                        \
+            goto fail_out;                                                                                \
+        }                                                                                                 \
+    } while (0)
+    {
+        CKC(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        c->d_screen.assign(c->L, nullptr);
+        c->d_pad[0].assign(c->L, nullptr);
+        c->d_pad[1].assign(c->L, nullptr);
+        c->loaded.assign(c->L, 0);
+        // classes by (N, Nout)
+        for (int i = 0; i < c->ninst; i++) {
+            const int N = (int)c->inst[i].wf_raw_size, No = (int)c->inst[i].wf_size;
+            Class* cl = nullptr;
+            for (Class& x : c->classes)
+                if (x.N == N && x.Nout == No) cl = &x;
+            if (!cl) {
+                c->classes.push_back(Class());
+                cl = &c->classes.back();
+                cl->N = N;
+                cl->Nout = No;
+                cl->RR = rows_per_cta(N);
+            }
+            cl->members.push_back(i);
+            c->Nmax = c->Nmax > N ? c->Nmax : N;
+        }
+        c->Wp = (int)c->M + c->Nmax + 64;
+        c->Hp = (int)c->M + c->Nmax + 8;
+        // output frame layout: instance i at frame_off[i] inside one step's frame block
+        c->frame_off.assign(c->ninst, 0);
+        for (int i = 0; i < c->ninst; i++) {
+            c->frame_off[i] = c->frame_floats;
+            c->frame_floats += (size_t)c->inst[i].wf_size * c->inst[i].wf_size;
+        }
+        CK(dalloc(c, (void**)&c->d_out_pha, sizeof(float) * c->frame_floats * c->ring));
+        CK(dalloc(c, (void**)&c->d_out_amp, sizeof(float) * c->frame_floats * c->ring));
+        c->slot_of.assign(c->ninst, 0);
+        std::vector<int> sci;
+        int slot = 0;
+        for (Class& cl : c->classes) {
+            cl.base = slot;
+            for (int i : cl.members) {
+                const atmwfs_instance& I = c->inst[i];
+                InstDev d;
+                memset(&d, 0, sizeof d);
+                const int N = cl.N, No = cl.Nout;
+                d.N = N;
+                d.Nout = No;
+                d.off = (N - No) / 2;
+                d.mode = I.mode;
+                d.ring = c->ring;
+                d.gidx = i;
+                for (int l = 0; l < c->L; l++) d.scoeff[l] = c->scoeff[i][l];
+                for (int b = 0; b < 2; b++) CK(dalloc(c, (void**)&d.fld[b], sizeof(float2) * (size_t)N * N));
+                if (P > 0) {
+                    std::vector<float2> h((size_t)P * N);
+                    for (int hh = 0; hh < P; hh++)
+                        transfer_table(h.data() + (size_t)hh * N, N, (double)c->pupil, c->hop_z[hh], I.lambda);
+                    float2* dh = nullptr;
+                    CK(dalloc(c, (void**)&dh, sizeof(float2) * h.size()));
+                    CKC(cudaMemcpy(dh, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice));
+                    d.H = dh;
+                }
+                // the ring holds the frames of all instances contiguously per slot
+                d.out_pha = c->d_out_pha + c->frame_off[i];
+                d.out_amp = c->d_out_amp + c->frame_off[i];
+                if (I.mode == ATMWFS_MODE_SCI) {
+                    d.nb = No / 20;
+                    CK(dalloc(c, (void**)&d.phisum, sizeof(float) * (size_t)No * No));
+                    const int nb2 = d.nb * d.nb > 0 ? d.nb * d.nb : 1;
+                    CK(dalloc(c, (void**)&d.bins, sizeof(float) * 2 * nb2));
+                    CKC(cudaMemset(d.bins, 0, sizeof(float) * 2 * nb2));
+                    CK(dalloc(c, (void**)&d.peak, sizeof(float) * nb2));
+                    std::vector<short> bx(No);
+                    for (int ii = 0; ii < No; ii++) bx[ii] = (short)(long)(1.0 * ii / No * d.nb);
+                    short* dbx = nullptr;
+                    CK(dalloc(c, (void**)&dbx, sizeof(short) * No));
+                    CKC(cudaMemcpy(dbx, bx.data(), sizeof(short) * No, cudaMemcpyHostToDevice));
+                    d.binx = dbx;
+                    sci.push_back(slot);
+                    c->maxnb = c->maxnb > d.nb ? c->maxnb : d.nb;
+                    c->maxnout = c->maxnout > No ? c->maxnout : No;
+                }
+                c->hinst.push_back(d);
+                c->slot_of[i] = slot;
+                slot++;
+            }
+        }
+        CK(dalloc(c, (void**)&c->d_inst, sizeof(InstDev) * c->hinst.size()));
+        CKC(cudaMemcpy(c->d_inst, c->hinst.data(), sizeof(InstDev) * c->hinst.size(), cudaMemcpyHostToDevice));
+        c->nsci = (int)sci.size();
+        if (c->nsci) {
+            CK(dalloc(c, (void**)&c->d_sci, sizeof(int) * sci.size()));
+            CKC(cudaMemcpy(c->d_sci, sci.data(), sizeof(int) * sci.size(), cudaMemcpyHostToDevice));
+        }
+        CK(dalloc(c, (void**)&c->d_step, sizeof(int)));
+        CKC(cudaMemset(c->d_step, 0, sizeof(int)));
+        CK(dalloc(c, (void**)&c->d_status, sizeof(unsigned)));
+        CKC(cudaMemset(c->d_status, 0, sizeof(unsigned)));
+        CK(dalloc(c, (void**)&c->d_iters, sizeof(int) * c->ninst * 0 + sizeof(int) * (c->hinst.size() + 1)));
+        const size_t posn = (size_t)c->poscap * c->ninst * c->L;
+        CK(dalloc(c, (void**)&c->d_pos, sizeof(LayerPos) * posn));
+        CKC(cudaMemset(c->d_pos, 0, sizeof(LayerPos) * posn));
+        for (int b = 0; b < 2; b++) {
+            CKC(cudaHostAlloc((void**)&c->h_pos[b], sizeof(LayerPos) * posn, cudaHostAllocDefault));
+            CKC(cudaEventCreateWithFlags(&c->ev[b], cudaEventDisableTiming));
+        }
+        for (int b = 0; b < 2; b++) CKC(cudaEventRecord(c->ev[b], c->st));
+        for (const Class& cl : c->classes) {
+            if (!twiddles(cl.N)) {
+                s = fail(ATMWFS_ERR_NOMEM, "twiddle table allocation failed");
+                goto fail_out;
+            }
+        }
+    }
+#undef CK
+#undef CKC
+    *out = c;
+    return ATMWFS_OK;
+fail_out:
+    atmwfs_destroy(c);
+    return s;
+}
+
+void atmwfs_destroy(atmwfs_ctx* c)
+{
+    if (!c) return;
+    if (c->st) cudaStreamSynchronize(c->st);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    for (void* p : c->allocs) cudaFree(p);
+    for (int b = 0; b < 2; b++) {
+        if (c->h_pos[b]) cudaFreeHost(c->h_pos[b]);
+        if (c->ev[b]) cudaEventDestroy(c->ev[b]);
+    }
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+}
+
+static atmwfs_status load_common(atmwfs_ctx* c, int layer, const float* src, long M, cudaMemcpyKind kind)
+{
+    if (!c || !src) return fail(ATMWFS_ERR_INVALID, "null argument");
+    if (layer < 0 || layer >= c->L) return fail(ATMWFS_ERR_INVALID, "layer %d out of range", layer);
+    if (M != c->M) return fail(ATMWFS_ERR_INVALID, "screen size %ld differs from master_size %ld", M, c->M);
+    if (c->normalized) return fail(ATMWFS_ERR_STATE, "screens already normalised");
+    if (!c->d_screen[layer]) AW_TRY(dalloc(c, (void**)&c->d_screen[layer], sizeof(float) * (size_t)M * M));
+    AW_CUDA(cudaMemcpyAsync(c->d_screen[layer], src, sizeof(float) * (size_t)M * M, kind, c->st));
+    AW_CUDA(cudaStreamSynchronize(c->st));
+    c->loaded[layer] = 1;
+    c->committed = false;
+    if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_load_screen(atmwfs_ctx* c, int layer, const float* host, long M)
+{
+    return load_common(c, layer, host, M, cudaMemcpyHostToDevice);
+}
+
+atmwfs_status atmwfs_load_screen_dev(atmwfs_ctx* c, int layer, const float* dev, long M)
+{
+    return load_common(c, layer, dev, M, cudaMemcpyDeviceToDevice);
+}
+
+atmwfs_status atmwfs_normalize_screens(atmwfs_ctx* c, float lambda_ref, float seeing, double* r0_pix)
+{
+    if (!c) return fail(ATMWFS_ERR_INVALID, "null context");
+    for (int l = 0; l < c->L; l++)
+        if (!c->loaded[l]) return fail(ATMWFS_ERR_STATE, "screen of layer %d not loaded", l);
+    const int dpix = 50;
+    if (c->M <= dpix) return fail(ATMWFS_ERR_INVALID, "master_size must exceed 50 pixels");
+    double* acc = nullptr;
+    AW_CUDA(cudaMalloc(&acc, sizeof(double) * c->L));
+    auto measure = [&](double* r0) -> atmwfs_status {
+        AW_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * c->L, c->st));
+        for (int l = 0; l < c->L; l++) AW_CUDA(lag_sumsq(c->d_screen[l], (int)c->M, dpix, acc + l, c->st));
+        std::vector<double> h(c->L);
+        AW_CUDA(cudaMemcpyAsync(h.data(), acc, sizeof(double) * c->L, cudaMemcpyDeviceToHost, c->st));
+        AW_CUDA(cudaStreamSynchronize(c->st));
+        const double cnt = (double)(c->M - dpix) * (double)c->M;
+        double tot = 0.0;
+        for (int l = 0; l < c->L; l++) tot += 1.0 * dpix * pow((h[l] / cnt) / 6.88, -3.0 / 5.0);
+        *r0 = tot / c->L;
+        return ATMWFS_OK;
+    };
+    double r0a = 0, r0b = 0;
+    atmwfs_status s = measure(&r0a);
+    if (s == ATMWFS_OK) {
+        // r0 target (:2278-2285): lambda / seeing[rad] / pixel scale
+        const double target = lambda_ref / (seeing / 3600.0 / 180.0 * kPi) / c->pupil * 1;
+        const double tmp1 = pow(r0a / target, 5.0 / 6.0);
+        for (int l = 0; l < c->L && s == ATMWFS_OK; l++)
+            if (scale_screen(c->d_screen[l], c->M * c->M, tmp1, c->st) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "scale failed");
+        if (s == ATMWFS_OK) s = measure(&r0b);
+        // per-layer weight sqrt(Cn2 / cos(zenith)) (:2340-2363)
+        for (int l = 0; l < c->L && s == ATMWFS_OK; l++)
+            if (scale_screen(c->d_screen[l], c->M * c->M, sqrt(c->cn2[l] / cos((double)c->zangle)), c->st) != cudaSuccess)
+                s = fail(ATMWFS_ERR_CUDA, "scale failed");
+    }
+    cudaStreamSynchronize(c->st);
+    cudaFree(acc);
+    if (s != ATMWFS_OK) return s;
+    if (r0_pix) { r0_pix[0] = r0a; r0_pix[1] = r0b; }
+    c->normalized = true;
+    c->committed = false;
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
+{
+    if (!c) return fail(ATMWFS_ERR_INVALID, "null context");
+    if (nsteps < 0) return fail(ATMWFS_ERR_INVALID, "nsteps < 0");
+    AW_TRY(commit(c));
+    const size_t per = (size_t)c->ninst * c->L;
+    long s = 0;
+    int b = 0;
+    while (s < nsteps) {
+        const long g0 = c->steps;
+        long chunk = nsteps - s;
+        if (chunk > c->poscap) chunk = c->poscap;
+        AW_CUDA(cudaEventSynchronize(c->ev[b]));
+        for (long i = 0; i < chunk; i++) {
+            double tnow = 0.0;
+            if (c->realtime) {
+                struct timespec ts;
+                clock_gettime(CLOCK_REALTIME, &ts);
+                tnow = (1.0 * ts.tv_sec + 1.0e-9 * ts.tv_nsec) * c->rtfactor;
+            }
+            advance_positions(c, tnow, c->h_pos[b] + (size_t)i * per);
+            c->steps++;
+        }
+        // upload into ring slots g0 .. g0 + chunk - 1 (mod poscap)
+        const long s0 = g0 % c->poscap;
+        const long n1 = chunk < c->poscap - s0 ? chunk : c->poscap - s0;
+        AW_CUDA(cudaMemcpyAsync(c->d_pos + s0 * per, c->h_pos[b], sizeof(LayerPos) * per * n1, cudaMemcpyHostToDevice, c->st));
+        if (chunk > n1)
+            AW_CUDA(cudaMemcpyAsync(c->d_pos, c->h_pos[b] + n1 * per, sizeof(LayerPos) * per * (chunk - n1),
+                                    cudaMemcpyHostToDevice, c->st));
+        AW_CUDA(cudaEventRecord(c->ev[b], c->st));
+        for (long i = 0; i < chunk; i++) {
+            AW_CUDA(cudaGraphLaunch(c->gexec, c->st));
+            if (sink) {
+                const long slot = (g0 + i) % c->ring;
+                const long hs = sink->nslots > 0 ? (s + i) % sink->nslots : (s + i);
+                const size_t ff = c->frame_floats;
+                if (sink->pha)
+                    AW_CUDA(cudaMemcpyAsync(sink->pha + (size_t)hs * ff, c->d_out_pha + slot * ff, sizeof(float) * ff,
+                                            cudaMemcpyDeviceToHost, c->st));
+                if (sink->amp)
+                    AW_CUDA(cudaMemcpyAsync(sink->amp + (size_t)hs * ff, c->d_out_amp + slot * ff, sizeof(float) * ff,
+                                            cudaMemcpyDeviceToHost, c->st));
+            }
+        }
+        s += chunk;
+        b ^= 1;
+    }
+    return check_status(c);
+}
+
+atmwfs_status atmwfs_frame_dev(atmwfs_ctx* c, int i, const float** pha, const float** amp)
+{
+    if (!c || i < 0 || i >= c->ninst) return fail(ATMWFS_ERR_INVALID, "bad instance");
+    if (c->steps == 0) return fail(ATMWFS_ERR_STATE, "no frame computed yet");
+    const long slot = (c->steps - 1) % c->ring;
+    if (pha) *pha = c->d_out_pha + slot * c->frame_floats + c->frame_off[i];
+    if (amp) *amp = c->d_out_amp + slot * c->frame_floats + c->frame_off[i];
+    return ATMWFS_OK;
+}
+
+void* atmwfs_stream(atmwfs_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int atmwfs_num_classes(const atmwfs_ctx* c) { return c ? (int)c->classes.size() : 0; }
+
+atmwfs_status atmwfs_time_pass(atmwfs_ctx* c, int k, int ci, int reps, double* ms, double* bytes, int* n, int* count)
+{
+    if (!c || ci < 0 || ci >= (int)c->classes.size()) return fail(ATMWFS_ERR_INVALID, "bad class");
+    if (k < 1 || k > (int)c->plane_lo.size() || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
+    AW_TRY(commit(c));
+    Class& cl = c->classes[ci];
+    cudaEvent_t e0, e1;
+    AW_CUDA(cudaEventCreate(&e0));
+    AW_CUDA(cudaEventCreate(&e1));
+    double b = 0;
+    atmwfs_status s = launch_pass(c, k, cl, &b);  // warm-up
+    if (s == ATMWFS_OK) {
+        cudaEventRecord(e0, c->st);
+        for (int r = 0; r < reps && s == ATMWFS_OK; r++) s = launch_pass(c, k, cl, nullptr);
+        cudaEventRecord(e1, c->st);
+    }
+    float t = 0;
+    if (s == ATMWFS_OK && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != ATMWFS_OK) return s;
+    if (ms) *ms = t / reps;
+    if (bytes) *bytes = b;
+    if (n) *n = cl.N;
+    if (count) *count = (int)cl.members.size();
+    return check_status(c);
+}
+
+size_t atmwfs_frame_offset(const atmwfs_ctx* c, int i) { return (c && i >= 0 && i < c->ninst) ? c->frame_off[i] : 0; }
+size_t atmwfs_frame_floats(const atmwfs_ctx* c) { return c ? c->frame_floats : 0; }
+
+long atmwfs_steps_done(const atmwfs_ctx* c) { return c ? c->steps : -1; }
+
+int atmwfs_num_planes(const atmwfs_ctx* c) { return c ? (int)c->plane_lo.size() : 0; }
+
+atmwfs_status atmwfs_plane_info(const atmwfs_ctx* c, int* lo, int* hi, double* z)
+{
+    if (!c) return fail(ATMWFS_ERR_INVALID, "null context");
+    for (size_t k = 0; k < c->plane_lo.size(); k++) {
+        if (lo) lo[k] = c->plane_lo[k];
+        if (hi) hi[k] = c->plane_hi[k];
+        if (z && k < c->hop_z.size()) z[k] = c->hop_z[k];
+    }
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_positions(const atmwfs_ctx* c, int i, double* x, double* y)
+{
+    if (!c || i < 0 || i >= c->ninst) return fail(ATMWFS_ERR_INVALID, "bad instance");
+    for (int l = 0; l < c->L; l++) {
+        if (x) x[l] = c->xpos[(size_t)i * c->L + l];
+        if (y) y[l] = c->ypos[(size_t)i * c->L + l];
+    }
+    return ATMWFS_OK;
+}
+
+int atmwfs_last_iters(atmwfs_ctx* c, int i)
+{
+    if (!c || i < 0 || i >= c->ninst || !c->d_iters) return -1;
+    int v = -1;
+    cudaMemcpy(&v, c->d_iters + c->slot_of[i], sizeof(int), cudaMemcpyDeviceToHost);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// unit operators
+// ---------------------------------------------------------------------------
+static atmwfs_status two_pass(const void* in, void* out, long n, int var, const float2* H, cudaStream_t st)
+{
+    const PassLauncher fn = pass_launcher((int)n);
+    if (!fn) return fail(ATMWFS_ERR_INVALID, "size %ld unsupported (power of two 64..2048)", n);
+    const float2* tw = twiddles((int)n);
+    if (!tw) return fail(ATMWFS_ERR_NOMEM, "twiddle allocation failed");
+    float2* tmp = nullptr;
+    AW_CUDA(cudaMallocAsync((void**)&tmp, sizeof(float2) * n * n, st));
+    const int RR = rows_per_cta((int)n);
+    PassArgs a;
+    memset(&a, 0, sizeof a);
+    a.H1 = H;
+    a.H2 = H;
+    a.ext_in = (const float2*)in;
+    a.ext_out = tmp;
+    cudaError_t e = fn(var, dim3((unsigned)(n / RR), 1), a, nullptr, tw, st);
+    if (e == cudaSuccess) {
+        a.ext_in = tmp;
+        a.ext_out = (float2*)out;
+        e = fn(var, dim3((unsigned)(n / RR), 1), a, nullptr, tw, st);
+    }
+    cudaFreeAsync(tmp, st);
+    AW_CUDA(e);
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_fresnel_dev(const void* in, void* out, long n, double dx, double z, double lambda, void* stream)
+{
+    if (!in || !out) return fail(ATMWFS_ERR_INVALID, "null buffer");
+    if (!pow2_in(n, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "size %ld unsupported (power of two 64..2048)", n);
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<float2> h(n);
+    transfer_table(h.data(), (int)n, dx, z, lambda);
+    float2* dh = nullptr;
+    AW_CUDA(cudaMallocAsync((void**)&dh, sizeof(float2) * n, st));
+    cudaError_t e = cudaMemcpyAsync(dh, h.data(), sizeof(float2) * n, cudaMemcpyHostToDevice, st);
+    atmwfs_status s = e == cudaSuccess ? two_pass(in, out, n, kVarUnitProp, dh, st)
+                                       : fail(ATMWFS_ERR_CUDA, "copy failed: %s", cudaGetErrorString(e));
+    cudaFreeAsync(dh, st);
+    // the host table must outlive the asynchronous copy
+    cudaStreamSynchronize(st);
+    return s;
+}
+
+atmwfs_status atmwfs_fft2d_dev(const void* in, void* out, long n, int sign, void* stream)
+{
+    if (!in || !out) return fail(ATMWFS_ERR_INVALID, "null buffer");
+    if (sign != -1 && sign != 1) return fail(ATMWFS_ERR_INVALID, "sign must be -1 or +1");
+    return two_pass(in, out, n, sign < 0 ? kVarUnitFwd : kVarUnitInv, nullptr, (cudaStream_t)stream);
+}
+
+static atmwfs_status host_unit(const float* in, float* out, long n,
+                               atmwfs_status (*fn)(const void*, void*, long, void*, const void*), const void* arg)
+{
+    if (!in || !out) return fail(ATMWFS_ERR_INVALID, "null buffer");
+    if (!pow2_in(n, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "size %ld unsupported (power of two 64..2048)", n);
+    const size_t bytes = sizeof(float2) * n * n;
+    void *din = nullptr, *dout = nullptr;
+    AW_CUDA(cudaMalloc(&din, bytes));
+    if (cudaMalloc(&dout, bytes) != cudaSuccess) {
+        cudaFree(din);
+        return fail(ATMWFS_ERR_NOMEM, "cudaMalloc failed");
+    }
+    atmwfs_status s = ATMWFS_OK;
+    if (cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "H2D failed");
+    if (s == ATMWFS_OK) s = fn(din, dout, n, nullptr, arg);
+    if (s == ATMWFS_OK && cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "D2H failed");
+    cudaFree(din);
+    cudaFree(dout);
+    return s;
+}
+
+struct FresnelArg { double dx, z, lambda; };
+
+static atmwfs_status fresnel_thunk(const void* in, void* out, long n, void* st, const void* arg)
+{
+    const FresnelArg* f = (const FresnelArg*)arg;
+    return atmwfs_fresnel_dev(in, out, n, f->dx, f->z, f->lambda, st);
+}
+
+static atmwfs_status fft_thunk(const void* in, void* out, long n, void* st, const void* arg)
+{
+    atmwfs_status s = atmwfs_fft2d_dev(in, out, n, *(const int*)arg, st);
+    if (s == ATMWFS_OK && cudaStreamSynchronize((cudaStream_t)st) != cudaSuccess) return fail(ATMWFS_ERR_CUDA, "sync failed");
+    return s;
+}
+
+atmwfs_status atmwfs_fresnel(const float* in, float* out, long n, double dx, double z, double lambda)
+{
+    FresnelArg f = {dx, z, lambda};
+    return host_unit(in, out, n, fresnel_thunk, &f);
+}
+
+atmwfs_status atmwfs_fft2d(const float* in, float* out, long n, int sign)
+{
+    if (sign != -1 && sign != 1) return fail(ATMWFS_ERR_INVALID, "sign must be -1 or +1");
+    return host_unit(in, out, n, fft_thunk, &sign);
+}
+
+atmwfs_status atmwfs_master_screen(uint64_t seed, uint32_t stream, long M, double outer_pix, double inner_pix,
+                                   float* out1, float* out2, double* cfit)
+{
+    if (!pow2_in(M, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "M=%ld unsupported (power of two 64..2048)", M);
+    if (!(outer_pix > 0) || !(inner_pix > 0)) return fail(ATMWFS_ERR_INVALID, "scales must be > 0");
+    const size_t n = (size_t)M * M;
+    float2 *C = nullptr, *F = nullptr;
+    double* acc = nullptr;
+    float *o1 = nullptr, *o2 = nullptr;
+    atmwfs_status s = ATMWFS_OK;
+    cudaStream_t st = nullptr;
+    if (cudaMalloc(&C, n * sizeof(float2)) != cudaSuccess || cudaMalloc(&F, n * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&acc, 8 * sizeof(double)) != cudaSuccess || cudaMalloc(&o1, n * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&o2, n * sizeof(float)) != cudaSuccess) {
+        s = fail(ATMWFS_ERR_NOMEM, "cudaMalloc failed");
+    }
+    // f0 = M / L0pix, fi = (5.92 / 2 pi) M / l0pix (:679-680)
+    const double fo = 1.0 * M / outer_pix;
+    const double fi = (5.92 / (2.0 * kPi)) * M / inner_pix;
+    double C12[2] = {0, 0};
+    if (s == ATMWFS_OK && screen_spectrum(seed, stream, (int)M, fo, fi, C, st) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "spectrum kernel failed");
+    if (s == ATMWFS_OK) s = atmwfs_fft2d_dev(C, F, M, -1, st);
+    if (s == ATMWFS_OK && cudaMemset(acc, 0, 8 * sizeof(double)) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "memset failed");
+    if (s == ATMWFS_OK && strf_lags(F, (int)M, acc, st) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "strf kernel failed");
+    double h[8];
+    if (s == ATMWFS_OK && cudaMemcpy(h, acc, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "D2H failed");
+    if (s == ATMWFS_OK) {
+        // C = 10^(mean over lags (1..2)^2 of log10 D - 5/3 log10 r)  (:795-816)
+        for (int part = 0; part < 2; part++) {
+            double v = 0.0;
+            for (int q = 0; q < 4; q++) {
+                const int lx = 1 + (q & 1), ly = 1 + (q >> 1);
+                const double D = h[part * 4 + q] / (double)n;
+                v += log10(D) - 5.0 / 3.0 * log10(sqrt((double)(lx * lx + ly * ly)));
+            }
+            C12[part] = pow(10.0, v / 4.0);
+        }
+        if (split_scale(F, (long)n, 1.0 / sqrt(C12[0]), 1.0 / sqrt(C12[1]), o1, o2, st) != cudaSuccess)
+            s = fail(ATMWFS_ERR_CUDA, "scale kernel failed");
+    }
+    if (s == ATMWFS_OK && out1 && cudaMemcpy(out1, o1, n * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "D2H failed");
+    if (s == ATMWFS_OK && out2 && cudaMemcpy(out2, o2, n * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "D2H failed");
+    if (s == ATMWFS_OK && cfit) { cfit[0] = C12[0]; cfit[1] = C12[1]; }
+    cudaFree(C); cudaFree(F); cudaFree(acc); cudaFree(o1); cudaFree(o2);
+    return s;
+}
+
+}  // extern "C"

@@ -1,0 +1,116 @@
+// engine.cuh -- device-side data structures of the wavefront-series engine.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fft_core.cuh"
+
+namespace atmwfs {
+
+constexpr int kMaxLayers = 16;
+
+// Integer and fractional sample position of one layer window for one
+// instance at one step, in the screen's own (untransposed) frame:
+// pixel (ii, jj) of the window samples the screen at (ix + fx + ii, iy + fy + jj).
+struct LayerPos {
+    int ix, iy;
+    float fx, fy;
+};
+
+// One (wavelength, direction, output-mode) instance.
+struct InstDev {
+    float2* fld[2];            // ping-pong N x N fields
+    const float2* H;           // hop transfer tables, [P][N], 1-D, include 1/N
+    float scoeff[kMaxLayers];  // per-layer phase multiplier
+    float* out_pha;            // output ring [ring][Nout*Nout]
+    float* out_amp;
+    float* phisum;             // science scratch: geometric phase sum [Nout*Nout]
+    float* bins;               // science scratch: [2][nb*nb] (re, im) sums
+    float* peak;               // science scratch: unwrapped bin phase [nb*nb]
+    const short* binx;         // bin index of each output coordinate [Nout]
+    int N, Nout, off, nb;
+    int mode;                  // kModeRef / kModeSci / kModePhase
+    int ring;                  // output frames kept on the device
+    int gidx;                  // global instance index (positions, scratch)
+};
+
+enum : int { kModeRef = 0, kModeSci = 1, kModePhase = 2 };
+
+// Operation flags of a row pass.
+enum : int {
+    OP_LOAD = 1,       // read the field (else start from 1 + 0i)
+    OP_PROP1 = 2,      // 1-D Fresnel propagation along the rows (table hop1)
+    OP_GATHER = 4,     // apply the phase screens of layers [g_lo, g_hi)
+    OP_PROP2 = 8,      // 1-D Fresnel propagation along the rows (table hop2)
+    OP_STORE_T = 16,   // store transposed
+    OP_EPI = 32,       // output epilogue (crop, phase sum, amplitude, phase)
+    OP_FFT_FWD = 64,   // unit: forward 1-D FFT only
+    OP_FFT_INV = 128,  // unit: inverse 1-D FFT only
+};
+
+constexpr int kVarFirst = OP_GATHER | OP_PROP2 | OP_STORE_T;
+constexpr int kVarMid = OP_LOAD | OP_PROP1 | OP_GATHER | OP_PROP2 | OP_STORE_T;
+constexpr int kVarLast = OP_LOAD | OP_PROP1 | OP_GATHER | OP_EPI;
+constexpr int kVarSingle = OP_GATHER | OP_EPI;
+constexpr int kVarUnitProp = OP_LOAD | OP_PROP2 | OP_STORE_T;
+constexpr int kVarUnitFwd = OP_LOAD | OP_FFT_FWD | OP_STORE_T;
+constexpr int kVarUnitInv = OP_LOAD | OP_FFT_INV | OP_STORE_T;
+
+// Status bits written by kernels.
+enum : unsigned {
+    kStatTmaTimeout = 1u,
+    kStatBadArg = 2u,
+    kStatUnwrapTimeout = 4u,
+};
+
+struct PassArgs {
+    const InstDev* inst;       // instances of this launch (blockIdx.y), or null (unit path)
+    const LayerPos* pos;       // [poscap][ninst_total][L]
+    const int* d_step;         // current step (device counter), may be null
+    unsigned* d_status;        // error bits
+    int L, ninst_total, poscap;
+    int g_lo, g_hi;            // layers gathered by OP_GATHER
+    int hop1, hop2;            // transfer table index for PROP1 / PROP2
+    int src, dst;              // field buffer index
+    int orient;                // 0: rows are screen rows; 1: rows are screen columns
+    int row0;                  // first row handled by blockIdx.x == 0
+    // unit path (inst == null)
+    const float2* ext_in;
+    float2* ext_out;
+    const float2* H1;
+    const float2* H2;
+};
+
+// Tensor maps of the halo-padded screens: [orientation][layer].
+struct TmaSet {
+    CUtensorMap m[2][kMaxLayers];
+};
+
+// Padded screen geometry: Pad[yp][xp] = S[(yp - kPadY) mod M][(xp - kPadX) mod M]
+// (and the transposed copy with the roles of the axes exchanged).
+constexpr int kPadX = 4;
+constexpr int kPadY = 1;
+constexpr int kBoxW = 32;  // TMA box width (floats)
+
+// Host-side launch entry of one row pass for grid size N (defined per N).
+typedef cudaError_t (*PassLauncher)(int var, dim3 grid, const PassArgs& a, const TmaSet* maps,
+                                    const float2* tw, cudaStream_t st);
+
+// Rows per CTA used for grid size N.
+inline int rows_per_cta(int N)
+{
+    switch (N) {
+        case 64: return 32;
+        case 128: return 32;
+        case 256: return 16;
+        case 512: return 16;
+        case 1024: return 8;
+        case 2048: return 4;
+        default: return 0;
+    }
+}
+
+PassLauncher pass_launcher(int N);
+
+}  // namespace atmwfs

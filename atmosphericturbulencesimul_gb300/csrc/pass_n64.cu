@@ -1,0 +1,9 @@
+// Row-pass kernels for 64 x 64 grids.
+#include "pass_impl.cuh"
+
+namespace atmwfs {
+cudaError_t launch_pass_64(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
+{
+    return launch_pass_n<64>(var, grid, a, maps, tw, st);
+}
+}  // namespace atmwfs

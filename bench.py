@@ -1,0 +1,325 @@
+#!/usr/bin/env python3
+"""Wavefront-series benchmark: frames/s per (wavelength, direction) instance.
+
+Default workload ("batched"): the 7-layer profile (0, 0.5, 1, 2, 4, 8, 16 km;
+Cn2 0.45/0.15/0.10/0.10/0.08/0.07/0.05; seeded winds 5-30 m/s, seeded
+directions), 2048^2 float32 master screens, 16 wavelengths log-spaced
+0.5-2.4 um x 9 directions (3 x 3 grid, 10 arcsec spacing) = 144 instances
+with seeded propagation grids from {256, 512, 1024}, science output with
+the bin unwrap; one step = one frame of every instance.
+
+  value : frames/s with screens and state resident in HBM (CUDA events on
+          the engine stream around K steps);
+  e2e   : the same through the C ABI with host buffers: per-step H2D of the
+          layer positions and D2H of every frame (pha + amp) into pinned memory.
+Multi-GPU (torchrun): every rank runs its own replica of the workload
+(weak scaling, no collective on the data path).
+
+--impl reference times the reference's float path as restated by the CPU
+oracle port (the reference itself needs FFTW/GSL/cfitsio, absent here) on
+all host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+ARCSEC = np.pi / 180.0 / 3600.0
+
+
+def workload(name: str, seed: int = 0) -> dict:
+    rng = np.random.default_rng(seed)
+    alt = [0.0, 500.0, 1000.0, 2000.0, 4000.0, 8000.0, 16000.0]
+    cn2 = [0.45, 0.15, 0.10, 0.10, 0.08, 0.07, 0.05]
+    speed = list(rng.uniform(5.0, 30.0, 7))
+    direction = list(rng.uniform(0.0, 2 * np.pi, 7))
+    base = dict(alt=alt, cn2=cn2, speed=speed, direction=direction, M=2048, pupil=0.01, dt=0.001,
+                lam_ref=0.5e-6, seeing=0.5e-6 / 0.15 / ARCSEC, fresnel_bin=100.0, L0=20.0, l0=0.01)
+    if name == "batched":
+        lams = list(0.5e-6 * (2.4 / 0.5) ** (np.arange(16) / 15.0))
+        dirs = [(dx * 10 * ARCSEC, dy * 10 * ARCSEC) for dy in (-1, 0, 1) for dx in (-1, 0, 1)]
+        sizes = list(rng.choice([256, 512, 1024], size=len(lams) * len(dirs)))
+        inst = []
+        k = 0
+        for d in dirs:
+            for lam in lams:
+                inst.append(dict(lam=float(lam), src=d, W=int(sizes[k])))
+                k += 1
+        base.update(name="batched: 7 layers, 2048^2 screens, 16 lambda x 9 directions, W mixed 256/512/1024",
+                    inst=inst, steps_nominal=5000)
+    elif name == "multilayer":
+        inst = [dict(lam=l, src=(0.0, 0.0), W=512) for l in (0.5e-6, 0.8e-6, 1.25e-6, 2.2e-6)]
+        base.update(name="multilayer: 7 layers, 2048^2 screens, 512^2 pupils, 4 lambda, on-axis", inst=inst,
+                    steps_nominal=2000)
+    elif name == "w1024":
+        inst = [dict(lam=l, src=(0.0, 0.0), W=1024) for l in (0.5e-6, 0.8e-6, 1.25e-6, 2.2e-6)]
+        base.update(name="w1024: 7 layers, 2048^2 screens, 1024^2 pupils, 4 lambda, on-axis", inst=inst,
+                    steps_nominal=2000)
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return base
+
+
+def make_series(wl: dict, ring: int = 1):
+    from atmosphericturbulencesimul_gb300 import MODE_SCI, InstanceSpec, Series, master_screen
+    from atmosphericturbulencesimul_gb300.refractivity import scoeff
+    L = len(wl["alt"])
+    specs = [InstanceSpec(lam=I["lam"], mode=MODE_SCI, src_x=I["src"][0], src_y=I["src"][1], wf_raw_size=I["W"],
+                          wf_size=I["W"], scoeff=scoeff(wl["lam_ref"], I["lam"], L)) for I in wl["inst"]]
+    s = Series(wl["alt"], wl["cn2"], wl["speed"], wl["direction"], master_size=wl["M"], instances=specs,
+               pupil_scale=wl["pupil"], time_step=wl["dt"], fresnel_bin=wl["fresnel_bin"], ring=ring)
+    M = wl["M"]
+    screens = []
+    for l in range(L):
+        s1, _, _ = master_screen(1000 + l, M, wl["L0"] / wl["pupil"], wl["l0"] / wl["pupil"])
+        screens.append(s1)
+        s.load_screen(l, s1)
+    s.normalize(np.float32(wl["lam_ref"]), np.float32(wl["seeing"]))
+    return s, screens
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = [r for r in csv.reader(io.StringIO(getattr(self, "out", "") or "")) if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def cpu_port_sample(wl: dict, screens, threads: int, frames_per_class: int = 1, budget_s: float = 30.0):
+    """Time the oracle's float port of the reference loop (one frame per grid
+    class present in the workload) and extrapolate to the workload's mix."""
+    from oracle import oracle as orc
+    from atmosphericturbulencesimul_gb300.refractivity import scoeff
+    o32 = orc.Oracle(32)
+    o32.set_threads(threads)
+    L = len(wl["alt"])
+    cn2 = np.asarray(wl["cn2"]) / np.sum(wl["cn2"])
+    salt, sidx = o32.superlayers(wl["alt"], cn2, wl["fresnel_bin"])
+    classes = sorted({I["W"] for I in wl["inst"]})
+    t_class = {}
+    t0all = time.perf_counter()
+    for W in classes:
+        I = next(i for i in wl["inst"] if i["W"] == W)
+        x, y, vx, vy = orc.init_positions(wl["M"], wl["alt"], wl["speed"], wl["direction"], wl["pupil"], *I["src"])
+        xc, yc = [0] * L, [0] * L
+        ts = []
+        for _ in range(frames_per_class):
+            orc.step_positions(x, y, xc, yc, vx, vy, wl["dt"], wl["M"])
+            t0 = time.perf_counter()
+            ph, fld = o32.frame(screens, x, y, scoeff(wl["lam_ref"], I["lam"], L).astype(np.float64), sidx, salt,
+                                float(np.float32(wl["pupil"])), 0.0, I["lam"], W)
+            o32.output_sci(ph, fld, W)
+            ts.append(time.perf_counter() - t0)
+            if time.perf_counter() - t0all > budget_s:
+                break
+        t_class[W] = float(np.mean(ts))
+    counts = {W: sum(1 for i in wl["inst"] if i["W"] == W) for W in classes}
+    t_step = sum(counts[W] * t_class[W] for W in classes)
+    fps = len(wl["inst"]) / t_step
+    sample = ", ".join(f"{frames_per_class} frame(s) at {W}^2 ({t_class[W]*1e3:.0f} ms)" for W in classes)
+    return fps, sample
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="batched")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    wl = workload(args.workload)
+    metric = "wavefront frames/s (7 layers,1024^2,per lambda-dir) surrogate vs plain at <=1nm rms"
+    cfg = {"workload": wl["name"], "instances": len(wl["inst"]), "layers": len(wl["alt"]),
+           "master": wl["M"], "grids": {str(W): sum(1 for i in wl["inst"] if i["W"] == W)
+                                         for W in sorted({i["W"] for i in wl["inst"]})},
+           "hops": 6, "path": "plain (Fresnel, FP32)", "l2": "inputs larger than L2 (screens + fields > 1 GB)",
+           "parallelism": f"replicas x{args.gpus}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import torch  # noqa: F401  (not used: CPU arm)
+        from atmosphericturbulencesimul_gb300 import master_screen
+        threads = os.cpu_count() or 1
+        screens = [master_screen(1000 + l, wl["M"], wl["L0"] / wl["pupil"], wl["l0"] / wl["pupil"])[0]
+                   if _has_gpu() else np.random.default_rng(l).standard_normal((wl["M"], wl["M"])).astype(np.float32)
+                   for l in range(len(wl["alt"]))]
+        for _ in range(args.warmup):
+            pass
+        vals = []
+        for _ in range(args.steps):
+            fps, sample = cpu_port_sample(wl, screens, threads, 1, 20.0)
+            vals.append(fps)
+        v = float(np.mean(vals))
+        line = {"metric": metric, "value": v, "unit": "frames/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * len(wl["inst"]) / v, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded screens)",
+                "config": cfg, "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
+                                 "sample": "per step: " + sample + "; extrapolated to the workload mix"},
+                "e2e": {"value": v, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    s, screens = make_series(wl)
+    ninst = len(wl["inst"])
+    L = len(wl["alt"])
+    # warm-up (also captures the step graph)
+    s.run(args.warmup)
+    stream = torch.cuda.ExternalStream(s.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    # device-resident throughput
+    barrier()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        s.run(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    t = e0.elapsed_time(e1) / 1e3
+    tt = torch.tensor([t], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    t = float(tt.item())
+    value = args.steps * ninst * world / t
+
+    # end to end through the C ABI with host buffers
+    ff = s.frame_floats
+    nslots = 2
+    pha_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
+    amp_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
+    barrier()
+    w0 = time.perf_counter()
+    s.run(args.steps, pha_ptr=pha_h.data_ptr(), amp_ptr=amp_h.data_ptr(), nslots=nslots)
+    torch.cuda.synchronize()
+    we = time.perf_counter() - w0
+    te = torch.tensor([we], dtype=torch.float64, device="cuda")
+    if dist:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e = args.steps * ninst * world / float(te.item())
+
+    # roofline of the dominant pass (timed live on the engine stream)
+    npl = len(s.planes()[0])
+    passes = []
+    for c in range(s.num_classes()):
+        for k in range(1, npl + 1):
+            r = s.time_pass(k, c, reps=5)
+            r.update(k=k, c=c)
+            passes.append(r)
+    tot = sum(p["ms"] for p in passes)
+    dom = max(passes, key=lambda p: p["ms"])
+    pk = peaks()
+    achieved = dom["bytes"] / (dom["ms"] * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(f"pass{dom['k']}_n{dom['n']}")
+        except Exception:
+            traffic = None
+    roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
+            "kernel": f"k_pass N={dom['n']} pass {dom['k']}/{npl} ({dom['count']} instances)",
+            "algorithmic_bytes": dom["bytes"], "ms": round(dom["ms"], 4), "share_of_passes": round(dom["ms"] / tot, 3),
+            "peak_source": pk["source"]}
+    launches = npl * s.num_classes() + 3
+
+    line = {"metric": metric, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox screens)",
+            "config": cfg, "clocks": clk.summary(),
+            "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": ninst * L * 16,
+                    "d2h_bytes_per_step": 2 * ff * 4},
+            "gpu_launches": launches * args.steps, "roofline": roof}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        fps, sample = cpu_port_sample(wl, screens, threads, 1, 25.0)
+        line["cpu_baseline"] = {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
+                                "sample": sample + "; extrapolated to the workload mix"}
+    s.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def _has_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,212 @@
+// pass_emul.cpp -- thread-by-thread CPU emulation of the engine's in-CTA
+// building blocks (the same template code the kernels instantiate):
+//   * Stockham FFT stages for every supported N (forward, inverse and the
+//     forward -> transfer -> inverse row propagation);
+//   * the TMA tile geometry of the screen gather and the separable bicubic,
+//     against a direct periodic Keys bicubic in double.
+// Prints one line per check: "<name> <max error>"; exit code 0.
+#include <array>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "fft_core.cuh"
+#include "gather_core.cuh"
+
+using namespace atmwfs;
+using cd = std::complex<double>;
+
+static unsigned long long g_rng = 88172645463325252ull;
+static double urand()
+{
+    g_rng ^= g_rng << 13;
+    g_rng ^= g_rng >> 7;
+    g_rng ^= g_rng << 17;
+    return (double)(g_rng >> 11) * (1.0 / 9007199254740992.0);
+}
+
+template <int N, int T, int E, int D, int NS, int R, int... Rest>
+void emu_stages(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw)
+{
+    for (int t = 0; t < T; t++) {
+        stage_twiddle<N, T, E, R, NS, D>(V[t].data(), t, tw);
+        stage_dft<E, R, D>(V[t].data());
+    }
+    if constexpr (sizeof...(Rest) > 0) {
+        for (int t = 0; t < T; t++) stage_store<N, T, E, R, NS>(V[t].data(), buf, t);
+        for (int t = 0; t < T; t++) stage_load<N, T, E, FirstRadix<Rest...>::value>(V[t].data(), buf, t);
+        emu_stages<N, T, E, D, NS * R, Rest...>(V, buf, tw);
+    }
+}
+
+template <int N, int T, int E, int D, int... Rs>
+void emu_fft(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw, Radices<Rs...>)
+{
+    emu_stages<N, T, E, D, 1, Rs...>(V, buf, tw);
+}
+
+template <int... Rs>
+constexpr int lastr(Radices<Rs...>) { return LastRadix<Rs...>::value; }
+
+static std::vector<cd> dft(const std::vector<cd>& x, int sign)
+{
+    const int n = (int)x.size();
+    std::vector<cd> X(n);
+    for (int k = 0; k < n; k++) {
+        cd s = 0;
+        for (int j = 0; j < n; j++) {
+            const long m = ((long)j * k) % n;
+            const double a = sign * 2.0 * M_PI * (double)m / n;
+            s += x[j] * cd(cos(a), sin(a));
+        }
+        X[k] = s;
+    }
+    return X;
+}
+
+template <int N>
+void check_fft()
+{
+    constexpr int T = Plan<N>::T, E = Plan<N>::E;
+    std::vector<float2> tw(N);
+    for (int k = 0; k < N; k++) tw[k] = make_float2((float)cos(-2 * M_PI * k / N), (float)sin(-2 * M_PI * k / N));
+    std::vector<float2> buf(padi(N) + 64);
+    std::vector<cd> x(N);
+    for (int i = 0; i < N; i++) x[i] = cd(urand() - 0.5, urand() - 0.5);
+    using FR = typename FwdRadices<N>::type;
+    using IR = typename InvRadices<N>::type;
+    constexpr int RL = lastr(FR{});
+    for (int D : {-1, +1}) {
+        std::vector<std::array<float2, E>> V(T);
+        for (int t = 0; t < T; t++)
+            for (int e = 0; e < E; e++) V[t][e] = make_float2((float)x[t + e * T].real(), (float)x[t + e * T].imag());
+        if (D < 0) emu_fft<N, T, E, -1>(V, buf.data(), tw.data(), FR{});
+        else emu_fft<N, T, E, +1>(V, buf.data(), tw.data(), FR{});
+        std::vector<cd> X = dft(x, D);
+        double err = 0, nrm = 0;
+        std::vector<int> seen(N, 0);
+        for (int t = 0; t < T; t++)
+            for (int s = 0; s < E; s++) {
+                const int k = last_index<N, T, RL>(t, s);
+                seen[k]++;
+                err = fmax(err, std::abs(cd(V[t][s].x, V[t][s].y) - X[k]));
+                nrm = fmax(nrm, std::abs(X[k]));
+            }
+        for (int k = 0; k < N; k++)
+            if (seen[k] != 1) { printf("fft%s_%d_coverage 1e9\n", D < 0 ? "fwd" : "inv", N); return; }
+        printf("fft%s_%d %.3e\n", D < 0 ? "fwd" : "inv", N, err / nrm);
+    }
+    // propagation: forward, multiply by a unit-modulus table, inverse
+    std::vector<float2> h(N);
+    std::vector<cd> hd(N);
+    for (int k = 0; k < N; k++) {
+        const double a = 2 * M_PI * urand();
+        hd[k] = cd(cos(a), sin(a)) / (double)N;
+        h[k] = make_float2((float)hd[k].real(), (float)hd[k].imag());
+    }
+    std::vector<std::array<float2, E>> V(T);
+    for (int t = 0; t < T; t++)
+        for (int e = 0; e < E; e++) V[t][e] = make_float2((float)x[t + e * T].real(), (float)x[t + e * T].imag());
+    emu_fft<N, T, E, -1>(V, buf.data(), tw.data(), FR{});
+    for (int t = 0; t < T; t++)
+        for (int s = 0; s < E; s++) V[t][s] = cmul(V[t][s], h[last_index<N, T, RL>(t, s)]);
+    emu_fft<N, T, E, +1>(V, buf.data(), tw.data(), IR{});
+    std::vector<cd> X = dft(x, -1);
+    for (int k = 0; k < N; k++) X[k] *= hd[k];
+    std::vector<cd> y = dft(X, +1);
+    double err = 0, nrm = 0;
+    for (int t = 0; t < T; t++)
+        for (int e = 0; e < E; e++) {
+            err = fmax(err, std::abs(cd(V[t][e].x, V[t][e].y) - y[t + e * T]));
+            nrm = fmax(nrm, std::abs(y[t + e * T]));
+        }
+    printf("prop_%d %.3e\n", N, err / nrm);
+}
+
+// ---------------------------------------------------------------------------
+// gather: padded periodic screen, TMA box layout, separable bicubic
+// ---------------------------------------------------------------------------
+static double keys(double t, int k)
+{
+    const double t2 = t * t, t3 = t2 * t;
+    switch (k) {
+        case 0: return 0.5 * (-t3 + 2 * t2 - t);
+        case 1: return 0.5 * (3 * t3 - 5 * t2 + 2);
+        case 2: return 0.5 * (-3 * t3 + 4 * t2 + t);
+        default: return 0.5 * (t3 - t2);
+    }
+}
+
+template <int N>
+void check_gather(int M, int ix, int iy, float fx, float fy, int orient, int y0)
+{
+    constexpr int RR = N == 64 || N == 128 ? 32 : N == 256 || N == 512 ? 16 : N == 1024 ? 8 : 4;
+    constexpr int NT = Plan<N>::T * RR;
+    constexpr int TROWS = RR + 3, NBOX = N / kBoxW + 1;
+    std::vector<float> S((size_t)M * M);
+    for (auto& v : S) v = (float)(urand() * 20 - 10);
+    const int Wp = M + N + 64, Hp = M + N + 8;
+    // padded copy, as k_pad_screen
+    std::vector<float> P((size_t)Wp * Hp);
+    for (int yp = 0; yp < Hp; yp++)
+        for (int xp = 0; xp < Wp; xp++) {
+            const int a = ((yp - kPadY) % M + M) % M, b = ((xp - kPadX) % M + M) % M;
+            P[(size_t)yp * Wp + xp] = orient ? S[(size_t)b * M + a] : S[(size_t)a * M + b];
+        }
+    LayerPos p{ix, iy, fx, fy};
+    const TileGeom g = tile_geom(p, orient, y0);
+    std::vector<float> tile((size_t)NBOX * TROWS * kBoxW);
+    bool inb = true;
+    for (int k = 0; k < NBOX; k++)
+        for (int r = 0; r < TROWS; r++)
+            for (int c = 0; c < kBoxW; c++) {
+                const int xp = g.xs + k * kBoxW + c, yp = g.ys + r;
+                if (xp < 0 || yp < 0 || xp >= Wp || yp >= Hp) { inb = false; continue; }
+                tile[((size_t)k * TROWS + r) * kBoxW + c] = P[(size_t)yp * Wp + xp];
+            }
+    std::vector<float> out((size_t)RR * N, NAN);
+    for (int tid = 0; tid < NT; tid++)
+        gather_tile<N, RR, NT>(tile.data(), g, 1.0f, tid, [&](int r, int x, float v) { out[(size_t)r * N + x] = v; });
+    double err = 0;
+    for (int r = 0; r < RR; r++)
+        for (int x = 0; x < N; x++) {
+            // pass coordinates (row y0 + r, column x) -> screen sample
+            const int row = y0 + r;
+            double X, Y;
+            if (orient == 0) { X = ix + (double)fx + x; Y = iy + (double)fy + row; }
+            else { X = ix + (double)fx + row; Y = iy + (double)fy + x; }
+            const long xi = (long)floor(X), yi = (long)floor(Y);
+            const double tx = X - xi, ty = Y - yi;
+            double v = 0;
+            for (int b = 0; b < 4; b++)
+                for (int a = 0; a < 4; a++) {
+                    const long sx = ((xi - 1 + a) % M + M) % M, sy = ((yi - 1 + b) % M + M) % M;
+                    v += keys(tx, a) * keys(ty, b) * S[(size_t)sy * M + sx];
+                }
+            err = fmax(err, fabs(v - out[(size_t)r * N + x]));
+        }
+    printf("gather_%d_o%d_ix%d_iy%d %.3e\n", N, orient, ix, iy, inb ? err : 1e9);
+}
+
+int main()
+{
+    check_fft<64>();
+    check_fft<128>();
+    check_fft<256>();
+    check_fft<512>();
+    check_fft<1024>();
+    check_fft<2048>();
+    const int M = 512;
+    for (int orient = 0; orient < 2; orient++) {
+        check_gather<64>(M, 0, 0, 0.25f, 0.75f, orient, 32);
+        check_gather<128>(M, M - 1, M - 2, 0.5f, 0.125f, orient, 96);
+        check_gather<256>(M, 7, M - 1, 0.9f, 0.01f, orient, 240);
+        check_gather<512>(M, M - 3, 5, 0.3f, 0.6f, orient, 496);
+        check_gather<1024>(M, 13, M - 7, 0.77f, 0.33f, orient, 1016);
+        check_gather<2048>(M, M - 1, M - 1, 0.999f, 0.001f, orient, 2044);
+        check_gather<1024>(M, 2, 3, 0.0f, 0.0f, orient, 0);
+    }
+    return 0;
+}

@@ -1,0 +1,132 @@
+"""Seeded small wavefront-series cases run through the GPU engine and the
+FP64 oracle with identical inputs (screens, positions, Scoeff), plus the
+error metrics used by the parity tests."""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from oracle import oracle as orc
+
+
+@dataclass
+class Case:
+    alt: list
+    cn2: list
+    speed: list
+    direction: list
+    M: int = 256
+    W: int = 128
+    Wout: int = 128
+    fresnel_bin: float = 100.0
+    pupil: float = 0.01
+    dt: float = 0.001
+    zangle: float = 0.0
+    lam_ref: float = 0.5e-6
+    seeing: float = 0.6875
+    sci: list = field(default_factory=lambda: [(1.6e-6, 0.0, 0.0)])  # (lambda, src_x, src_y)
+    ref: bool = True
+    amplitude: int = 1
+    fresnel: int = 1
+    seed: int = 7
+
+
+def make_screens(case: Case, o64) -> list[np.ndarray]:
+    """Seeded master screens (the oracle's synthesis of Philox noise), then the
+    reference's r0 renormalisation and Cn2 weights in float storage."""
+    L = len(case.alt)
+    o32 = orc.Oracle(32)
+    screens = []
+    for l in range(L):
+        u, g = o64.screen_noise(case.seed, l, case.M)
+        s1, _, _ = o32.master_screen(u, g, 20.0 / case.pupil, 0.01 / case.pupil)
+        screens.append(s1.astype(np.float32))
+    cn2 = np.asarray(case.cn2, float)
+    cn2 = cn2 * (1.0 / cn2.sum())
+    orc.r0_renormalise(o32, screens, np.float32(case.lam_ref), np.float32(case.seeing), np.float32(case.pupil), cn2,
+                       np.float32(case.zangle))
+    return screens
+
+
+def scoeff_for(case: Case, lam: float) -> np.ndarray:
+    """A deterministic stand-in for CONF_LAMBDA/SLAMBDA * N(h,lam)/N(h,lam_ref):
+    the vacuum ratio times a mild altitude-dependent dispersion factor."""
+    L = len(case.alt)
+    disp = 1.0 - 2e-3 * (1.0 - case.lam_ref / lam) * np.exp(-np.asarray(case.alt) / 8000.0)
+    return (np.float32(case.lam_ref) / lam * disp).astype(np.float32) * np.ones(L, np.float32)
+
+
+def instances(case: Case):
+    from atmosphericturbulencesimul_gb300 import MODE_PHASE, MODE_REF, MODE_SCI, InstanceSpec
+    out = []
+    if case.ref:
+        mode = MODE_REF if case.amplitude else MODE_PHASE
+        out.append(InstanceSpec(lam=float(np.float32(case.lam_ref)), mode=mode, wf_raw_size=case.W, wf_size=case.Wout))
+    for lam, sx, sy in case.sci:
+        mode = MODE_SCI if case.amplitude else MODE_PHASE
+        out.append(InstanceSpec(lam=lam, mode=mode, src_x=sx, src_y=sy, wf_raw_size=case.W, wf_size=case.Wout,
+                                scoeff=scoeff_for(case, lam)))
+    return out
+
+
+def run_gpu(case: Case, screens, nsteps: int):
+    from atmosphericturbulencesimul_gb300 import Series
+    inst = instances(case)
+    s = Series(case.alt, case.cn2, case.speed, case.direction, master_size=case.M, instances=inst,
+               pupil_scale=case.pupil, time_step=case.dt, fresnel_bin=case.fresnel_bin, zangle=case.zangle,
+               amplitude=case.amplitude, fresnel=case.fresnel)
+    for l, sc in enumerate(screens):
+        s.load_screen(l, sc)
+    frames = s.run_frames(nsteps)
+    pos = [s.positions(i) for i in range(len(inst))]
+    planes = s.planes()
+    s.close()
+    return inst, frames, pos, planes
+
+
+def run_oracle(case: Case, o64, screens, nsteps: int):
+    """Per step, per instance (pha, amp) from the FP64 oracle."""
+    inst = instances(case)
+    cn2 = np.asarray(case.cn2, float)
+    cn2 = cn2 * (1.0 / cn2.sum())
+    salt, sidx = o64.superlayers(case.alt, cn2, case.fresnel_bin)
+    res = []
+    states = []
+    for I in inst:
+        x, y, vx, vy = orc.init_positions(case.M, case.alt, case.speed, case.direction, case.pupil, I.src_x, I.src_y)
+        states.append([x, y, [0] * len(x), [0] * len(x), vx, vy])
+    for _ in range(nsteps):
+        step = []
+        for I, st in zip(inst, states):
+            orc.step_positions(st[0], st[1], st[2], st[3], st[4], st[5], case.dt, case.M)
+            sc = None if I.scoeff is None else I.scoeff.astype(np.float64)
+            phasum, fld = o64.frame(screens, st[0], st[1], sc, sidx, salt, float(np.float32(case.pupil)),
+                                    float(np.float32(case.zangle)), I.lam, case.W, case.amplitude, case.fresnel)
+            from atmosphericturbulencesimul_gb300 import MODE_SCI
+            if I.mode == MODE_SCI:
+                pha, amp, _, _ = o64.output_sci(phasum, fld, case.Wout, case.amplitude)
+            else:
+                pha, amp = o64.output_ref(phasum, fld, case.Wout, case.amplitude)
+            step.append((pha, amp))
+        res.append(step)
+    final_pos = [(st[0].copy(), st[1].copy()) for st in states]
+    return inst, res, final_pos, (salt, sidx)
+
+
+def metrics(pha_g, amp_g, pha_o, amp_o, lam):
+    """Error metrics of one frame against the oracle."""
+    d = pha_g.astype(np.float64) - pha_o.astype(np.float64)
+    wrapped = np.angle(np.exp(1j * d))
+    flips = np.abs(d - wrapped) > 1.0
+    nm = lam / (2 * np.pi) * 1e9
+    opd_g = pha_g.astype(np.float64) * lam / (2 * np.pi)
+    opd_o = pha_o.astype(np.float64) * lam / (2 * np.pi)
+    return {
+        "wrapped_rms_nm": float(np.sqrt(np.mean(wrapped ** 2)) * nm),
+        "opd_rms_err_nm": float(np.sqrt(np.mean(d ** 2)) * nm),
+        "flip_frac": float(flips.mean()),
+        "amp_max_err": float(np.max(np.abs(amp_g.astype(np.float64) - amp_o))),
+        "opd_rms_rel": float(abs(opd_g.std() - opd_o.std()) / max(opd_o.std(), 1e-30)),
+        "amp_var_rel": float(abs(amp_g.var() - amp_o.var()) / max(amp_o.var(), 1e-30)),
+    }

@@ -1,0 +1,125 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the FP64 oracle and numpy.
+
+Tolerances (floating point, FP32 engine vs FP64 oracle):
+  * 2-D FFT: relative max error <= 2e-5 (FP32 Stockham, log2 N stages);
+  * Fresnel hop: relative max error <= 2e-5;
+  * series frames: wrapped phase error <= 0.05 nm rms, amplitude error <= 2e-3,
+    and (the reference's bar) relative OPD rms and amplitude variance within 1e-4;
+    the unwrapped phase may differ by a 2 pi jump on at most 0.2 % of the pixels.
+"""
+import numpy as np
+import pytest
+
+from series_case import Case, make_screens, metrics, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fft2d_matches_numpy(lib, n, sign):
+    from atmosphericturbulencesimul_gb300 import fft2d
+    rng = np.random.default_rng(n)
+    a = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    got = fft2d(a, sign)
+    ref = np.fft.fft2(a.astype(np.complex128)) if sign < 0 else np.fft.ifft2(a.astype(np.complex128)) * n * n
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 2e-5, err
+
+
+@pytest.mark.parametrize("n,z,lam", [(128, 5000.0, 0.5e-6), (256, 8000.0, 2.2e-6), (1024, 500.0, 1.6e-6)])
+def test_fresnel_matches_oracle(lib, oracle64, n, z, lam):
+    from atmosphericturbulencesimul_gb300 import fresnel
+    rng = np.random.default_rng(n)
+    ph = rng.standard_normal((n, n)) * 3
+    a = np.exp(1j * ph).astype(np.complex64)
+    dx = float(np.float32(0.01))
+    got = fresnel(a, dx, z, lam)
+    ref = oracle64.fresnel(a.astype(np.complex128), dx, z, lam)
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 2e-5, err
+    # Parseval: the hop conserves energy
+    assert abs(np.sum(np.abs(got) ** 2) / np.sum(np.abs(a) ** 2) - 1) < 1e-5
+
+
+def _compare(case, o64, nsteps, wrapped_nm=0.05, flip=2e-3):
+    screens = make_screens(case, o64)
+    inst_g, frames, pos_g, planes = run_gpu(case, screens, nsteps)
+    inst_o, res, pos_o, _ = run_oracle(case, o64, screens, nsteps)
+    # positions follow the reference's sequential update bit for bit
+    for (xg, yg), (xo, yo) in zip(pos_g, pos_o):
+        assert np.array_equal(xg, xo) and np.array_equal(yg, yo)
+    out = []
+    for i, I in enumerate(inst_g):
+        for s in range(nsteps):
+            pha_g, amp_g = frames[i][0][s], frames[i][1][s]
+            pha_o, amp_o = res[s][i]
+            m = metrics(pha_g, amp_g, pha_o, amp_o, I.lam)
+            out.append(m)
+            assert m["wrapped_rms_nm"] < wrapped_nm, (i, s, m)
+            assert m["amp_max_err"] < 2e-3, (i, s, m)
+            assert m["flip_frac"] < flip, (i, s, m)
+            assert m["opd_rms_rel"] < 1e-4 or m["flip_frac"] > 0, (i, s, m)
+            if amp_o.var() > 1e-6:
+                assert m["amp_var_rel"] < 1e-4 * 10, (i, s, m)
+    return out
+
+
+def test_series_three_planes(lib, oracle64):
+    case = Case(alt=[0.0, 2000.0, 8000.0], cn2=[0.6, 0.25, 0.15], speed=[10.0, 20.0, 15.0],
+                direction=[0.5236, 2.0, 4.0], M=256, W=128, Wout=128, fresnel_bin=100.0)
+    _compare(case, oracle64, 4)
+
+
+def test_series_crop_and_grouped_layers(lib, oracle64):
+    # layers at 0 and 50 m share a super-layer; 64-pixel crop of a 128 grid
+    case = Case(alt=[0.0, 50.0, 5000.0, 12000.0], cn2=[0.4, 0.2, 0.3, 0.1], speed=[8.0, 12.0, 25.0, 30.0],
+                direction=[0.1, 1.0, 3.0, 5.5], M=256, W=128, Wout=64, fresnel_bin=100.0,
+                sci=[(1.25e-6, 0.0, 0.0), (2.2e-6, 4.85e-5, -4.85e-5)])
+    _compare(case, oracle64, 3)
+
+
+def test_series_single_layer_no_hop(lib, oracle64):
+    case = Case(alt=[5000.0], cn2=[1.0], speed=[10.0], direction=[0.5236], M=256, W=256, Wout=256)
+    _compare(case, oracle64, 3)
+
+
+def test_series_phase_only(lib, oracle64):
+    case = Case(alt=[0.0, 3000.0], cn2=[0.5, 0.5], speed=[10.0, -20.0], direction=[0.3, 1.2], M=256, W=64,
+                Wout=64, amplitude=0)
+    _compare(case, oracle64, 3)
+
+
+def test_series_large_grid(lib, oracle64):
+    case = Case(alt=[0.0, 4000.0, 16000.0], cn2=[0.5, 0.3, 0.2], speed=[10.0, 20.0, 30.0], direction=[0.5, 2.5, 4.5],
+                M=1024, W=512, Wout=512, fresnel_bin=100.0)
+    _compare(case, oracle64, 2)
+
+
+def test_master_screen_matches_oracle(lib, oracle64):
+    from atmosphericturbulencesimul_gb300 import master_screen
+    M = 256
+    g1, g2, gc = master_screen(11, M, 2000.0, 1.0, stream=3)
+    u, g = oracle64.screen_noise(11, 3, M)
+    o1, o2, oc = oracle64.master_screen(u, g, 2000.0, 1.0)
+    assert np.abs(g1 - o1).max() / np.abs(o1).max() < 1e-4
+    assert np.abs(g2 - o2).max() / np.abs(o2).max() < 1e-4
+    assert np.allclose(gc, oc, rtol=1e-4)
+
+
+def test_normalize_matches_oracle(lib, oracle32):
+    from oracle import oracle as orc
+    from atmosphericturbulencesimul_gb300 import InstanceSpec, Series
+    M = 256
+    rng = np.random.default_rng(5)
+    screens = [rng.standard_normal((M, M)).astype(np.float32) * 5 for _ in range(2)]
+    s = Series([0.0, 1000.0], [0.7, 0.3], [5.0, 5.0], [0.0, 1.0], master_size=M,
+               instances=[InstanceSpec(lam=0.5e-6, wf_raw_size=64)], pupil_scale=0.01, time_step=0.001)
+    for l, sc in enumerate(screens):
+        s.load_screen(l, sc)
+    r0g = s.normalize(np.float32(0.5e-6), np.float32(0.6875))
+    ref = [x.copy() for x in screens]
+    r0o = orc.r0_renormalise(oracle32, ref, np.float32(0.5e-6), np.float32(0.6875), np.float32(0.01),
+                             np.array([0.7, 0.3]), np.float32(0.0))
+    assert np.allclose(r0g, r0o, rtol=1e-6)
+    s.close()
