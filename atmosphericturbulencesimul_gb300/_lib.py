@@ -82,6 +82,8 @@ SIGNATURES = [
     ("atmwfs_num_planes", C.c_int, [_ctx]),
     ("atmwfs_plane_info", C.c_int, [_ctx, _ip, _ip, _dp]),
     ("atmwfs_positions", C.c_int, [_ctx, C.c_int, _dp, _dp]),
+    ("atmwfs_layer_planes", C.c_int, [_dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int, C.c_float, _ip, _dp, _ip,
+                                      _ip, _ip, _ip, _dp]),
     ("atmwfs_stream", C.c_void_p, [_ctx]),
     ("atmwfs_num_classes", C.c_int, [_ctx]),
     ("atmwfs_time_pass", C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip]),

@@ -21,9 +21,13 @@ LIB = PKG / "libatmwfs.so"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code is compiled without floating-point contraction so that the
+# frozen-flow position updates round like the reference's x86 build (an FMA
+# in `pos += v * dt` changes the last bit on Arm hosts).
 NVCC_FLAGS = ["-std=c++17", "--expt-relaxed-constexpr", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-ffp-contract=off",
               "-I", str(INCLUDE), "-I", str(CSRC)]
-CC_FLAGS = ["-std=c11", "-O2", "-fPIC", "-Wall", "-Wno-unused-result", "-I", str(INCLUDE), "-I", str(CSRC)]
+CC_FLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-result", "-I", str(INCLUDE), "-I", str(CSRC)]
 
 
 def _nvcc() -> str:

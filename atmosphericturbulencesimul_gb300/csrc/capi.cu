@@ -149,6 +149,31 @@ static int group_superlayers(const std::vector<double>& alt, const std::vector<d
     return S;
 }
 
+// Propagation planes: runs of layers with one super-layer index met while
+// walking from the top layer down (:2649-2692); hop k goes from plane k to
+// plane k + 1 over (salt[upper] - salt[lower]) / cos(zenith).  Without
+// amplitude or Fresnel propagation all layers share one plane.
+static void build_planes(const std::vector<double>& salt, const std::vector<int>& sidx, int amplitude, int fresnel,
+                         float zangle, std::vector<int>& lo, std::vector<int>& hi, std::vector<double>& hop)
+{
+    const int L = (int)sidx.size();
+    lo.clear(); hi.clear(); hop.clear();
+    if (amplitude && fresnel) {
+        int h = L;
+        for (int l = L - 1; l >= 0; l--) {
+            if (l == 0 || sidx[l - 1] != sidx[l]) {
+                lo.push_back(l);
+                hi.push_back(h);
+                if (l > 0) hop.push_back((salt[sidx[l]] - salt[sidx[l - 1]]) / cos((double)zangle));
+                h = l;
+            }
+        }
+    } else {
+        lo.push_back(0);
+        hi.push_back(L);
+    }
+}
+
 struct Class {
     int N = 0, Nout = 0, RR = 0;
     std::vector<int> members;  // global instance indices
@@ -479,21 +504,7 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
         if (!c->amplitude) c->inst[i].mode = ATMWFS_MODE_PHASE;
     }
     group_superlayers(c->alt, c->cn2, p->fresnel_bin, c->salt, c->sidx);
-    // planes: layer runs met while walking from the top layer down (:2649-2692)
-    if (c->amplitude && c->fresnel) {
-        int hi = c->L;
-        for (int l = c->L - 1; l >= 0; l--) {
-            if (l == 0 || c->sidx[l - 1] != c->sidx[l]) {
-                c->plane_lo.push_back(l);
-                c->plane_hi.push_back(hi);
-                if (l > 0) c->hop_z.push_back((c->salt[c->sidx[l]] - c->salt[c->sidx[l - 1]]) / cos((double)c->zangle));
-                hi = l;
-            }
-        }
-    } else {
-        c->plane_lo.push_back(0);
-        c->plane_hi.push_back(c->L);
-    }
+    build_planes(c->salt, c->sidx, c->amplitude, c->fresnel, c->zangle, c->plane_lo, c->plane_hi, c->hop_z);
     const int P = (int)c->hop_z.size();
     init_positions(c);
 
@@ -772,6 +783,32 @@ atmwfs_status atmwfs_frame_dev(atmwfs_ctx* c, int i, const float** pha, const fl
     const long slot = (c->steps - 1) % c->ring;
     if (pha) *pha = c->d_out_pha + slot * c->frame_floats + c->frame_off[i];
     if (amp) *amp = c->d_out_amp + slot * c->frame_floats + c->frame_off[i];
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_layer_planes(const double* alt, const double* cn2, int L, double fresnel_bin, int amplitude,
+                                  int fresnel, float zangle, int* nsuper, double* salt, int* sidx, int* nplanes,
+                                  int* plane_lo, int* plane_hi, double* hop_z)
+{
+    if (!alt || !cn2 || L < 1) return fail(ATMWFS_ERR_INVALID, "bad profile");
+    std::vector<double> a(alt, alt + L), c2(cn2, cn2 + L), sa;
+    double tot = 0.0;
+    for (double v : c2) tot += v;
+    if (!(tot > 0)) return fail(ATMWFS_ERR_INVALID, "sum of cn2 must be > 0");
+    for (double& v : c2) v *= 1.0 / tot;
+    std::vector<int> si, lo, hi;
+    std::vector<double> hz;
+    const int S = group_superlayers(a, c2, fresnel_bin, sa, si);
+    build_planes(sa, si, amplitude, amplitude ? fresnel : 0, zangle, lo, hi, hz);
+    if (nsuper) *nsuper = S;
+    for (int i = 0; i < S && salt; i++) salt[i] = sa[i];
+    for (int l = 0; l < L && sidx; l++) sidx[l] = si[l];
+    if (nplanes) *nplanes = (int)lo.size();
+    for (size_t k = 0; k < lo.size(); k++) {
+        if (plane_lo) plane_lo[k] = lo[k];
+        if (plane_hi) plane_hi[k] = hi[k];
+        if (hop_z && k < hz.size()) hop_z[k] = hz[k];
+    }
     return ATMWFS_OK;
 }
 

@@ -19,7 +19,7 @@ import numpy as np
 from . import _lib
 from ._lib import MODE_PHASE, MODE_REF, MODE_SCI, check
 
-__all__ = ["Series", "InstanceSpec", "fresnel", "fft2d", "master_screen", "MODE_REF", "MODE_SCI", "MODE_PHASE"]
+__all__ = ["Series", "InstanceSpec", "layer_planes", "fresnel", "fft2d", "master_screen", "MODE_REF", "MODE_SCI", "MODE_PHASE"]
 
 
 def _f32p(a: np.ndarray):
@@ -196,6 +196,26 @@ class Series:
             self.close()
         except Exception:
             pass
+
+
+def layer_planes(alt, cn2, fresnel_bin: float, amplitude: int = 1, fresnel: int = 1, zangle: float = 0.0):
+    """Super-layer grouping and propagation planes (host only, no GPU needed).
+    Returns (super-layer altitudes, layer -> super-layer index, planes [(lo, hi)], hop distances)."""
+    lib = _lib.load()
+    alt = np.ascontiguousarray(alt, np.float64)
+    cn2 = np.ascontiguousarray(cn2, np.float64)
+    L = len(alt)
+    ns, npl = C.c_int(), C.c_int()
+    salt = np.zeros(L)
+    sidx = np.zeros(L, np.int32)
+    lo = np.zeros(L, np.int32)
+    hi = np.zeros(L, np.int32)
+    hz = np.zeros(max(L - 1, 1))
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+    check(lib.atmwfs_layer_planes(_f64p(alt), _f64p(cn2), L, fresnel_bin, amplitude, fresnel, zangle, C.byref(ns),
+                                  _f64p(salt), ip(sidx), C.byref(npl), ip(lo), ip(hi), _f64p(hz)))
+    n = npl.value
+    return salt[:ns.value].copy(), sidx, list(zip(lo[:n].tolist(), hi[:n].tolist())), hz[:max(n - 1, 0)].copy()
 
 
 def fresnel(field_in: np.ndarray, dx: float, z: float, lam: float) -> np.ndarray:

@@ -125,6 +125,14 @@ long atmwfs_steps_done(const atmwfs_ctx* ctx);
 int atmwfs_num_planes(const atmwfs_ctx* ctx);
 atmwfs_status atmwfs_plane_info(const atmwfs_ctx* ctx, int* layer_lo, int* layer_hi, double* hop_z);
 
+/* Host-only (no GPU needed): super-layer grouping of a profile
+ * (AtmosphericTurbulence.c:2067-2147) and the propagation planes the engine
+ * derives from it.  cn2 is normalised internally.  Arrays have room for L
+ * entries (hop_z: L - 1). */
+atmwfs_status atmwfs_layer_planes(const double* alt, const double* cn2, int L, double fresnel_bin, int amplitude,
+                                  int fresnel, float zangle, int* nsuper, double* salt, int* sidx, int* nplanes,
+                                  int* plane_lo, int* plane_hi, double* hop_z);
+
 /* CUDA stream (cudaStream_t) on which the context runs. */
 void* atmwfs_stream(atmwfs_ctx* ctx);
 

@@ -597,15 +597,23 @@ static inline void philox_round(uint32_t c[4], const uint32_t k[2])
     c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
 }
 
-OR_EXPORT void or_philox(uint64_t seed, uint32_t ctr0, uint32_t ctr1, uint32_t out[4])
+/* full-width form: 4-word counter, 2-word key (for the published known-answer vectors) */
+OR_EXPORT void or_philox4(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
 {
-    uint32_t c[4] = {ctr0, ctr1, 0u, 0u};
-    uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t c[4] = {ctr[0], ctr[1], ctr[2], ctr[3]};
+    uint32_t k[2] = {key[0], key[1]};
     for (int r = 0; r < 10; r++) {
         philox_round(c, k);
         if (r < 9) { k[0] += 0x9E3779B9u; k[1] += 0xBB67AE85u; }
     }
     memcpy(out, c, sizeof(c));
+}
+
+OR_EXPORT void or_philox(uint64_t seed, uint32_t ctr0, uint32_t ctr1, uint32_t out[4])
+{
+    const uint32_t c[4] = {ctr0, ctr1, 0u, 0u};
+    const uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    or_philox4(c, k, out);
 }
 
 OR_EXPORT void or_screen_noise(uint64_t seed, uint32_t stream, long M, float *upha, float *gau)

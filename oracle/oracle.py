@@ -61,6 +61,7 @@ class Oracle:
         L.or_measure_r0.restype = C.c_double
         L.or_master_screen.argtypes = [_vp, _vp, C.c_long, C.c_double, C.c_double, _vp, _vp, _dp]
         L.or_philox.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]
+        L.or_philox4.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.or_screen_noise.argtypes = [C.c_uint64, C.c_uint32, C.c_long, _vp, _vp]
 
     # -- basic operators -------------------------------------------------
@@ -158,6 +159,13 @@ class Oracle:
         cf = np.zeros(2)
         self.lib.or_master_screen(_ptr(u), _ptr(g), M, L0pix, l0pix, _ptr(o1), _ptr(o2), cf.ctypes.data_as(_dp))
         return o1, o2, cf
+
+    def philox4(self, ctr, key):
+        c = (C.c_uint32 * 4)(*ctr)
+        k = (C.c_uint32 * 2)(*key)
+        out = (C.c_uint32 * 4)()
+        self.lib.or_philox4(c, k, out)
+        return list(out)
 
     def philox(self, seed: int, c0: int, c1: int):
         out = (C.c_uint32 * 4)()
