@@ -67,6 +67,11 @@ def workload(name: str, seed: int = 0) -> dict:
         inst = [dict(lam=l, src=(0.0, 0.0), W=1024) for l in (0.5e-6, 0.8e-6, 1.25e-6, 2.2e-6)]
         base.update(name="w1024: 7 layers, 2048^2 screens, 1024^2 pupils, 4 lambda, on-axis", inst=inst,
                     steps_nominal=2000)
+    elif name == "prof1024":
+        lams = list(0.5e-6 * (2.4 / 0.5) ** (np.arange(16) / 15.0))
+        inst = [dict(lam=float(l), src=(0.0, 0.0), W=1024) for l in lams]
+        base.update(name="prof1024: 7 layers, 2048^2 screens, 1024^2 pupils, 16 lambda (profiling case)", inst=inst,
+                    steps_nominal=100)
     else:
         raise SystemExit(f"unknown workload {name}")
     return base
