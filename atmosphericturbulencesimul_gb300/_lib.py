@@ -90,6 +90,8 @@ SIGNATURES = [
     ("atmwfs_fresnel", C.c_int, [_fp, _fp, C.c_long, C.c_double, C.c_double, C.c_double]),
     ("atmwfs_fresnel_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_double,
                                      C.c_void_p]),
+    ("atmwfs_fresnel_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_double,
+                                         C.c_void_p]),
     ("atmwfs_fft2d", C.c_int, [_fp, _fp, C.c_long, C.c_int]),
     ("atmwfs_fft2d_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
     ("atmwfs_master_screen", C.c_int, [C.c_uint64, C.c_uint32, C.c_long, C.c_double, C.c_double, _fp, _fp, _dp]),

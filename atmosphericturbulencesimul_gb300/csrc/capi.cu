@@ -51,6 +51,9 @@ static atmwfs_status fail(atmwfs_status s, const char* fmt, ...)
         if (s_ != ATMWFS_OK) return s_;         \
     } while (0)
 
+// Error message for entry points defined in other translation units.
+void set_error_message(const char* msg) { g_err = msg ? msg : ""; }
+
 PassLauncher pass_launcher(int N)
 {
     switch (N) {

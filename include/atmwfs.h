@@ -154,6 +154,23 @@ atmwfs_status atmwfs_fresnel(const float* in, float* out, long n, double dx, dou
 atmwfs_status atmwfs_fresnel_dev(const void* in, void* out, long n, double dx, double z, double lambda,
                                  void* stream);
 
+/* Allocation-free variant of atmwfs_fresnel_dev (no counterpart in the
+ * reference).  For callers that must not allocate device memory while they
+ * run: a real-time loop feeding an adaptive-optics controller cannot call the
+ * CUDA allocator per frame (an allocation or free may wait on the whole
+ * device and takes unbounded time), and a host that gives all device memory
+ * to its own pool at start-up has nothing left to allocate from.  The
+ * intermediate field and tables live in static device arrays of the library
+ * sized for n <= ATMWFS_NOALLOC_MAX_N (2 MiB per GPU that loads the library,
+ * kept until exit); larger n is rejected with ATMWFS_ERR_INVALID.  The first
+ * call on a device looks the arrays up on that device, so make it before any
+ * stream capture.  Every call shares the arrays, which keep the last call's
+ * contents (the first pass overwrites the whole region the second reads):
+ * calls that overlap on the GPU race, so issue them on one stream. */
+#define ATMWFS_NOALLOC_MAX_N 512
+atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long n, double dx, double z, double lambda,
+                                     void* stream);
+
 /* do2dfft / do2dffti (src/fft/fft.c:1298-1315): unnormalised 2-D complex
  * DFT, sign -1 forward, +1 inverse. */
 atmwfs_status atmwfs_fft2d(const float* in, float* out, long n, int sign);
