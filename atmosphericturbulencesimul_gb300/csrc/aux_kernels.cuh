@@ -22,4 +22,17 @@ cudaError_t launch_pass_512(int var, dim3 grid, const PassArgs& a, const TmaSet*
 cudaError_t launch_pass_1024(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
 cudaError_t launch_pass_2048(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
 
+cudaError_t launch_pass_cfg_64(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                                cudaStream_t st);
+cudaError_t launch_pass_cfg_128(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                                cudaStream_t st);
+cudaError_t launch_pass_cfg_256(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                                cudaStream_t st);
+cudaError_t launch_pass_cfg_512(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                                cudaStream_t st);
+cudaError_t launch_pass_cfg_1024(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                                cudaStream_t st);
+cudaError_t launch_pass_cfg_2048(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                                cudaStream_t st);
+
 }  // namespace atmwfs

@@ -67,10 +67,67 @@ PassLauncher pass_launcher(int N)
     }
 }
 
+PassLauncherCfg pass_launcher_cfg(int N)
+{
+    switch (N) {
+        case 64: return launch_pass_cfg_64;
+        case 128: return launch_pass_cfg_128;
+        case 256: return launch_pass_cfg_256;
+        case 512: return launch_pass_cfg_512;
+        case 1024: return launch_pass_cfg_1024;
+        case 2048: return launch_pass_cfg_2048;
+        default: return nullptr;
+    }
+}
+
 static bool pow2_in(long n, long lo, long hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; }
 
-// Twiddle table exp(-2 pi i k / N), k < N, evaluated in double.  One copy per
-// (device, N) for the life of the process.
+// Concatenated stage twiddle tables of grid size N (build_twiddles).
+static std::vector<float2> host_twiddles(int N)
+{
+    std::vector<float2> h;
+    switch (N) {
+        case 64: h.resize(tw_total<64>()); build_twiddles<64>(h.data()); break;
+        case 128: h.resize(tw_total<128>()); build_twiddles<128>(h.data()); break;
+        case 256: h.resize(tw_total<256>()); build_twiddles<256>(h.data()); break;
+        case 512: h.resize(tw_total<512>()); build_twiddles<512>(h.data()); break;
+        case 1024: h.resize(tw_total<1024>()); build_twiddles<1024>(h.data()); break;
+        case 2048: h.resize(tw_total<2048>()); build_twiddles<2048>(h.data()); break;
+        default: break;
+    }
+    return h;
+}
+
+// Size and contents of the tables without any allocation (used by the
+// allocation-free entry point).
+int twiddle_count(int N)
+{
+    switch (N) {
+        case 64: return tw_total<64>();
+        case 128: return tw_total<128>();
+        case 256: return tw_total<256>();
+        case 512: return tw_total<512>();
+        case 1024: return tw_total<1024>();
+        case 2048: return tw_total<2048>();
+        default: return 0;
+    }
+}
+
+void twiddle_fill(int N, float2* out)
+{
+    switch (N) {
+        case 64: build_twiddles<64>(out); break;
+        case 128: build_twiddles<128>(out); break;
+        case 256: build_twiddles<256>(out); break;
+        case 512: build_twiddles<512>(out); break;
+        case 1024: build_twiddles<1024>(out); break;
+        case 2048: build_twiddles<2048>(out); break;
+        default: break;
+    }
+}
+
+// Stage twiddle tables evaluated in double.  One copy per (device, N) for
+// the life of the process.
 static const float2* twiddles(int N)
 {
     static std::mutex mu;
@@ -81,14 +138,10 @@ static const float2* twiddles(int N)
     auto key = std::make_pair(dev, N);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
-    std::vector<float2> h(N);
-    for (int k = 0; k < N; k++) {
-        const double a = -2.0 * kPi * (double)k / (double)N;
-        h[k] = make_float2((float)cos(a), (float)sin(a));
-    }
+    const std::vector<float2> h = host_twiddles(N);
     float2* d = nullptr;
-    if (cudaMalloc(&d, sizeof(float2) * N) != cudaSuccess) return nullptr;
-    if (cudaMemcpy(d, h.data(), sizeof(float2) * N, cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&d, sizeof(float2) * h.size()) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
     cache[key] = d;
     return d;
 }
@@ -179,9 +232,11 @@ static void build_planes(const std::vector<double>& salt, const std::vector<int>
 
 struct Class {
     int N = 0, Nout = 0, RR = 0;
+    int cfg = 0;               // tile configuration (tile_cfg), chosen by the autotuner
     std::vector<int> members;  // global instance indices
     int base = 0;              // first slot in the class-ordered InstDev array
-    TmaSet maps;
+    TmaSet maps[kNumTileCfg];  // per configuration: the box height is RR + 3
+    double tuned_ms[kNumTileCfg] = {0, 0};
 };
 
 }  // namespace atmwfs
@@ -234,6 +289,10 @@ struct atmwfs_ctx {
     LayerPos* h_pos[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaGraphExec_t gexec = nullptr;
+    // graph branches: one stream per grid class, one for the phase sums
+    std::vector<cudaStream_t> cls_st;
+    cudaStream_t sum_st = nullptr;
+    std::vector<cudaEvent_t> gev;
 };
 
 namespace {
@@ -326,10 +385,31 @@ int pass_orient(int k, int Q) { return (Q - k) & 1; }
 
 // Launch pass k (1-based) for grid class cl; optionally report the
 // algorithmic bytes of the launch.
-atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes)
+atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaStream_t st)
 {
     const int Q = (int)c->plane_lo.size();
     const int P = Q - 1;
+    if (k == 0) {
+        // geometric phase sum of all layers over the crop (k_phasum)
+        PassArgs a;
+        memset(&a, 0, sizeof a);
+        a.inst = c->d_inst + cl.base;
+        a.pos = c->d_pos;
+        a.d_step = c->d_step;
+        a.d_status = c->d_status;
+        a.L = c->L;
+        a.ninst_total = c->ninst;
+        a.poscap = c->poscap;
+        // always the configuration-0 tile shape (most rows per tile, least halo)
+        const int RR0 = tile_cfg(cl.N, 0).rr;
+        const int off = (cl.N - cl.Nout) / 2;
+        a.row0 = off / RR0 * RR0;
+        const int rows = (off + cl.Nout - a.row0 + RR0 - 1) / RR0 * RR0;
+        if (bytes) *bytes = ((double)rows * cl.N * 4.0 * c->L + 4.0 * cl.Nout * cl.Nout) * cl.members.size();
+        AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarPhasum, dim3(rows / RR0, (unsigned)cl.members.size()), a, &cl.maps[0],
+                                        nullptr, st));
+        return ATMWFS_OK;
+    }
     {
         {
             PassArgs a;
@@ -349,7 +429,8 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes)
             a.dst = (k + 1) & 1;
             a.orient = pass_orient(k, Q);
             int var;
-            if (P == 0) var = kVarSingle;
+            (void)P;
+            if (Q == 1) var = kVarSingle;
             else if (k == 1) var = kVarFirst;
             else if (k == Q) var = kVarLast;
             else var = kVarMid;
@@ -365,34 +446,98 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes)
                 // field read / transposed write (8 B/px each), one screen tile
                 // of the window per gathered layer (4 B/px), outputs
                 const double px = (double)cl.N * cl.N, npx = (double)rows * cl.N, cnt = (double)cl.members.size();
-                const int ng = (var & OP_EPI) ? c->L : a.g_hi - a.g_lo;
+                const int ng = a.g_hi - a.g_lo;
                 double b = 0;
                 if (var & OP_LOAD) b += 8.0 * npx;
                 if (var & OP_STORE_T) b += 8.0 * px;
                 b += 4.0 * npx * ng;
-                if (var & OP_EPI) {
-                    const int mode = c->inst[cl.members[0]].mode;
-                    b += (double)cl.Nout * cl.Nout * (mode == ATMWFS_MODE_SCI ? 12.0 : 8.0);
-                }
+                if (var & OP_EPI) b += (double)cl.Nout * cl.Nout * 12.0;  // phase sum in, pha + amp out
                 *bytes = b * cnt;
             }
-            AW_CUDA(pass_launcher(cl.N)(var, grid, a, &cl.maps, twiddles(cl.N), c->st));
+            AW_CUDA(pass_launcher_cfg(cl.N)(cl.cfg, var, grid, a, &cl.maps[cl.cfg], twiddles(cl.N), st));
         }
     }
     return ATMWFS_OK;
 }
 
+// One step.  The graph forks: the phase sums (independent of the field) on
+// their own branch, every grid class's chain of passes on its own branch; the
+// last pass of each class waits for the phase sums; everything joins before
+// the science unwrap.
 atmwfs_status launch_step(atmwfs_ctx* c)
 {
     const int Q = (int)c->plane_lo.size();
-    for (int k = 1; k <= Q; k++)
-        for (Class& cl : c->classes) AW_TRY(launch_pass(c, k, cl, nullptr));
+    const int nc = (int)c->classes.size();
+    cudaEvent_t fork = c->gev[0], sums = c->gev[1];
+    AW_CUDA(cudaEventRecord(fork, c->st));
+    AW_CUDA(cudaStreamWaitEvent(c->sum_st, fork, 0));
+    for (Class& cl : c->classes) AW_TRY(launch_pass(c, 0, cl, nullptr, c->sum_st));
+    AW_CUDA(cudaEventRecord(sums, c->sum_st));
+    for (int ci = 0; ci < nc; ci++) {
+        cudaStream_t cs = c->cls_st[ci];
+        AW_CUDA(cudaStreamWaitEvent(cs, fork, 0));
+        for (int k = 1; k <= Q; k++) {
+            if (k == Q) AW_CUDA(cudaStreamWaitEvent(cs, sums, 0));
+            AW_TRY(launch_pass(c, k, c->classes[ci], nullptr, cs));
+        }
+        AW_CUDA(cudaEventRecord(c->gev[2 + ci], cs));
+        AW_CUDA(cudaStreamWaitEvent(c->st, c->gev[2 + ci], 0));
+    }
     if (c->nsci > 0) {
         AW_CUDA(unwrap_bins(c->d_inst, c->d_sci, c->nsci, c->maxnb, c->d_status, c->d_iters, c->st));
         AW_CUDA(sci_apply(c->d_inst, c->d_sci, c->nsci, c->maxnout, c->d_step, c->st));
     }
     AW_CUDA(step_advance(c->d_step, c->st));
     return ATMWFS_OK;
+}
+
+atmwfs_status check_status(atmwfs_ctx* c);
+
+// Project autotuner: for every grid class time the representative pass
+// (a middle pass when there is one) in each tile configuration and keep the
+// fastest.  ATMWFS_TILE_CFG=<k> forces configuration k.  Science bins are
+// cleared afterwards (a timed last pass accumulates into them).
+atmwfs_status autotune(atmwfs_ctx* c)
+{
+    const int Q = (int)c->plane_lo.size();
+    const char* force = getenv("ATMWFS_TILE_CFG");
+    const int k = Q >= 3 ? 2 : 1;
+    cudaEvent_t e0, e1;
+    AW_CUDA(cudaEventCreate(&e0));
+    AW_CUDA(cudaEventCreate(&e1));
+    atmwfs_status s = ATMWFS_OK;
+    for (Class& cl : c->classes) {
+        if (force) {
+            const int g = atoi(force);
+            cl.cfg = (g >= 0 && g < kNumTileCfg) ? g : 0;
+        } else {
+            double best = 1e30;
+            int bg = 0;
+            for (int g = 0; g < kNumTileCfg && s == ATMWFS_OK; g++) {
+                cl.cfg = g;
+                cl.RR = tile_cfg(cl.N, g).rr;
+                s = launch_pass(c, k, cl, nullptr, c->st);
+                if (s != ATMWFS_OK) break;
+                cudaEventRecord(e0, c->st);
+                for (int r = 0; r < 3 && s == ATMWFS_OK; r++) s = launch_pass(c, k, cl, nullptr, c->st);
+                cudaEventRecord(e1, c->st);
+                float ms = 0;
+                if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+                    s = fail(ATMWFS_ERR_CUDA, "autotune timing failed");
+                cl.tuned_ms[g] = ms / 3;
+                if (ms < best) { best = ms; bg = g; }
+            }
+            cl.cfg = bg;
+        }
+        cl.RR = tile_cfg(cl.N, cl.cfg).rr;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != ATMWFS_OK) return s;
+    for (const InstDev& d : c->hinst)
+        if (d.bins) AW_CUDA(cudaMemsetAsync(d.bins, 0, sizeof(float) * 2 * (d.nb * d.nb > 0 ? d.nb * d.nb : 1), c->st));
+    AW_CUDA(cudaStreamSynchronize(c->st));
+    return check_status(c);
 }
 
 atmwfs_status commit(atmwfs_ctx* c)
@@ -416,12 +561,15 @@ atmwfs_status commit(atmwfs_ctx* c)
         }
     }
     for (Class& cl : c->classes) {
-        memset(&cl.maps, 0, sizeof cl.maps);
-        for (int o = 0; o < 2; o++)
-            for (int l = 0; l < c->L; l++)
-                if (c->d_pad[o][l]) AW_TRY(make_tma_map(&cl.maps.m[o][l], c->d_pad[o][l], c->Wp, c->Hp, cl.RR + 3));
+        memset(cl.maps, 0, sizeof cl.maps);
+        for (int g = 0; g < kNumTileCfg; g++)
+            for (int o = 0; o < 2; o++)
+                for (int l = 0; l < c->L; l++)
+                    if (c->d_pad[o][l])
+                        AW_TRY(make_tma_map(&cl.maps[g].m[o][l], c->d_pad[o][l], c->Wp, c->Hp, tile_cfg(cl.N, g).rr + 3));
     }
     AW_CUDA(cudaStreamSynchronize(c->st));
+    AW_TRY(autotune(c));
     // capture one step
     cudaGraph_t g = nullptr;
     AW_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeRelaxed));
@@ -542,7 +690,8 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                 cl = &c->classes.back();
                 cl->N = N;
                 cl->Nout = No;
-                cl->RR = rows_per_cta(N);
+                cl->cfg = 0;
+                cl->RR = tile_cfg(N, 0).rr;
             }
             cl->members.push_back(i);
             c->Nmax = c->Nmax > N ? c->Nmax : N;
@@ -587,9 +736,9 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                 // the ring holds the frames of all instances contiguously per slot
                 d.out_pha = c->d_out_pha + c->frame_off[i];
                 d.out_amp = c->d_out_amp + c->frame_off[i];
+                CK(dalloc(c, (void**)&d.phisum, sizeof(float) * (size_t)No * No));
                 if (I.mode == ATMWFS_MODE_SCI) {
                     d.nb = No / 20;
-                    CK(dalloc(c, (void**)&d.phisum, sizeof(float) * (size_t)No * No));
                     const int nb2 = d.nb * d.nb > 0 ? d.nb * d.nb : 1;
                     CK(dalloc(c, (void**)&d.bins, sizeof(float) * 2 * nb2));
                     CKC(cudaMemset(d.bins, 0, sizeof(float) * 2 * nb2));
@@ -635,6 +784,11 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                 goto fail_out;
             }
         }
+        CKC(cudaStreamCreateWithFlags(&c->sum_st, cudaStreamNonBlocking));
+        c->cls_st.assign(c->classes.size(), nullptr);
+        for (auto& cs : c->cls_st) CKC(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        c->gev.assign(2 + c->classes.size(), nullptr);
+        for (auto& e : c->gev) CKC(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
 #undef CK
 #undef CKC
@@ -655,6 +809,11 @@ void atmwfs_destroy(atmwfs_ctx* c)
         if (c->h_pos[b]) cudaFreeHost(c->h_pos[b]);
         if (c->ev[b]) cudaEventDestroy(c->ev[b]);
     }
+    for (auto cs : c->cls_st)
+        if (cs) cudaStreamDestroy(cs);
+    if (c->sum_st) cudaStreamDestroy(c->sum_st);
+    for (auto e : c->gev)
+        if (e) cudaEventDestroy(e);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
 }
@@ -815,6 +974,19 @@ atmwfs_status atmwfs_layer_planes(const double* alt, const double* cn2, int L, d
     return ATMWFS_OK;
 }
 
+atmwfs_status atmwfs_class_info(const atmwfs_ctx* c, int ci, int* n, int* nout, int* count, int* rows_per_cta,
+                                double* tuned_ms)
+{
+    if (!c || ci < 0 || ci >= (int)c->classes.size()) return fail(ATMWFS_ERR_INVALID, "bad class");
+    const Class& cl = c->classes[ci];
+    if (n) *n = cl.N;
+    if (nout) *nout = cl.Nout;
+    if (count) *count = (int)cl.members.size();
+    if (rows_per_cta) *rows_per_cta = cl.RR;
+    for (int g = 0; g < kNumTileCfg && tuned_ms; g++) tuned_ms[g] = cl.tuned_ms[g];
+    return ATMWFS_OK;
+}
+
 void* atmwfs_stream(atmwfs_ctx* c) { return c ? (void*)c->st : nullptr; }
 
 int atmwfs_num_classes(const atmwfs_ctx* c) { return c ? (int)c->classes.size() : 0; }
@@ -822,17 +994,17 @@ int atmwfs_num_classes(const atmwfs_ctx* c) { return c ? (int)c->classes.size() 
 atmwfs_status atmwfs_time_pass(atmwfs_ctx* c, int k, int ci, int reps, double* ms, double* bytes, int* n, int* count)
 {
     if (!c || ci < 0 || ci >= (int)c->classes.size()) return fail(ATMWFS_ERR_INVALID, "bad class");
-    if (k < 1 || k > (int)c->plane_lo.size() || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
+    if (k < 0 || k > (int)c->plane_lo.size() || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
     AW_TRY(commit(c));
     Class& cl = c->classes[ci];
     cudaEvent_t e0, e1;
     AW_CUDA(cudaEventCreate(&e0));
     AW_CUDA(cudaEventCreate(&e1));
     double b = 0;
-    atmwfs_status s = launch_pass(c, k, cl, &b);  // warm-up
+    atmwfs_status s = launch_pass(c, k, cl, &b, c->st);  // warm-up
     if (s == ATMWFS_OK) {
         cudaEventRecord(e0, c->st);
-        for (int r = 0; r < reps && s == ATMWFS_OK; r++) s = launch_pass(c, k, cl, nullptr);
+        for (int r = 0; r < reps && s == ATMWFS_OK; r++) s = launch_pass(c, k, cl, nullptr, c->st);
         cudaEventRecord(e1, c->st);
     }
     float t = 0;

@@ -25,7 +25,7 @@ struct InstDev {
     float scoeff[kMaxLayers];  // per-layer phase multiplier
     float* out_pha;            // output ring [ring][Nout*Nout]
     float* out_amp;
-    float* phisum;             // science scratch: geometric phase sum [Nout*Nout]
+    float* phisum;             // geometric phase sum of the crop [Nout*Nout] (k_phasum)
     float* bins;               // science scratch: [2][nb*nb] (re, im) sums
     float* peak;               // science scratch: unwrapped bin phase [nb*nb]
     const short* binx;         // bin index of each output coordinate [Nout]
@@ -47,6 +47,7 @@ enum : int {
     OP_EPI = 32,       // output epilogue (crop, phase sum, amplitude, phase)
     OP_FFT_FWD = 64,   // unit: forward 1-D FFT only
     OP_FFT_INV = 128,  // unit: inverse 1-D FFT only
+    OP_PHASUM = 256,   // geometric phase sum of all layers (k_phasum)
 };
 
 constexpr int kVarFirst = OP_GATHER | OP_PROP2 | OP_STORE_T;
@@ -56,6 +57,7 @@ constexpr int kVarSingle = OP_GATHER | OP_EPI;
 constexpr int kVarUnitProp = OP_LOAD | OP_PROP2 | OP_STORE_T;
 constexpr int kVarUnitFwd = OP_LOAD | OP_FFT_FWD | OP_STORE_T;
 constexpr int kVarUnitInv = OP_LOAD | OP_FFT_INV | OP_STORE_T;
+constexpr int kVarPhasum = OP_PHASUM;
 
 // Status bits written by kernels.
 enum : unsigned {
@@ -96,21 +98,34 @@ constexpr int kBoxW = 32;  // TMA box width (floats)
 // Host-side launch entry of one row pass for grid size N (defined per N).
 typedef cudaError_t (*PassLauncher)(int var, dim3 grid, const PassArgs& a, const TmaSet* maps,
                                     const float2* tw, cudaStream_t st);
+// Same, for tile configuration `cfg` (see tile_cfg).
+typedef cudaError_t (*PassLauncherCfg)(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps,
+                                       const float2* tw, cudaStream_t st);
 
-// Rows per CTA used for grid size N.
-inline int rows_per_cta(int N)
+// Tile configurations compiled for every grid size: rows per CTA and the
+// minimum number of resident CTAs per SM the kernel is register-limited to.
+// Configuration 0 is the one-CTA-per-SM shape; configuration 1 trades
+// halo overhead (fewer rows per tile) for several resident CTAs per SM.
+// The engine's autotuner picks one per grid class at set-up.
+struct TileCfg {
+    int rr, minb;
+};
+constexpr int kNumTileCfg = 2;
+constexpr TileCfg tile_cfg(int N, int c)
 {
-    switch (N) {
-        case 64: return 32;
-        case 128: return 32;
-        case 256: return 16;
-        case 512: return 16;
-        case 1024: return 8;
-        case 2048: return 4;
-        default: return 0;
-    }
+    return N == 64    ? (c == 0 ? TileCfg{32, 1} : TileCfg{16, 2})
+         : N == 128   ? (c == 0 ? TileCfg{32, 1} : TileCfg{16, 2})
+         : N == 256   ? (c == 0 ? TileCfg{16, 1} : TileCfg{8, 3})
+         : N == 512   ? (c == 0 ? TileCfg{16, 1} : TileCfg{8, 3})
+         : N == 1024  ? (c == 0 ? TileCfg{8, 1} : TileCfg{4, 3})
+         : N == 2048  ? (c == 0 ? TileCfg{4, 1} : TileCfg{2, 3})
+                      : TileCfg{0, 0};
 }
 
+// Rows per CTA of configuration 0 (unit operators).
+inline int rows_per_cta(int N) { return tile_cfg(N, 0).rr; }
+
 PassLauncher pass_launcher(int N);
+PassLauncherCfg pass_launcher_cfg(int N);
 
 }  // namespace atmwfs

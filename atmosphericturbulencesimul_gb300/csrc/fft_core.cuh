@@ -66,6 +66,20 @@ AW_HD float2 tw_const(float2 d, int k, int n)
     return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
 }
 
+// d * exp(ds 2 pi i k / n) with the direction ds = -1 (forward) or +1
+// (inverse) known only at run time: one code copy serves both directions.
+AW_HD float2 tw_rt(float2 d, int k, int n, float ds)
+{
+    if (k == 0) return d;
+    const int j = k * (32 / n);
+    if (j == 16) return make_float2(-d.x, -d.y);
+    if (j == 8) return make_float2(-ds * d.y, ds * d.x);
+    if (j == 24) return make_float2(ds * d.y, -ds * d.x);
+    const float c = cos32(j);
+    const float s = ds * sin32(j);
+    return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
+}
+
 template <int R>
 AW_HD constexpr int brev(int i)
 {
@@ -89,6 +103,28 @@ AW_HD void dft(float2* v)
                 const float2 a = v[base + k], b = v[base + k + span];
                 v[base + k] = cadd(a, b);
                 v[base + k + span] = tw_const<D>(csub(a, b), k, 2 * span);
+            }
+        }
+    }
+    float2 t[R];
+    AW_UNROLL
+    for (int i = 0; i < R; i++) t[i] = v[i];
+    AW_UNROLL
+    for (int i = 0; i < R; i++) v[i] = t[brev<R>(i)];
+}
+
+template <int R>
+AW_HD void dft_rt(float2* v, float ds)
+{
+    AW_UNROLL
+    for (int span = R / 2; span >= 1; span >>= 1) {
+        AW_UNROLL
+        for (int base = 0; base < R; base += 2 * span) {
+            AW_UNROLL
+            for (int k = 0; k < span; k++) {
+                const float2 a = v[base + k], b = v[base + k + span];
+                v[base + k] = cadd(a, b);
+                v[base + k + span] = tw_rt(csub(a, b), k, 2 * span, ds);
             }
         }
     }
@@ -163,6 +199,45 @@ AW_HD void stage_store(const float2* v, float2* buf, int t)
     }
 }
 
+// The same with the stride NS and the direction known at run time (ns is a
+// power of two): the stage loop below runs every stage of every transform
+// through one copy of the code of each radix.
+// tws: the stage's twiddle table tws[r * ns + k] = exp(-2 pi i k r / (ns R))
+// (see tw_offset), read with consecutive k across a warp.
+template <int N, int T, int E, int R>
+AW_HD void stage_twiddle_rt(float2* v, int t, const float2* tws, int ns, float ds)
+{
+    if (ns == 1) return;
+    AW_UNROLL
+    for (int w = 0; w < E / R; w++) {
+        const int k = (t + T * w) & (ns - 1);
+        AW_UNROLL
+        for (int r = 1; r < R; r++) {
+            const float2 w0 = tws[r * ns + k];
+            v[w * R + r] = cmul(v[w * R + r], make_float2(w0.x, -ds * w0.y));
+        }
+    }
+}
+
+template <int E, int R>
+AW_HD void stage_dft_rt(float2* v, float ds)
+{
+    AW_UNROLL
+    for (int w = 0; w < E / R; w++) dft_rt<R>(v + w * R, ds);
+}
+
+template <int N, int T, int E, int R>
+AW_HD void stage_store_rt(const float2* v, float2* buf, int t, int ns)
+{
+    AW_UNROLL
+    for (int w = 0; w < E / R; w++) {
+        const int j = t + T * w;
+        const int base = (j & ~(ns - 1)) * R + (j & (ns - 1));
+        AW_UNROLL
+        for (int q = 0; q < R; q++) buf[padi(base + q * ns)] = v[w * R + q];
+    }
+}
+
 // Frequency (or output) index held in register slot s after the last stage
 // of radix RL: k = j_w + q N/RL with w = s / RL, q = s % RL.
 template <int N, int T, int RL>
@@ -197,6 +272,102 @@ template <> struct InvRadices<256>  { using type = Radices<16, 16>; };
 template <> struct InvRadices<512>  { using type = Radices<16, 32>; };
 template <> struct InvRadices<1024> { using type = Radices<32, 32>; };
 template <> struct InvRadices<2048> { using type = Radices<8, 8, 32>; };
+
+// Radix sequence of the forward transform as a runtime-indexable table; the
+// inverse of a propagation walks it backwards.
+template <int N> struct Stages;
+template <> struct Stages<64>   { static constexpr int S = 2, R0 = 8, R1 = 8, R2 = 0; };
+template <> struct Stages<128>  { static constexpr int S = 2, R0 = 16, R1 = 8, R2 = 0; };
+template <> struct Stages<256>  { static constexpr int S = 2, R0 = 16, R1 = 16, R2 = 0; };
+template <> struct Stages<512>  { static constexpr int S = 2, R0 = 32, R1 = 16, R2 = 0; };
+template <> struct Stages<1024> { static constexpr int S = 2, R0 = 32, R1 = 32, R2 = 0; };
+template <> struct Stages<2048> { static constexpr int S = 3, R0 = 32, R1 = 8, R2 = 8; };
+
+template <int N>
+AW_HD constexpr bool has_radix(int r)
+{
+    return Stages<N>::R0 == r || Stages<N>::R1 == r || Stages<N>::R2 == r;
+}
+
+// last radix of the forward sequence
+template <int N>
+AW_HD constexpr int last_radix() { return Stages<N>::S == 3 ? Stages<N>::R2 : Stages<N>::R1; }
+
+// radix of stage st, forward order (rev = 0) or reversed (rev = 1)
+template <int N>
+AW_HD int stage_radix(int st, int rev)
+{
+    const int i = rev ? Stages<N>::S - 1 - st : st;
+    return i == 0 ? Stages<N>::R0 : i == 1 ? Stages<N>::R1 : Stages<N>::R2;
+}
+
+// Stride (product of the earlier radices) of stage st in the given order.
+template <int N>
+AW_HD int stage_ns(int st, int rev)
+{
+    int ns = 1;
+    for (int i = 0; i < st; i++) ns *= stage_radix<N>(i, rev);
+    return ns;
+}
+
+// Twiddle tables: for each order (rev = 0, 1) and stage st >= 1 a table of
+// R x ns entries tab[r * ns + k] = exp(-2 pi i k r / (ns R)); this gives the
+// offset of table (rev, st) in the concatenation and the total size.
+template <int N>
+AW_HD int tw_offset(int rev, int st)
+{
+    int off = 0;
+    for (int o = 0; o <= rev; o++)
+        for (int i = 1; i < Stages<N>::S; i++) {
+            if (o == rev && i == st) return off;
+            off += stage_radix<N>(i, o) * stage_ns<N>(i, o);
+        }
+    return off;
+}
+template <int N>
+AW_HD int tw_total() { return tw_offset<N>(1, Stages<N>::S); }
+
+// Fill the concatenated stage tables (host side, double precision).
+template <int N>
+inline void build_twiddles(float2* out)
+{
+    for (int o = 0; o < 2; o++)
+        for (int st = 1; st < Stages<N>::S; st++) {
+            const int R = stage_radix<N>(st, o), ns = stage_ns<N>(st, o);
+            float2* tab = out + tw_offset<N>(o, st);
+            for (int r = 0; r < R; r++)
+                for (int k = 0; k < ns; k++) {
+                    const double a = -2.0 * 3.14159265358979323846264338328 * (double)(k * r) / (double)(ns * R);
+                    tab[r * ns + k] = make_float2((float)cos(a), (float)sin(a));
+                }
+        }
+}
+
+// Stage body (twiddles + butterflies) of radix r and stride ns for one
+// thread; a uniform branch selects the code of the radix.
+template <int N, int T, int E>
+AW_HD void stage_compute(float2* v, int t, const float2* tw, int r, int ns, float ds)
+{
+    if constexpr (has_radix<N>(32)) if (r == 32) { stage_twiddle_rt<N, T, E, 32>(v, t, tw, ns, ds); stage_dft_rt<E, 32>(v, ds); return; }
+    if constexpr (has_radix<N>(16)) if (r == 16) { stage_twiddle_rt<N, T, E, 16>(v, t, tw, ns, ds); stage_dft_rt<E, 16>(v, ds); return; }
+    if constexpr (has_radix<N>(8)) if (r == 8) { stage_twiddle_rt<N, T, E, 8>(v, t, tw, ns, ds); stage_dft_rt<E, 8>(v, ds); return; }
+}
+
+template <int N, int T, int E>
+AW_HD void stage_exchange_store(const float2* v, float2* buf, int t, int r, int ns)
+{
+    if constexpr (has_radix<N>(32)) if (r == 32) { stage_store_rt<N, T, E, 32>(v, buf, t, ns); return; }
+    if constexpr (has_radix<N>(16)) if (r == 16) { stage_store_rt<N, T, E, 16>(v, buf, t, ns); return; }
+    if constexpr (has_radix<N>(8)) if (r == 8) { stage_store_rt<N, T, E, 8>(v, buf, t, ns); return; }
+}
+
+template <int N, int T, int E>
+AW_HD void stage_exchange_load(float2* v, const float2* buf, int t, int r)
+{
+    if constexpr (has_radix<N>(32)) if (r == 32) { stage_load<N, T, E, 32>(v, buf, t); return; }
+    if constexpr (has_radix<N>(16)) if (r == 16) { stage_load<N, T, E, 16>(v, buf, t); return; }
+    if constexpr (has_radix<N>(8)) if (r == 8) { stage_load<N, T, E, 8>(v, buf, t); return; }
+}
 
 template <int R0, int... Rs> struct LastRadix { static constexpr int value = LastRadix<Rs...>::value; };
 template <int R0> struct LastRadix<R0> { static constexpr int value = R0; };

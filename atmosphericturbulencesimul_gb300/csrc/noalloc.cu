@@ -17,6 +17,8 @@
 
 namespace atmwfs {
 void set_error_message(const char* msg);
+int twiddle_count(int N);
+void twiddle_fill(int N, float2* out);
 }
 
 namespace {
@@ -24,15 +26,16 @@ namespace {
 using namespace atmwfs;
 
 constexpr long kMaxN = ATMWFS_NOALLOC_MAX_N;
+constexpr long kMaxTw = 2 * kMaxN;  // stage twiddle tables of the largest grid
 constexpr int kMaxDevices = 64;
 const double kPi = 3.14159265358979323846264338328;
 
 // Scratch shared by every call on a device: the field after the first
 // (transposed) pass, the 1-D transfer table and the twiddles of the call's
-// size.  2 MiB + 8 KiB per device that loads the library, held until exit.
+// size.  2 MiB + 12 KiB per device that loads the library, held until exit.
 __device__ __align__(256) float2 g_field[kMaxN * kMaxN];
 __device__ __align__(256) float2 g_table[kMaxN];
-__device__ __align__(256) float2 g_twiddle[kMaxN];
+__device__ __align__(256) float2 g_twiddle[kMaxTw];
 
 // Device addresses of the scratch arrays.  In host code the array names are
 // host-side stand-ins, so the addresses are looked up once per device.
@@ -87,19 +90,20 @@ extern "C" atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long 
     cudaStream_t cs = (cudaStream_t)stream;
     // transfer table and twiddles of this size, built on the stack (the same
     // formulas as the allocating path) and copied into the static arrays
-    float2 h[kMaxN], tw[kMaxN];
+    float2 h[kMaxN], tw[kMaxTw];
     const double coeff = kPi * z * lambda / (dx * (double)n) / (dx * (double)n);
     for (long k = 0; k < n; k++) {
         const long f = k < n / 2 ? k : k - n;
         double ang = -coeff * (double)(f * f);
         ang -= 2.0 * kPi * nearbyint(ang / (2.0 * kPi));
         h[k] = make_float2((float)(cos(ang) / n), (float)(sin(ang) / n));
-        const double a = -2.0 * kPi * (double)k / (double)n;
-        tw[k] = make_float2((float)cos(a), (float)sin(a));
     }
+    const int ntw = twiddle_count((int)n);
+    if (ntw > kMaxTw) return err(ATMWFS_ERR_INVALID, "twiddle tables exceed the static scratch");
+    twiddle_fill((int)n, tw);
     // pageable sources: each copy is staged before the call returns
     if (cudaMemcpyAsync(s->table, h, sizeof(float2) * n, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
-        cudaMemcpyAsync(s->twiddle, tw, sizeof(float2) * n, cudaMemcpyHostToDevice, cs) != cudaSuccess)
+        cudaMemcpyAsync(s->twiddle, tw, sizeof(float2) * ntw, cudaMemcpyHostToDevice, cs) != cudaSuccess)
         return err(ATMWFS_ERR_CUDA, "copy of the transfer table failed");
     const PassLauncher fn = pass_launcher((int)n);
     PassArgs a;

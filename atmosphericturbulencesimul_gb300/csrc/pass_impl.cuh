@@ -98,7 +98,7 @@ struct PassGeom {
     static constexpr int NBOX = N / kBoxW + 1;
     static constexpr int TROWS = RR + 3;
     static constexpr size_t XBYTES = size_t(RR) * RS * 8;
-    static constexpr size_t PHI_EPI_BYTES = size_t(3) * RR * N * 4;
+    static constexpr size_t PHI_EPI_BYTES = size_t(RR) * RS * 8;
     static constexpr size_t TILE_BYTES = size_t(NBOX) * TROWS * kBoxW * 4;
     AW_HD static constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
     AW_HD static constexpr size_t region(bool epi) { return round128((epi && PHI_EPI_BYTES > XBYTES) ? PHI_EPI_BYTES : XBYTES); }
@@ -163,6 +163,49 @@ __device__ __forceinline__ void prop_row(float2* v, float2* xrow, int t, const f
     run_fft<N, T, E, +1>(v, xrow, t, tw, IR{});
 }
 
+// One 1-D transform of the row in v through a runtime stage loop: every
+// stage of every transform of the kernel runs through the same code of its
+// radix, which keeps the kernel inside the instruction cache.  ds = -1
+// forward, +1 inverse; rev walks the radix sequence backwards (the inverse of
+// a propagation, which starts from the forward's register layout and ends in
+// the natural layout x[t + e T]).
+template <int N, int T, int E>
+__device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev)
+{
+    int ns = 1, rp = 0, nsp = 1;
+#pragma unroll 1
+    for (int st = 0; st < Stages<N>::S; st++) {
+        const int r = stage_radix<N>(st, rev);
+        if (st > 0) {
+            __syncthreads();
+            stage_exchange_store<N, T, E>(v, xrow, t, rp, nsp);
+            __syncthreads();
+            stage_exchange_load<N, T, E>(v, xrow, t, r);
+        }
+        stage_compute<N, T, E>(v, t, tw + tw_offset<N>(rev, st), r, ns, ds);
+        rp = r;
+        nsp = ns;
+        ns *= r;
+    }
+}
+
+// 1-D Fresnel propagation (forward FFT, transfer table, inverse FFT) with a
+// single copy of the transform code.
+template <int N, int T, int E>
+__device__ __forceinline__ void prop_row_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw,
+                                            const float2* __restrict__ h)
+{
+    constexpr int RL = last_radix<N>();
+#pragma unroll 1
+    for (int dir = 0; dir < 2; dir++) {
+        fft_rt<N, T, E>(v, xrow, t, tw, dir ? 1.0f : -1.0f, dir);
+        if (dir == 0) {
+#pragma unroll
+            for (int s = 0; s < E; s++) v[s] = cmul(v[s], __ldg(h + last_index<N, T, RL>(t, s)));
+        }
+    }
+}
+
 // Nearest integer to (hi + lo) / 2 pi, halves rounded up, with the
 // remainder evaluated against a two-term 2 pi so that the decision is exact
 // to ~1e-7 rad (the reference rounds with (long)(x / 2 pi + 1000.5) - 1000).
@@ -180,6 +223,18 @@ __device__ __forceinline__ float round_2pi(float hi, float lo)
     return k;
 }
 
+// exp(i phi) with phi reduced to [-pi, pi] against a two-term 2 pi, then the
+// hardware sine/cosine (absolute error ~4e-7 on that range).
+__device__ __forceinline__ float2 phasor(float phi)
+{
+    const float k = rintf(phi * 0.159154943091895336f);
+    float r = fmaf(-k, 6.28125f, phi);
+    r = fmaf(-k, 0.0019353071795864769f, r);
+    float s, c;
+    __sincosf(r, &s, &c);
+    return make_float2(c, s);
+}
+
 __device__ __forceinline__ float add_2pi_multiple(float p, float k)
 {
     return fmaf(k, 6.28125f, p) + k * 0.0019353071795864769f;
@@ -195,12 +250,12 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // ---------------------------------------------------------------------------
 // the pass kernel
 // ---------------------------------------------------------------------------
-template <int N, int RR, int OPS>
-__global__ void __launch_bounds__(Plan<N>::T* RR, 1)
+template <int N, int RR, int MINB, int OPS>
+__global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     k_pass(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps, const float2* __restrict__ tw)
 {
     using G = PassGeom<N, RR>;
-    constexpr int T = G::T, E = G::E, NT = G::NT, RS = G::RS, TROWS = G::TROWS;
+    constexpr int T = G::T, E = G::E, NT = G::NT, RS = G::RS;
     constexpr bool kEpi = (OPS & OP_EPI) != 0;
     constexpr bool kGather = (OPS & (OP_GATHER | OP_EPI)) != 0;
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -208,7 +263,6 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 1)
     // TMA destination: 128-byte aligned whatever the dynamic smem base
     float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm + G::region(kEpi)) + 127) & ~uintptr_t(127));
     __shared__ __align__(8) uint64_t bar;
-    __shared__ float sbins[3 * 2 * 104];
 
     const int tid = threadIdx.x;
     const int t = tid % T;
@@ -220,8 +274,8 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 1)
     const LayerPos* P = I ? a.pos + ((size_t)(step % a.poscap) * a.ninst_total + I->gidx) * a.L : nullptr;
     float2* xrow = xb + rr * RS;
 
-    const int ltop = kEpi ? a.L - 1 : a.g_hi - 1;
-    const int lbot = kEpi ? 0 : a.g_lo;
+    const int ltop = a.g_hi - 1;
+    const int lbot = a.g_lo;
     int parity = 0;
     if constexpr (kGather) {
         if (tid == 0) mbar_init(&bar, 1);
@@ -239,121 +293,130 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 1)
         for (int e = 0; e < E; e++) v[e] = make_float2(1.0f, 0.0f);
     }
 
-    if constexpr ((OPS & OP_PROP1) != 0) prop_row<N, T, E>(v, xrow, t, tw, I ? I->H + (size_t)a.hop1 * N : a.H1);
-    if constexpr ((OPS & OP_FFT_FWD) != 0) run_fft<N, T, E, -1>(v, xrow, t, tw, typename FwdRadices<N>::type{});
-    if constexpr ((OPS & OP_FFT_INV) != 0) run_fft<N, T, E, +1>(v, xrow, t, tw, typename FwdRadices<N>::type{});
-
-    if constexpr (kGather && !kEpi) {
-        float* phi = reinterpret_cast<float*>(xb);  // [RR][N]
-        __syncthreads();
-        for (int l = ltop; l >= lbot; l--) {
-            if (!cta_wait_tile(&bar, parity, a.d_status)) return;
-            parity ^= 1;
-            const bool first = (l == ltop);
-            gather_tile<N, RR, NT>(tile, tile_geom(P[l], a.orient, y0), I->scoeff[l], tid, [=](int r, int x, float val) {
-                phi[r * N + x] = first ? val : phi[r * N + x] + val;
-            });
-            __syncthreads();
-            if (tid == 0 && l > lbot) tma_issue_layer<N, RR>(maps, a.orient, l - 1, tile_geom(P[l - 1], a.orient, y0), tile, &bar);
-        }
+    if constexpr ((OPS & (OP_FFT_FWD | OP_FFT_INV)) != 0) {
+        fft_rt<N, T, E>(v, xrow, t, tw, (OPS & OP_FFT_FWD) ? -1.0f : 1.0f, 0);
+    } else {
+        // phase 0: propagation 1; phase 1: screens of this plane; phase 2:
+        // propagation 2 -- a runtime loop, so the transform code appears once
+#pragma unroll 1
+        for (int ph = 0; ph < 3; ph++) {
+            if (ph == 1) {
+                if constexpr (kGather) {
+                    float* phi = reinterpret_cast<float*>(xb);  // [RR][N]
+                    __syncthreads();
+                    for (int l = ltop; l >= lbot; l--) {
+                        if (!cta_wait_tile(&bar, parity, a.d_status)) return;
+                        parity ^= 1;
+                        const bool first = (l == ltop);
+                        gather_tile<N, RR, NT>(tile, tile_geom(P[l], a.orient, y0), I->scoeff[l], tid,
+                                               [=](int r, int x, float val) {
+                                                   phi[r * N + x] = first ? val : phi[r * N + x] + val;
+                                               });
+                        __syncthreads();
+                        if (tid == 0 && l > lbot)
+                            tma_issue_layer<N, RR>(maps, a.orient, l - 1, tile_geom(P[l - 1], a.orient, y0), tile, &bar);
+                    }
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-            float s, c;
-            sincosf(phi[rr * N + t + e * T], &s, &c);
-            v[e] = cmul(v[e], make_float2(c, s));
+                    for (int e = 0; e < E; e++) v[e] = cmul(v[e], phasor(phi[rr * N + t + e * T]));
+                }
+                continue;
+            }
+            const bool run = ph == 0 ? ((OPS & OP_PROP1) != 0) : ((OPS & OP_PROP2) != 0);
+            if (!run) continue;
+            const int hop = ph == 0 ? a.hop1 : a.hop2;
+            const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
+            prop_row_rt<N, T, E>(v, xrow, t, tw, h);
         }
     }
 
     if constexpr (kEpi) {
-        // phi0: phase of the layers at the last plane; (hi, lo): compensated
-        // geometric phase sum over all layers (reference array1 / sarray1).
-        float* phi0 = reinterpret_cast<float*>(xb);
-        float* shi = phi0 + RR * N;
-        float* slo = shi + RR * N;
-        __syncthreads();
-        for (int i = tid; i < 3 * RR * N; i += NT) phi0[i] = 0.0f;
-        for (int i = tid; i < 3 * 2 * 104; i += NT) sbins[i] = 0.0f;
-        __syncthreads();
-        for (int l = ltop; l >= lbot; l--) {
-            if (!cta_wait_tile(&bar, parity, a.d_status)) return;
-            parity ^= 1;
-            const bool in0 = (l >= a.g_lo && l < a.g_hi);
-            gather_tile<N, RR, NT>(tile, tile_geom(P[l], a.orient, y0), I->scoeff[l], tid, [=](int r, int x, float val) {
-                const int i = r * N + x;
-                if (in0) phi0[i] += val;
-                float s, e;
-                two_sum(shi[i], val, s, e);
-                shi[i] = s;
-                slo[i] += e;
-            });
-            __syncthreads();
-            if (tid == 0 && l > lbot) tma_issue_layer<N, RR>(maps, a.orient, l - 1, tile_geom(P[l - 1], a.orient, y0), tile, &bar);
-        }
+        // Outputs of the crop.  The geometric phase sum over all layers
+        // (reference array1 / sarray1) comes from k_phasum.  The field is
+        // staged in shared memory so that one rolled loop serves all pixels.
+        __shared__ float sbins[3 * 2 * 104];
+        __shared__ short jrow[RR];
         const int off = I->off, Nout = I->Nout, mode = I->mode;
         const int slot = step % I->ring;
-        const bool rowin = (y >= off) && (y < off + Nout);
-        const int yo = y - off;
-        float* opha = I->out_pha + (size_t)slot * Nout * Nout;
-        float* oamp = I->out_amp + (size_t)slot * Nout * Nout;
-        const int nb = I->nb;
-        const int yb = max(y0, off) - off;
-        const int jb0 = (nb > 0 && yb < Nout) ? I->binx[yb] : 0;
+        float* __restrict__ opha = I->out_pha + (size_t)slot * Nout * Nout;
+        float* __restrict__ oamp = I->out_amp + (size_t)slot * Nout * Nout;
+        const float* __restrict__ psum = I->phisum;
+        __syncthreads();  // phasor reads of phi are done
 #pragma unroll
-        for (int e = 0; e < E; e++) {
-            const int x = t + e * T;
-            if (!rowin || x < off || x >= off + Nout) continue;
-            const int i = rr * N + x;
-            const float hi = shi[i], lo = slo[i];
-            const size_t o = (size_t)yo * Nout + (x - off);
-            if (mode == kModePhase) {
-                opha[o] = hi + lo;
-                oamp[o] = 1.0f;
-                continue;
-            }
-            float s, c;
-            sincosf(phi0[i], &s, &c);
-            const float2 u = cmul(v[e], make_float2(c, s));
-            const float amp = sqrtf(u.x * u.x + u.y * u.y);
-            const float pha = atan2f(u.y, u.x);
-            oamp[o] = amp;
-            if (mode == kModeRef) {
-                opha[o] = add_2pi_multiple(pha, round_2pi(hi, lo));
-            } else {
-                opha[o] = pha;
-                I->phisum[o] = hi + lo;
-                if (nb > 0) {
+        for (int e = 0; e < E; e++) xrow[padi(t + e * T)] = v[e];
+        __syncthreads();
+        const int ya = max(y0, off), yb = min(y0 + RR, off + Nout);
+        if (ya >= yb) return;
+        const int nrows = yb - ya;
+        for (int r = ya - y0; r < yb - y0; r++) {
+            const size_t orow = (size_t)(y0 + r - off) * Nout - off;
+            float2* crow = xb + r * RS;
+#pragma unroll 4
+            for (int x = off + tid; x < off + Nout; x += NT) {
+                const size_t o = orow + x;
+                const float ps = psum[o];
+                if (mode == kModePhase) {
+                    opha[o] = ps;
+                    oamp[o] = 1.0f;
+                    continue;
+                }
+                float2* cell = crow + padi(x);
+                const float2 u = *cell;
+                oamp[o] = sqrtf(u.x * u.x + u.y * u.y);
+                const float pha = atan2f(u.y, u.x);
+                if (mode == kModeRef) {
+                    opha[o] = add_2pi_multiple(pha, round_2pi(ps, 0.0f));
+                } else {
+                    opha[o] = pha;
                     float d, de;
-                    two_sum(hi, -pha, d, de);
-                    float bs, bc;
-                    sincosf(d + (de + lo), &bs, &bc);
-                    const int ib = I->binx[x - off];
-                    const int jb = I->binx[yo] - jb0;
-                    atomicAdd(&sbins[(jb * nb + ib) * 2 + 0], bc);
-                    atomicAdd(&sbins[(jb * nb + ib) * 2 + 1], bs);
+                    two_sum(ps, -pha, d, de);
+                    *cell = phasor(d + de);  // exp(i (sum - pha)) for the science bins
                 }
             }
         }
+        const int nb = I->nb;
         if (mode == kModeSci && nb > 0) {
+            // column sums over the CTA's rows, split at bin-row boundaries,
+            // then one shared atomic per (column, bin row)
+            const short* __restrict__ binx = I->binx;
+            for (int i = tid; i < 3 * 2 * 104; i += NT) sbins[i] = 0.0f;
+            if (tid < nrows) jrow[tid] = binx[ya - off + tid];
             __syncthreads();
-            const int ylast = min(y0 + RR, off + Nout) - 1;
-            if (ylast >= max(y0, off)) {
-                const int nj = I->binx[ylast - off] - jb0 + 1;
-                for (int k = tid; k < nj * nb; k += NT) {
-                    const int jb = jb0 + k / nb, ib = k % nb;
-                    atomicAdd(&I->bins[jb * nb + ib], sbins[k * 2 + 0]);
-                    atomicAdd(&I->bins[nb * nb + jb * nb + ib], sbins[k * 2 + 1]);
+            const int jb0 = jrow[0];
+            for (int x = off + tid; x < off + Nout; x += NT) {
+                const int ib = binx[x - off];
+                int jb = jb0;
+                float sr = 0.0f, si = 0.0f;
+                for (int yy = ya; yy < yb; yy++) {
+                    const int j = jrow[yy - ya];
+                    if (j != jb) {
+                        atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 0], sr);
+                        atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 1], si);
+                        sr = si = 0.0f;
+                        jb = j;
+                    }
+                    const float2 z = xb[(yy - y0) * RS + padi(x)];
+                    sr += z.x;
+                    si += z.y;
                 }
+                atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 0], sr);
+                atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 1], si);
+            }
+            __syncthreads();
+            const int nj = jrow[nrows - 1] - jb0 + 1;
+            float* __restrict__ gb = I->bins;
+            for (int k = tid; k < nj * nb; k += NT) {
+                const int jb = jb0 + k / nb, ib = k % nb;
+                atomicAdd(&gb[jb * nb + ib], sbins[k * 2 + 0]);
+                atomicAdd(&gb[nb * nb + jb * nb + ib], sbins[k * 2 + 1]);
             }
         }
         return;
     }
 
-    if constexpr ((OPS & OP_PROP2) != 0) prop_row<N, T, E>(v, xrow, t, tw, I ? I->H + (size_t)a.hop2 * N : a.H2);
-
     if constexpr ((OPS & OP_STORE_T) != 0) {
         __syncthreads();
         constexpr bool kFreq = (OPS & (OP_FFT_FWD | OP_FFT_INV)) != 0;
-        constexpr int RL = last_of(typename FwdRadices<N>::type{});
+        constexpr int RL = last_radix<N>();
 #pragma unroll
         for (int s = 0; s < E; s++) {
             const int x = kFreq ? last_index<N, T, RL>(t, s) : t + s * T;
@@ -370,11 +433,95 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 1)
     }
 }
 
-// host launcher for one N
-template <int N>
-cudaError_t launch_pass_n(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
+// ---------------------------------------------------------------------------
+// geometric phase sum over all layers for the crop (reference array1 /
+// sarray1, AtmosphericTurbulence.c:2909-2916, 3237-3245): gather only, one
+// TMA tile per layer, compensated (two-sum) accumulation in registers.
+// Independent of the field, so it runs beside the propagation passes.
+// ---------------------------------------------------------------------------
+template <int N, int RR>
+__global__ void __launch_bounds__(Plan<N>::T* RR, 2)
+    k_phasum(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps)
 {
-    constexpr int RR = (N == 64 || N == 128) ? 32 : (N == 256 || N == 512) ? 16 : (N == 1024) ? 8 : 4;
+    using G = PassGeom<N, RR>;
+    constexpr int NT = G::NT, TROWS = G::TROWS, NC = (N + NT - 1) / NT;
+    constexpr int TILE_FLOATS = (int)(G::TILE_BYTES / 4);
+    extern __shared__ __align__(1024) unsigned char sm[];
+    // two tile buffers: the next layer's copy overlaps this layer's sums
+    float* tiles = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) uint64_t bar[2];
+    const int tid = threadIdx.x;
+    const int y0 = a.row0 + blockIdx.x * RR;
+    const InstDev* I = a.inst + blockIdx.y;
+    const int step = *a.d_step;
+    const LayerPos* P = a.pos + ((size_t)(step % a.poscap) * a.ninst_total + I->gidx) * a.L;
+    const int L = a.L;
+    if (tid == 0) { mbar_init(&bar[0], 1); mbar_init(&bar[1], 1); }
+    __syncthreads();
+    if (tid == 0) {
+        tma_issue_layer<N, RR>(maps, 0, L - 1, tile_geom(P[L - 1], 0, y0), tiles, &bar[0]);
+        if (L > 1) tma_issue_layer<N, RR>(maps, 0, L - 2, tile_geom(P[L - 2], 0, y0), tiles + TILE_FLOATS, &bar[1]);
+    }
+    float hi[NC][RR], lo[NC][RR];
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+#pragma unroll
+        for (int r = 0; r < RR; r++) hi[c][r] = lo[c][r] = 0.0f;
+    int parity = 0;  // bit b: phase parity of buffer b
+    for (int l = L - 1; l >= 0; l--) {
+        const int b = (L - 1 - l) & 1;
+        float* tile = tiles + b * TILE_FLOATS;
+        if (!cta_wait_tile(&bar[b], (parity >> b) & 1, a.d_status)) {
+            // the other buffer may still be in flight: let it land first
+            if (l > 0) cta_wait_tile(&bar[b ^ 1], (parity >> (b ^ 1)) & 1, nullptr);
+            return;
+        }
+        parity ^= 1 << b;
+        const TileGeom g = tile_geom(P[l], 0, y0);
+        const float sc = I->scoeff[l];
+        float wx[4], wy[4];
+        keys_weights(g.fx, wx);
+        keys_weights(g.fy, wy);
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int x = tid + c * NT;
+            if (x < N) {
+                const int cc = g.d + x;
+                float h[TROWS];
+#pragma unroll
+                for (int q = 0; q < TROWS; q++)
+                    h[q] = wx[0] * tile[tile_index<TROWS>(q, cc)] + wx[1] * tile[tile_index<TROWS>(q, cc + 1)] +
+                           wx[2] * tile[tile_index<TROWS>(q, cc + 2)] + wx[3] * tile[tile_index<TROWS>(q, cc + 3)];
+#pragma unroll
+                for (int r = 0; r < RR; r++) {
+                    const float val = (wy[0] * h[r] + wy[1] * h[r + 1] + wy[2] * h[r + 2] + wy[3] * h[r + 3]) * sc;
+                    float s, e;
+                    two_sum(hi[c][r], val, s, e);
+                    hi[c][r] = s;
+                    lo[c][r] += e;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && l > 1) tma_issue_layer<N, RR>(maps, 0, l - 2, tile_geom(P[l - 2], 0, y0), tile, &bar[b]);
+    }
+    const int off = I->off, Nout = I->Nout;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const int x = tid + c * NT;
+#pragma unroll
+        for (int r = 0; r < RR; r++) {
+            const int y = y0 + r;
+            if (x < N && x >= off && x < off + Nout && y >= off && y < off + Nout)
+                I->phisum[(size_t)(y - off) * Nout + (x - off)] = hi[c][r] + lo[c][r];
+        }
+    }
+}
+
+// host launcher for one (N, tile configuration)
+template <int N, int RR, int MINB>
+cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
+{
     using G = PassGeom<N, RR>;
     static TmaSet empty_maps;  // unit passes gather nothing
     const TmaSet& m = maps ? *maps : empty_maps;
@@ -384,11 +531,11 @@ cudaError_t launch_pass_n(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         constexpr size_t sm = G::smem(VAR);                                                            \
         static bool attr = false;                                                                      \
         if (!attr) {                                                                                   \
-            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
             if (e != cudaSuccess) return e;                                                            \
             attr = true;                                                                               \
         }                                                                                              \
-        k_pass<N, RR, VAR><<<grid, block, sm, st>>>(a, m, tw);                                         \
+        k_pass<N, RR, MINB, VAR><<<grid, block, sm, st>>>(a, m, tw);                                   \
         return cudaGetLastError();                                                                     \
     }
     switch (var) {
@@ -399,9 +546,36 @@ cudaError_t launch_pass_n(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         AW_CASE(kVarUnitProp)
         AW_CASE(kVarUnitFwd)
         AW_CASE(kVarUnitInv)
+        case kVarPhasum: {
+            constexpr size_t sm = 2 * G::TILE_BYTES + 128;
+            static bool attr = false;
+            if (!attr) {
+                cudaError_t e = cudaFuncSetAttribute(k_phasum<N, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                if (e != cudaSuccess) return e;
+                attr = true;
+            }
+            k_phasum<N, RR><<<grid, block, sm, st>>>(a, m);
+            return cudaGetLastError();
+        }
         default: return cudaErrorInvalidValue;
     }
 #undef AW_CASE
+}
+
+template <int N>
+cudaError_t launch_pass_n(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
+{
+    constexpr TileCfg c0 = tile_cfg(N, 0);
+    return launch_pass_t<N, c0.rr, c0.minb>(var, grid, a, maps, tw, st);
+}
+
+template <int N>
+cudaError_t launch_pass_nc(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
+                           cudaStream_t st)
+{
+    constexpr TileCfg c0 = tile_cfg(N, 0), c1 = tile_cfg(N, 1);
+    if (cfg == 1) return launch_pass_t<N, c1.rr, c1.minb>(var, grid, a, maps, tw, st);
+    return launch_pass_t<N, c0.rr, c0.minb>(var, grid, a, maps, tw, st);
 }
 
 }  // namespace atmwfs

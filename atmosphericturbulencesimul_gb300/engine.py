@@ -170,6 +170,13 @@ class Series:
     def num_classes(self) -> int:
         return int(self._lib.atmwfs_num_classes(self._ctx))
 
+    def class_info(self, c: int) -> dict:
+        n, no, cnt, rr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        t = (C.c_double * 2)()
+        check(self._lib.atmwfs_class_info(self._ctx, c, C.byref(n), C.byref(no), C.byref(cnt), C.byref(rr), t))
+        return {"n": n.value, "nout": no.value, "count": cnt.value, "rows_per_cta": rr.value,
+                "tuned_ms": [t[0], t[1]]}
+
     def time_pass(self, k: int, c: int, reps: int = 10):
         """Mean duration [ms] and algorithmic bytes of pass k of grid class c."""
         ms, b = C.c_double(), C.c_double()

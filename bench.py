@@ -277,7 +277,7 @@ def main():
     npl = len(s.planes()[0])
     passes = []
     for c in range(s.num_classes()):
-        for k in range(1, npl + 1):
+        for k in range(0, npl + 1):
             r = s.time_pass(k, c, reps=5)
             r.update(k=k, c=c)
             passes.append(r)
@@ -297,7 +297,10 @@ def main():
             "kernel": f"k_pass N={dom['n']} pass {dom['k']}/{npl} ({dom['count']} instances)",
             "algorithmic_bytes": dom["bytes"], "ms": round(dom["ms"], 4), "share_of_passes": round(dom["ms"] / tot, 3),
             "peak_source": pk["source"]}
-    launches = npl * s.num_classes() + 3
+    launches = (npl + 1) * s.num_classes() + 3
+    cfg["tiles"] = {str(ci["n"]): {"rows_per_cta": ci["rows_per_cta"], "tuned_ms": [round(x, 4) for x in ci["tuned_ms"]]}
+                    for ci in (s.class_info(c) for c in range(s.num_classes()))}
+    cfg["pass_ms"] = {f"n{p['n']}_k{p['k']}": round(p["ms"], 4) for p in passes}
 
     line = {"metric": metric, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,

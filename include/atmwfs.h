@@ -136,14 +136,20 @@ atmwfs_status atmwfs_layer_planes(const double* alt, const double* cn2, int L, d
 /* CUDA stream (cudaStream_t) on which the context runs. */
 void* atmwfs_stream(atmwfs_ctx* ctx);
 
-/* Diagnostics: launch pass k (1-based, of atmwfs_num_planes passes) for the
- * instances of grid class c `reps` times, timed with CUDA events on the
+/* Diagnostics: launch pass k (1-based, of atmwfs_num_planes passes; k = 0 is
+ * the geometric phase-sum kernel) for the instances of grid class c `reps` times, timed with CUDA events on the
  * context stream.  Returns the mean duration [ms], the algorithmic bytes of
  * one launch (field in/out, screen tiles, outputs), and the class's grid
  * size and instance count.  Does not advance the simulation. */
 atmwfs_status atmwfs_time_pass(atmwfs_ctx* ctx, int k, int c, int reps, double* ms, double* bytes, int* n,
                                int* count);
 int atmwfs_num_classes(const atmwfs_ctx* ctx);
+
+/* Grid class ci (instances sharing wf_raw_size and wf_size): sizes, member
+ * count, the rows per CTA the autotuner chose, and the mean time [ms] of the
+ * tuned pass in each of the 2 tile configurations (0 if forced). */
+atmwfs_status atmwfs_class_info(const atmwfs_ctx* ctx, int ci, int* n, int* nout, int* count, int* rows_per_cta,
+                                double* tuned_ms);
 
 /* Current layer positions (pixels) of instance i, after the last step. */
 atmwfs_status atmwfs_positions(const atmwfs_ctx* ctx, int i, double* xpos, double* ypos);

@@ -1,7 +1,7 @@
 // pass_emul.cpp -- thread-by-thread CPU emulation of the engine's in-CTA
 // building blocks (the same template code the kernels instantiate):
-//   * Stockham FFT stages for every supported N (forward, inverse and the
-//     forward -> transfer -> inverse row propagation);
+//   * the runtime Stockham stage loop for every supported N (forward,
+//     inverse and the forward -> transfer -> reversed inverse propagation);
 //   * the TMA tile geometry of the screen gather and the separable bicubic,
 //     against a direct periodic Keys bicubic in double.
 // Prints one line per check: "<name> <max error>"; exit code 0.
@@ -27,28 +27,24 @@ static double urand()
     return (double)(g_rng >> 11) * (1.0 / 9007199254740992.0);
 }
 
-template <int N, int T, int E, int D, int NS, int R, int... Rest>
-void emu_stages(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw)
+// The kernel's runtime stage loop, one thread after the other (the
+// __syncthreads of the device loop separate the per-thread sweeps).
+template <int N, int T, int E>
+void emu_fft_rt(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw, float ds, int rev)
 {
-    for (int t = 0; t < T; t++) {
-        stage_twiddle<N, T, E, R, NS, D>(V[t].data(), t, tw);
-        stage_dft<E, R, D>(V[t].data());
-    }
-    if constexpr (sizeof...(Rest) > 0) {
-        for (int t = 0; t < T; t++) stage_store<N, T, E, R, NS>(V[t].data(), buf, t);
-        for (int t = 0; t < T; t++) stage_load<N, T, E, FirstRadix<Rest...>::value>(V[t].data(), buf, t);
-        emu_stages<N, T, E, D, NS * R, Rest...>(V, buf, tw);
+    int ns = 1, rp = 0, nsp = 1;
+    for (int st = 0; st < Stages<N>::S; st++) {
+        const int r = stage_radix<N>(st, rev);
+        if (st > 0) {
+            for (int t = 0; t < T; t++) stage_exchange_store<N, T, E>(V[t].data(), buf, t, rp, nsp);
+            for (int t = 0; t < T; t++) stage_exchange_load<N, T, E>(V[t].data(), buf, t, r);
+        }
+        for (int t = 0; t < T; t++) stage_compute<N, T, E>(V[t].data(), t, tw + tw_offset<N>(rev, st), r, ns, ds);
+        rp = r;
+        nsp = ns;
+        ns *= r;
     }
 }
-
-template <int N, int T, int E, int D, int... Rs>
-void emu_fft(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw, Radices<Rs...>)
-{
-    emu_stages<N, T, E, D, 1, Rs...>(V, buf, tw);
-}
-
-template <int... Rs>
-constexpr int lastr(Radices<Rs...>) { return LastRadix<Rs...>::value; }
 
 static std::vector<cd> dft(const std::vector<cd>& x, int sign)
 {
@@ -70,20 +66,17 @@ template <int N>
 void check_fft()
 {
     constexpr int T = Plan<N>::T, E = Plan<N>::E;
-    std::vector<float2> tw(N);
-    for (int k = 0; k < N; k++) tw[k] = make_float2((float)cos(-2 * M_PI * k / N), (float)sin(-2 * M_PI * k / N));
+    std::vector<float2> tw(tw_total<N>() + 1);
+    build_twiddles<N>(tw.data());
     std::vector<float2> buf(padi(N) + 64);
     std::vector<cd> x(N);
     for (int i = 0; i < N; i++) x[i] = cd(urand() - 0.5, urand() - 0.5);
-    using FR = typename FwdRadices<N>::type;
-    using IR = typename InvRadices<N>::type;
-    constexpr int RL = lastr(FR{});
+    constexpr int RL = last_radix<N>();
     for (int D : {-1, +1}) {
         std::vector<std::array<float2, E>> V(T);
         for (int t = 0; t < T; t++)
             for (int e = 0; e < E; e++) V[t][e] = make_float2((float)x[t + e * T].real(), (float)x[t + e * T].imag());
-        if (D < 0) emu_fft<N, T, E, -1>(V, buf.data(), tw.data(), FR{});
-        else emu_fft<N, T, E, +1>(V, buf.data(), tw.data(), FR{});
+        emu_fft_rt<N, T, E>(V, buf.data(), tw.data(), (float)D, 0);
         std::vector<cd> X = dft(x, D);
         double err = 0, nrm = 0;
         std::vector<int> seen(N, 0);
@@ -109,10 +102,10 @@ void check_fft()
     std::vector<std::array<float2, E>> V(T);
     for (int t = 0; t < T; t++)
         for (int e = 0; e < E; e++) V[t][e] = make_float2((float)x[t + e * T].real(), (float)x[t + e * T].imag());
-    emu_fft<N, T, E, -1>(V, buf.data(), tw.data(), FR{});
+    emu_fft_rt<N, T, E>(V, buf.data(), tw.data(), -1.0f, 0);
     for (int t = 0; t < T; t++)
         for (int s = 0; s < E; s++) V[t][s] = cmul(V[t][s], h[last_index<N, T, RL>(t, s)]);
-    emu_fft<N, T, E, +1>(V, buf.data(), tw.data(), IR{});
+    emu_fft_rt<N, T, E>(V, buf.data(), tw.data(), 1.0f, 1);
     std::vector<cd> X = dft(x, -1);
     for (int k = 0; k < N; k++) X[k] *= hd[k];
     std::vector<cd> y = dft(X, +1);
@@ -139,10 +132,10 @@ static double keys(double t, int k)
     }
 }
 
-template <int N>
+template <int N, int CFG = 0>
 void check_gather(int M, int ix, int iy, float fx, float fy, int orient, int y0)
 {
-    constexpr int RR = N == 64 || N == 128 ? 32 : N == 256 || N == 512 ? 16 : N == 1024 ? 8 : 4;
+    constexpr int RR = tile_cfg(N, CFG).rr;
     constexpr int NT = Plan<N>::T * RR;
     constexpr int TROWS = RR + 3, NBOX = N / kBoxW + 1;
     std::vector<float> S((size_t)M * M);
@@ -187,7 +180,7 @@ void check_gather(int M, int ix, int iy, float fx, float fy, int orient, int y0)
                 }
             err = fmax(err, fabs(v - out[(size_t)r * N + x]));
         }
-    printf("gather_%d_o%d_ix%d_iy%d %.3e\n", N, orient, ix, iy, inb ? err : 1e9);
+    printf("gather_%d_c%d_o%d_ix%d_iy%d %.3e\n", N, CFG, orient, ix, iy, inb ? err : 1e9);
 }
 
 int main()
@@ -207,6 +200,10 @@ int main()
         check_gather<1024>(M, 13, M - 7, 0.77f, 0.33f, orient, 1016);
         check_gather<2048>(M, M - 1, M - 1, 0.999f, 0.001f, orient, 2044);
         check_gather<1024>(M, 2, 3, 0.0f, 0.0f, orient, 0);
+        check_gather<64, 1>(M, 1, 2, 0.4f, 0.2f, orient, 48);
+        check_gather<256, 1>(M, M - 2, 9, 0.7f, 0.9f, orient, 248);
+        check_gather<1024, 1>(M, 5, M - 1, 0.1f, 0.5f, orient, 1020);
+        check_gather<2048, 1>(M, M - 4, 3, 0.6f, 0.3f, orient, 2046);
     }
     return 0;
 }

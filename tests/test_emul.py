@@ -31,6 +31,6 @@ def test_fft_stages(emul_output, n):
 
 def test_gather_geometry(emul_output):
     g = {k: v for k, v in emul_output.items() if k.startswith("gather_")}
-    assert len(g) == 14
+    assert len(g) == 22
     for k, v in g.items():
         assert v < 1e-5, (k, v)
