@@ -743,12 +743,19 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                     CK(dalloc(c, (void**)&d.bins, sizeof(float) * 2 * nb2));
                     CKC(cudaMemset(d.bins, 0, sizeof(float) * 2 * nb2));
                     CK(dalloc(c, (void**)&d.peak, sizeof(float) * nb2));
-                    std::vector<short> bx(No);
+                    // bin of each output coordinate, as the reference computes it
+                    // (long)(1.0 * ii / Wout * nb), and the first coordinate of each bin
+                    std::vector<short> bx(No), b0(d.nb + 2, (short)No);
                     for (int ii = 0; ii < No; ii++) bx[ii] = (short)(long)(1.0 * ii / No * d.nb);
+                    for (int ii = No - 1; ii >= 0; ii--) b0[bx[ii]] = (short)ii;
+                    for (int ib = d.nb - 1; ib >= 0; ib--)
+                        if (b0[ib] > b0[ib + 1]) b0[ib] = b0[ib + 1];
                     short* dbx = nullptr;
-                    CK(dalloc(c, (void**)&dbx, sizeof(short) * No));
+                    CK(dalloc(c, (void**)&dbx, sizeof(short) * (No + d.nb + 2)));
                     CKC(cudaMemcpy(dbx, bx.data(), sizeof(short) * No, cudaMemcpyHostToDevice));
+                    CKC(cudaMemcpy(dbx + No, b0.data(), sizeof(short) * (d.nb + 2), cudaMemcpyHostToDevice));
                     d.binx = dbx;
+                    d.binx0 = dbx + No;
                     sci.push_back(slot);
                     c->maxnb = c->maxnb > d.nb ? c->maxnb : d.nb;
                     c->maxnout = c->maxnout > No ? c->maxnout : No;

@@ -29,6 +29,7 @@ struct InstDev {
     float* bins;               // science scratch: [2][nb*nb] (re, im) sums
     float* peak;               // science scratch: unwrapped bin phase [nb*nb]
     const short* binx;         // bin index of each output coordinate [Nout]
+    const short* binx0;        // first output coordinate of each bin [nb + 1]
     int N, Nout, off, nb;
     int mode;                  // kModeRef / kModeSci / kModePhase
     int ring;                  // output frames kept on the device

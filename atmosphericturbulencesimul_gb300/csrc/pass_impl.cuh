@@ -332,9 +332,9 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     if constexpr (kEpi) {
         // Outputs of the crop.  The geometric phase sum over all layers
         // (reference array1 / sarray1) comes from k_phasum.  The field is
-        // staged in shared memory so that one rolled loop serves all pixels.
-        __shared__ float sbins[3 * 2 * 104];
-        __shared__ short jrow[RR];
+        // staged in shared memory; each thread then owns whole columns of the
+        // CTA's rows, so the science bin sums need no shared atomics.
+        constexpr int CPT = (N + NT - 1) / NT;  // columns per thread
         const int off = I->off, Nout = I->Nout, mode = I->mode;
         const int slot = step % I->ring;
         float* __restrict__ opha = I->out_pha + (size_t)slot * Nout * Nout;
@@ -343,71 +343,89 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         __syncthreads();  // phasor reads of phi are done
 #pragma unroll
         for (int e = 0; e < E; e++) xrow[padi(t + e * T)] = v[e];
-        __syncthreads();
         const int ya = max(y0, off), yb = min(y0 + RR, off + Nout);
-        if (ya >= yb) return;
-        const int nrows = yb - ya;
-        for (int r = ya - y0; r < yb - y0; r++) {
-            const size_t orow = (size_t)(y0 + r - off) * Nout - off;
-            float2* crow = xb + r * RS;
-#pragma unroll 4
-            for (int x = off + tid; x < off + Nout; x += NT) {
-                const size_t o = orow + x;
-                const float ps = psum[o];
+        if (ya >= yb) return;  // uniform: the CTA has no crop row
+        // prefetch this thread's phase sums
+        float ps[RR][CPT];
+#pragma unroll
+        for (int r = 0; r < RR; r++)
+#pragma unroll
+            for (int c = 0; c < CPT; c++) {
+                const int x = off + tid + c * NT, y = y0 + r;
+                ps[r][c] = (y >= ya && y < yb && x < off + Nout) ? psum[(size_t)(y - off) * Nout + (x - off)] : 0.0f;
+            }
+        __syncthreads();
+        const int nb = I->nb;
+        const bool bins = (mode == kModeSci) && nb > 0;
+        const short* __restrict__ binx = I->binx;
+        const int jb0 = bins ? binx[ya - off] : 0;
+        // bins are at least 20 rows tall: RR rows touch at most NJ bin rows
+        constexpr int NJ = RR > 16 ? 3 : 2;
+        float2* colsum = reinterpret_cast<float2*>(tile);  // [NJ][N]: per bin row, per column
+        static_assert(size_t(NJ) * N * 8 <= G::TILE_BYTES, "column sums must fit in the tile buffer");
+#pragma unroll
+        for (int c = 0; c < CPT; c++) {
+            const int x = off + tid + c * NT;
+            if (x >= off + Nout) continue;
+            float2 acc0 = make_float2(0.0f, 0.0f), acc1 = acc0, acc2 = acc0;
+#pragma unroll
+            for (int r = 0; r < RR; r++) {
+                const int y = y0 + r;
+                if (y < ya || y >= yb) continue;
+                const size_t o = (size_t)(y - off) * Nout + (x - off);
                 if (mode == kModePhase) {
-                    opha[o] = ps;
+                    opha[o] = ps[r][c];
                     oamp[o] = 1.0f;
                     continue;
                 }
-                float2* cell = crow + padi(x);
-                const float2 u = *cell;
+                const float2 u = xb[r * RS + padi(x)];
                 oamp[o] = sqrtf(u.x * u.x + u.y * u.y);
                 const float pha = atan2f(u.y, u.x);
                 if (mode == kModeRef) {
-                    opha[o] = add_2pi_multiple(pha, round_2pi(ps, 0.0f));
+                    opha[o] = add_2pi_multiple(pha, round_2pi(ps[r][c], 0.0f));
                 } else {
                     opha[o] = pha;
-                    float d, de;
-                    two_sum(ps, -pha, d, de);
-                    *cell = phasor(d + de);  // exp(i (sum - pha)) for the science bins
+                    if (bins) {
+                        float d, de;
+                        two_sum(ps[r][c], -pha, d, de);
+                        const float2 z = phasor(d + de);  // exp(i (sum - pha))
+                        const int j = binx[y - off] - jb0;
+                        if (j == 0) {
+                            acc0.x += z.x;
+                            acc0.y += z.y;
+                        } else if (NJ == 2 || j == 1) {
+                            acc1.x += z.x;
+                            acc1.y += z.y;
+                        } else {
+                            acc2.x += z.x;
+                            acc2.y += z.y;
+                        }
+                    }
                 }
             }
+            if (bins) {
+                colsum[x - off] = acc0;
+                colsum[N + x - off] = acc1;
+                if (NJ == 3) colsum[2 * N + x - off] = acc2;
+            }
         }
-        const int nb = I->nb;
-        if (mode == kModeSci && nb > 0) {
-            // column sums over the CTA's rows, split at bin-row boundaries,
-            // then one shared atomic per (column, bin row)
-            const short* __restrict__ binx = I->binx;
-            for (int i = tid; i < 3 * 2 * 104; i += NT) sbins[i] = 0.0f;
-            if (tid < nrows) jrow[tid] = binx[ya - off + tid];
+        if (bins) {
+            // one thread per (bin row, bin): sum its contiguous columns in a
+            // fixed order, one global atomic per bin and CTA
             __syncthreads();
-            const int jb0 = jrow[0];
-            for (int x = off + tid; x < off + Nout; x += NT) {
-                const int ib = binx[x - off];
-                int jb = jb0;
+            const int nj = binx[yb - 1 - off] - jb0 + 1;
+            const short* __restrict__ bx0 = I->binx0;
+            float* __restrict__ gb = I->bins;
+            for (int k = tid; k < nj * nb; k += NT) {
+                const int j = k / nb, ib = k % nb;
                 float sr = 0.0f, si = 0.0f;
-                for (int yy = ya; yy < yb; yy++) {
-                    const int j = jrow[yy - ya];
-                    if (j != jb) {
-                        atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 0], sr);
-                        atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 1], si);
-                        sr = si = 0.0f;
-                        jb = j;
-                    }
-                    const float2 z = xb[(yy - y0) * RS + padi(x)];
+                for (int x = bx0[ib]; x < bx0[ib + 1]; x++) {
+                    const float2 z = colsum[j * N + x];
                     sr += z.x;
                     si += z.y;
                 }
-                atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 0], sr);
-                atomicAdd(&sbins[((jb - jb0) * nb + ib) * 2 + 1], si);
-            }
-            __syncthreads();
-            const int nj = jrow[nrows - 1] - jb0 + 1;
-            float* __restrict__ gb = I->bins;
-            for (int k = tid; k < nj * nb; k += NT) {
-                const int jb = jb0 + k / nb, ib = k % nb;
-                atomicAdd(&gb[jb * nb + ib], sbins[k * 2 + 0]);
-                atomicAdd(&gb[nb * nb + jb * nb + ib], sbins[k * 2 + 1]);
+                atomicAdd(&gb[(jb0 + j) * nb + ib], sr);
+                atomicAdd(&gb[nb * nb + (jb0 + j) * nb + ib], si);
             }
         }
         return;

@@ -90,6 +90,15 @@ def test_series_phase_only(lib, oracle64):
     _compare(case, oracle64, 3)
 
 
+def test_series_bins_straddling_three_rows(lib, oracle64, monkeypatch):
+    # 32-row tiles (tile configuration 0 of a 128 grid) with a 100-pixel crop:
+    # the rows 32..63 tile covers output rows 18..49, i.e. science bins 0, 1, 2
+    monkeypatch.setenv("ATMWFS_TILE_CFG", "0")
+    case = Case(alt=[0.0, 6000.0], cn2=[0.7, 0.3], speed=[12.0, 25.0], direction=[0.2, 2.4], M=256, W=128,
+                Wout=100, fresnel_bin=100.0)
+    _compare(case, oracle64, 2)
+
+
 def test_series_large_grid(lib, oracle64):
     case = Case(alt=[0.0, 4000.0, 16000.0], cn2=[0.5, 0.3, 0.2], speed=[10.0, 20.0, 30.0], direction=[0.5, 2.5, 4.5],
                 M=1024, W=512, Wout=512, fresnel_bin=100.0)
