@@ -16,7 +16,14 @@
  *   atmref stdN <conf> <lambda_model> <alt> <lambda> [<alt> <lambda> ...]
  *       AtmosphereModel_Create_from_CONF then AtmosphereModel_stdAtmModel_N
  *       (src/AtmosphereModel/AtmosphereModel.c:3212) for each pair.
+ *   atmref roffset <conf> <lambda_model> <lambda_ref> <slambda> <zangle> <alt>...
+ *       the per-layer refraction offset RoffsetS - Roffset [m] that
+ *       make_AtmosphericTurbulence_wavefront_series adds to the start row
+ *       (src/AtmosphericTurbulence/AtmosphericTurbulence.c:2159-2183): the
+ *       same 1 m altitude steps from the site altitude over the reference's
+ *       stdAtmModel_N, with its float/double operand types.
  */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -29,6 +36,13 @@
 
 DATA data;
 pid_t CLIPID;
+int C_ERRNO;     /* globals of src/CLIcore.c:102-104 */
+int TYPESIZE[9];
+
+int init_AtmosphericTurbulence(void), init_AtmosphereModel(void), init_OpticsMaterials(void),
+    init_WFpropagate(void), init_image_gen(void), init_statistic(void), init_fft(void), init_info(void),
+    init_COREMOD_arith(void), init_COREMOD_iofits(void), init_COREMOD_memory(void), init_COREMOD_tools(void),
+    init_00CORE(void);
 
 static void init_data(void)
 {
@@ -48,6 +62,32 @@ static void init_data(void)
     data.rndgen = gsl_rng_alloc(gsl_rng_mt19937);
     data.SHARED_DFT = 0;
     data.NBKEWORD_DFT = 10;
+    /* element sizes as src/CLIcore.c:588-596 */
+    TYPESIZE[0] = 0;
+    TYPESIZE[1] = sizeof(char);
+    TYPESIZE[2] = sizeof(int);
+    TYPESIZE[3] = sizeof(float);
+    TYPESIZE[4] = sizeof(double);
+    TYPESIZE[5] = 2 * sizeof(float);
+    TYPESIZE[6] = 2 * sizeof(double);
+    TYPESIZE[7] = sizeof(unsigned short);
+    TYPESIZE[8] = sizeof(long);
+    C_ERRNO = 0;
+    /* the module set-up of src/initmodules.c:27-51, for the compiled modules
+       (the atmosphere model allocates its profile tables here) */
+    init_AtmosphericTurbulence();
+    init_AtmosphereModel();
+    init_OpticsMaterials();
+    init_WFpropagate();
+    init_image_gen();
+    init_statistic();
+    init_fft();
+    init_info();
+    init_COREMOD_arith();
+    init_COREMOD_iofits();
+    init_COREMOD_memory();
+    init_COREMOD_tools();
+    init_00CORE();
 }
 
 static int cmd_fresnel(int argc, char **argv)
@@ -80,6 +120,31 @@ static int cmd_stdn(int argc, char **argv)
     return 0;
 }
 
+extern float SiteAlt;
+
+static int cmd_roffset(int argc, char **argv)
+{
+    if (argc < 8) return 2;
+    AtmosphereModel_Create_from_CONF(argv[2], (float)atof(argv[3]));
+    const float lam_ref = (float)atof(argv[4]);
+    const double slam = atof(argv[5]);
+    const float za = (float)atof(argv[6]);
+    for (int i = 7; i < argc; i++) {
+        const double alt = atof(argv[i]);
+        double off[2] = {0.0, 0.0};
+        for (int w = 0; w < 2; w++) {
+            for (double h = SiteAlt; h < alt; h += 1.0) {
+                const double n = 1.0 + AtmosphereModel_stdAtmModel_N(h, w == 0 ? lam_ref : slam, 0);
+                double t = sin(za) / sqrt(n * n - sin(za) * sin(za));
+                t -= sin(za) / sqrt(1.0 - sin(za) * sin(za));
+                off[w] += t;
+            }
+        }
+        printf("ROFF %.17g %.17g\n", alt, off[1] - off[0]);
+    }
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 2) {
@@ -93,5 +158,6 @@ int main(int argc, char **argv)
         return 0;
     }
     if (strcmp(argv[1], "stdN") == 0) return cmd_stdn(argc, argv);
+    if (strcmp(argv[1], "roffset") == 0) return cmd_roffset(argc, argv);
     return 2;
 }

@@ -35,7 +35,7 @@ REF_SOURCES = [
     "00CORE/00CORE.c",
 ]
 SHIMS = ["shim_fftw.c", "shim_fitsio.c", "shim_rng_stubs.c", "atmref_driver.c"]
-CFLAGS = ["-std=gnu99", "-O2", "-fcommon", "-w", "-ffp-contract=off", "-fno-builtin-rand",
+CFLAGS = ["-std=gnu99", "-O2", "-U_FORTIFY_SOURCE", "-D_FORTIFY_SOURCE=0", "-fcommon", "-w", "-ffp-contract=off", "-fno-builtin-rand",
           f"-I{HERE / 'shim'}", f"-I{REF}", '-DFFTCONFIGDIR="/tmp"']
 
 

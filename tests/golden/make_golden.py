@@ -1,0 +1,166 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures of tests/golden/ by running the reference's
+own code (the checker build oracle/_ref/atmref, compiled from the reference
+sources by oracle/ref/build_ref.py) on small seeded cases.
+
+  fresnel.npz  Fresnel_propagate_wavefront (WFpropagate.c:68) on seeded
+               complex_float fields.
+  mkwfs.npz    make_AtmosphericTurbulence_wavefront_series (mkwfs <slambda> 0)
+  mkwfs_b.npz  on the two profiles of MKWFS_CASES, with master screens
+               synthesised by the reference from Philox noise injected into
+               its rand()/GSL calls: the master screens it wrote (before its
+               r0 renormalisation), the Scoeff of each layer and the start-row
+               refraction offsets from its atmosphere model, and its
+               lambda_ref and science phase/amplitude cubes.
+
+Run from the repository root where the reference is mounted:
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path[:0] = [str(ROOT), str(HERE)]
+
+from oracle import oracle as orc  # noqa: E402
+import fits_io as fitsio  # noqa: E402
+
+ATMREF = ROOT / "oracle" / "_ref" / "atmref"
+
+# altitude, relative Cn2, speed, direction, L0, l0, sigma wind, wind outer scale
+MKWFS_CASES = {
+    # three super-layers, full-frame output, zenith
+    "mkwfs": dict(
+        M=128, W=64, Wout=64, nframes=3, lam_ref_um=0.5, slam_um=1.6, seeing=0.6875, pupil=0.01, dt=0.001,
+        bin=100.0, seed=2024, zangle=0.0, src=(0.0, 0.0),
+        profile=[(0.0, 0.5, 10.0, 0.5236, 20.0, 0.01, 1.0, 10.0),
+                 (3000.0, 0.3, 20.0, 2.0, 20.0, 0.01, 1.0, 10.0),
+                 (10000.0, 0.2, 15.0, 4.0, 20.0, 0.01, 1.0, 10.0)]),
+    # layers 0 and 50 m share a super-layer; 100-pixel crop of a 128 grid
+    # (5 x 5 science bins); 0.5 rad zenith angle (refraction offsets, slant
+    # hops, Cn2 / cos z); off-axis source
+    "mkwfs_b": dict(
+        M=256, W=128, Wout=100, nframes=3, lam_ref_um=0.5, slam_um=2.2, seeing=0.8, pupil=0.01, dt=0.002,
+        bin=100.0, seed=77, zangle=0.5, src=(4.85e-5, -2.4e-5),
+        profile=[(0.0, 0.4, 8.0, 0.1, 25.0, 0.01, 1.0, 10.0),
+                 (50.0, 0.2, 12.0, 1.0, 25.0, 0.01, 1.0, 10.0),
+                 (5000.0, 0.3, 25.0, 3.0, 25.0, 0.01, 1.0, 10.0),
+                 (12000.0, 0.1, 30.0, 5.5, 25.0, 0.01, 1.0, 10.0)]),
+}
+
+
+def conf_text(c: dict) -> str:
+    kv = [
+        ("TURBULENCE_REF_WAVEL", f"{c['lam_ref_um']:f}"), ("TURBULENCE_SEEING", f"{c['seeing']:f}"),
+        ("TURBULENCE_PROF_FILE", "turbul.prof"), ("ZENITH_ANGLE", f"{c['zangle']!r}"), ("SOURCE_XPOS", f"{c['src'][0]!r}"),
+        ("SOURCE_YPOS", f"{c['src'][1]!r}"), ("TIME_DAY_OF_YEAR", "150"), ("TIME_LOCAL_SOLAR_TIME", "0.0"),
+        ("SITE_ALT", "0.0"), ("SITE_LATITUDE", "20.0"), ("SITE_LONGITUDE", "-155.5"), ("CO2_PPM", "400.0"),
+        ("SITE_TP_AUTO", "1"), ("SITE_TEMP", "273.15"), ("SITE_PRESS", "1.0"), ("SITE_H2O_METHOD", "1"),
+        ("SITE_RH", "30.0"), ("SITE_TPW", "10.0"), ("SITE_PW_SCALEH", "2000.0"), ("WFOUTPUT", "1"),
+        ("WF_FILE_PREFIX", "./WF_files/wf_"), ("SHM_OUTPUT", "0"), ("MAKE_SWAVEFRONT", "1"),
+        ("SLAMBDA", f"{c['slam_um']:f}"), ("SWF_WRITE2DISK", "1"), ("SWF_FILE_PREFIX", "./WFS_files/wf_"),
+        ("SHM_SOUTPUT", "0"), ("SHM_SPREFIX", "outwf"), ("SHM_SOUTPUTM", "2"), ("WFsize", str(c["Wout"])),
+        ("PUPIL_SCALE", f"{c['pupil']:f}"), ("REALTIME", "0"), ("REALTIMEFACTOR", "1.0"),
+        ("WFTIME_STEP", f"{c['dt']:f}"), ("TIME_SPAN", f"{c['dt'] * c['nframes']:f}"), ("NB_TSPAN", "1"),
+        ("SIMTDELAY", "0"), ("WAITFORSEM", "0"), ("WAITSEMIMNAME", "wfsimwait"),
+        ("WF_RAW_SIZE", str(c["W"])), ("MASTER_SIZE", str(c["M"])), ("WAVEFRONT_AMPLITUDE", "1"),
+        ("FRESNEL_PROPAGATION", "1"), ("FRESNEL_PROPAGATION_BIN", f"{c['bin']:f}"),
+    ]
+    return "\n".join(f"{k:25s} {v:>20s}  # generated" for k, v in kv) + "\n"
+
+
+def run(cmd, cwd, env=None):
+    r = subprocess.run(cmd, cwd=cwd, env=env, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(" ".join(map(str, cmd)) + "\n" + r.stdout[-2000:] + r.stderr[-2000:])
+    return r.stdout
+
+
+def make_fresnel() -> dict:
+    out = {}
+    cases = [(64, 0.01, 3000.0, 1.6e-6), (128, 0.01, 8000.0, 0.5e-6)]
+    with tempfile.TemporaryDirectory() as td:
+        for k, (n, dx, z, lam) in enumerate(cases):
+            rng = np.random.default_rng(100 + k)
+            a = np.exp(1j * rng.standard_normal((n, n)) * 2).astype(np.complex64)
+            a.tofile(Path(td) / "in.c64")
+            run([str(ATMREF), "fresnel", str(n), repr(dx), repr(z), repr(lam), "in.c64", "out.c64"], td)
+            b = np.fromfile(Path(td) / "out.c64", np.complex64).reshape(n, n)
+            out[f"in{k}"] = a
+            out[f"out{k}"] = b
+            out[f"par{k}"] = np.array([n, dx, z, lam])
+    return out
+
+
+def make_mkwfs(c: dict) -> dict:
+    M, L = c["M"], len(c["profile"])
+    o64 = orc.Oracle(64)
+    with tempfile.TemporaryDirectory() as td:
+        td = Path(td)
+        (td / "WF_files").mkdir()
+        (td / "WFS_files").mkdir()
+        (td / "WFsim.conf").write_text(conf_text(c))
+        (td / "turbul.prof").write_text("# alt cn2 speed dir L0 l0 sigmawind Lwind\n" + "".join(
+            " ".join(f"{v:g}" for v in row) + "\n" for row in c["profile"]))
+        # the wind-scatter series is unused by the loop: pre-create it
+        for l in range(L):
+            fitsio.write(td / f"wspeed_{l:03d}.fits", np.zeros((3, 8), np.float32))
+        noise = []
+        for l in range(L):
+            u, g = o64.screen_noise(c["seed"], l, M)
+            noise += [u, g]
+        np.concatenate([x.ravel() for x in noise]).astype(np.float32).tofile(td / "noise.f32")
+        env = dict(os.environ, ATMREF_NOISE=str(td / "noise.f32"), ATMREF_NOISE_M=str(M))
+        run([str(ATMREF), "mkwfs", f"{c['slam_um']}", "0"], td, env)
+        screens = [fitsio.read(td / f"t{l:03d}_{M}_f.fits") for l in range(L)]
+        lam_pm = int(c["slam_um"] * 1e-6 * 1e12 + 0.5)
+        cubes = {}
+        for key, pre in (("ref", "WF_files/wf_"), ("sci", "WFS_files/wf_")):
+            for q in ("pha", "amp"):
+                cubes[f"{key}_{q}"] = fitsio.read(td / f"{pre}{0:08d}.{lam_pm:09d}.{q}.fits")
+        # Scoeff(h) = CONF_LAMBDA/SLAMBDA * N(h, SLAMBDA)/N(h, CONF_LAMBDA) from the
+        # reference's atmosphere model, with its float operands (:2661-2663)
+        lam_ref = np.float32(c["lam_ref_um"] * 1e-6)
+        slam = c["slam_um"] * 1e-6
+        args = []
+        for row in c["profile"]:
+            args += [repr(row[0]), repr(float(lam_ref)), repr(row[0]), repr(slam)]
+        txt = run([str(ATMREF), "stdN", "WFsim.conf", repr(slam)] + args, td)
+        vals = [float(line.split()[3]) for line in txt.splitlines() if line.startswith("STDN")]
+        scoeff = []
+        for l in range(L):
+            n_ref, n_sci = np.float32(vals[2 * l]), np.float32(vals[2 * l + 1])
+            scoeff.append(float(lam_ref) / slam * float(n_sci) / float(n_ref))
+        # the start-row refraction offsets (RoffsetS - Roffset, metres)
+        txt = run([str(ATMREF), "roffset", "WFsim.conf", repr(slam), repr(float(lam_ref)), repr(slam),
+                   repr(c["zangle"])] + [repr(row[0]) for row in c["profile"]], td)
+        roffset = [float(line.split()[2]) for line in txt.splitlines() if line.startswith("ROFF")]
+    out = dict(screens=np.stack(screens), scoeff=np.array(scoeff), roffset=np.array(roffset), **cubes,
+               profile=np.array(c["profile"]), params=np.array([M, c["W"], c["Wout"], c["nframes"], c["lam_ref_um"],
+                                                                c["slam_um"], c["seeing"], c["pupil"], c["dt"],
+                                                                c["bin"], c["seed"], c["zangle"], c["src"][0],
+                                                                c["src"][1]]))
+    return out
+
+
+def main():
+    if not ATMREF.exists():
+        sys.path.insert(0, str(ROOT / "oracle" / "ref"))
+        import build_ref
+        build_ref.build()
+    np.savez_compressed(HERE / "fresnel.npz", **make_fresnel())
+    for name, case in MKWFS_CASES.items():
+        np.savez_compressed(HERE / f"{name}.npz", **make_mkwfs(case))
+    print("wrote", ", ".join(["fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,51 @@
+"""GPU engine (through the C ABI) against the reference's own outputs
+(tests/golden/, written by the reference's code on the same inputs).
+
+Tolerances (FP32 engine vs the reference's FP32 arrays):
+  * master screens from the same Philox noise: relative max error <= 1e-4;
+  * Fresnel hop: relative max error <= 2e-5;
+  * series cubes: wrapped phase error <= 0.05 nm rms, amplitude error
+    <= 2e-3, OPD rms and amplitude variance within 1e-4 relative; the
+    unwrapped phase may differ by a 2 pi jump on at most 0.2 % of pixels.
+"""
+import numpy as np
+import pytest
+
+import golden_case as gcm
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", gcm.CASES)
+def test_gpu_master_screens_match_reference(lib, name):
+    from atmosphericturbulencesimul_gb300 import master_screen
+    gc = gcm.load(name)
+    for l in range(len(gc.alt)):
+        s, _, _ = master_screen(gc.seed, gc.M, gc.outer[l] / gc.pupil, gc.inner[l] / gc.pupil, stream=l)
+        ref = gc.screens[l]
+        assert np.abs(s - ref).max() / np.abs(ref).max() < 1e-4, l
+
+
+def test_gpu_fresnel_matches_reference(lib):
+    from atmosphericturbulencesimul_gb300 import fresnel
+    g = np.load(gcm.GOLDEN / "fresnel.npz")
+    for k in range(2):
+        n, dx, z, lam = g[f"par{k}"]
+        got = fresnel(g[f"in{k}"], float(dx), float(z), float(lam))
+        ref = g[f"out{k}"]
+        assert np.abs(got - ref).max() / np.abs(ref).max() < 2e-5, k
+
+
+@pytest.mark.parametrize("name", gcm.CASES)
+def test_gpu_series_matches_reference(lib, name):
+    gc = gcm.load(name)
+    got = gcm.run_gpu(gc)
+    for key, lam in (("ref", gc.lam_ref), ("sci", gc.slam)):
+        for f in range(gc.nframes):
+            e = gcm.frame_errors(got[key + "_pha"][f], got[key + "_amp"][f], gc.cubes[key + "_pha"][f],
+                                 gc.cubes[key + "_amp"][f], lam)
+            assert e["wrapped_rms_nm"] < 0.05, (key, f, e)
+            assert e["amp_max_err"] < 2e-3, (key, f, e)
+            assert e["flip_frac"] < 2e-3, (key, f, e)
+            assert e["opd_rms_rel"] < 1e-4 or e["flip_frac"] > 0, (key, f, e)
+            assert e["amp_var_rel"] < 1e-4, (key, f, e)
