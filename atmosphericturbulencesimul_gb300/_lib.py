@@ -1,4 +1,5 @@
-"""ctypes binding of libatmwfs.so (the C ABI declared in include/atmwfs.h).
+"""ctypes binding of libatmwfs.so (the C ABI declared in include/atmwfs.h and
+include/atmwfs_mkwfs.h).
 
 The library is the only compute path: if it is missing or cannot be loaded
 this module raises; there is no CPU fallback.
@@ -62,6 +63,59 @@ class Sink(C.Structure):
     _fields_ = [("pha", C.POINTER(C.c_float)), ("amp", C.POINTER(C.c_float)), ("nslots", C.c_long)]
 
 
+class Conf(C.Structure):
+    """atmwfs_conf: the CONF_* values of the configuration file."""
+    _fields_ = [
+        ("lambda_", C.c_float),
+        ("seeing", C.c_float),
+        ("prof_file", C.c_char * 200),
+        ("zangle", C.c_float),
+        ("source_xpos", C.c_float),
+        ("source_ypos", C.c_float),
+        ("wfoutput", C.c_int),
+        ("wf_file_prefix", C.c_char * 200),
+        ("shm_output", C.c_int),
+        ("make_swavefront", C.c_int),
+        ("swf_write2disk", C.c_int),
+        ("swf_file_prefix", C.c_char * 200),
+        ("shm_soutput", C.c_int),
+        ("shm_sprefix", C.c_char * 100),
+        ("shm_soutputm", C.c_int),
+        ("pupil_scale", C.c_float),
+        ("wfsize", C.c_long),
+        ("realtime", C.c_int),
+        ("realtime_factor", C.c_double),
+        ("wftime_step", C.c_float),
+        ("time_span", C.c_float),
+        ("nb_tspan", C.c_long),
+        ("simtdelay", C.c_long),
+        ("waitforsem", C.c_int),
+        ("waitsemimname", C.c_char * 100),
+        ("skip_existing", C.c_int),
+        ("wf_raw_size", C.c_long),
+        ("master_size", C.c_long),
+        ("wavefront_amplitude", C.c_int),
+        ("fresnel_propagation", C.c_int),
+        ("fresnel_propagation_bin", C.c_float),
+        ("site_alt", C.c_float),
+    ]
+
+
+REFRACTIVITY_FN = C.CFUNCTYPE(C.c_float, C.c_float, C.c_float, C.c_void_p)
+
+
+class MkwfsOpts(C.Structure):
+    _fields_ = [
+        ("refractivity", REFRACTIVITY_FN),
+        ("refractivity_user", C.c_void_p),
+        ("scoeff", C.POINTER(C.c_double)),
+        ("roffset", C.POINTER(C.c_double)),
+        ("seed", C.c_ulonglong),
+        ("verbose", C.c_int),
+        ("semwait_timeout", C.c_double),
+    ]
+
+
 # (name, restype, argtypes) of every exported entry point
 _ctx = C.c_void_p
 _fp = C.POINTER(C.c_float)
@@ -73,6 +127,7 @@ SIGNATURES = [
     ("atmwfs_load_screen", C.c_int, [_ctx, C.c_int, _fp, C.c_long]),
     ("atmwfs_load_screen_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_long]),
     ("atmwfs_normalize_screens", C.c_int, [_ctx, C.c_float, C.c_float, _dp]),
+    ("atmwfs_normalize_screens_ext", C.c_int, [_ctx, C.c_float, C.c_float, C.POINTER(_fp), C.c_long, _dp]),
     ("atmwfs_run", C.c_int, [_ctx, C.c_long, C.POINTER(Sink)]),
     ("atmwfs_frame_dev", C.c_int, [_ctx, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     ("atmwfs_frame_floats", C.c_size_t, [_ctx]),
@@ -97,6 +152,18 @@ SIGNATURES = [
     ("atmwfs_fft2d_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_int, C.c_void_p]),
     ("atmwfs_master_screen", C.c_int, [C.c_uint64, C.c_uint32, C.c_long, C.c_double, C.c_double, _fp, _fp, _dp]),
     ("atmwfs_last_error", C.c_char_p, []),
+    # include/atmwfs_mkwfs.h
+    ("atmwfs_conf_read", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_long]),
+    ("atmwfs_conf_exists", C.c_int, [C.c_char_p, C.c_char_p]),
+    ("atmwfs_conf_load", C.c_int, [C.c_char_p, C.POINTER(Conf)]),
+    ("atmwfs_profile_read", C.c_int, [C.c_char_p, C.c_double, _dp, C.c_long, C.POINTER(C.c_long)]),
+    ("atmwfs_fits_write", C.c_int, [C.c_char_p, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_long)]),
+    ("atmwfs_fits_read_f32", C.c_int, [C.c_char_p, _fp, C.c_long, _ip, C.POINTER(C.c_long)]),
+    ("atmwfs_shm_create", C.c_int, [C.c_char_p, C.c_long, C.c_long, C.c_int, C.POINTER(C.c_void_p)]),
+    ("atmwfs_shm_write", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    ("atmwfs_shm_close", None, [C.c_void_p]),
+    ("atmwfs_shm_semwait", C.c_int, [C.c_char_p, C.c_long, C.c_double]),
+    ("atmwfs_mkwfs", C.c_int, [C.c_char_p, C.c_float, C.c_long, C.POINTER(MkwfsOpts)]),
 ]
 
 _lib = None

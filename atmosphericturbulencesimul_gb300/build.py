@@ -28,6 +28,9 @@ NVCC_FLAGS = ["-std=c++17", "--expt-relaxed-constexpr", "-O3", "-lineinfo", "-Xc
               "-Xcompiler", "-ffp-contract=off",
               "-I", str(INCLUDE), "-I", str(CSRC)]
 CC_FLAGS = ["-std=c11", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-result", "-I", str(INCLUDE), "-I", str(CSRC)]
+# host-only C++ (configuration, profile, FITS, shared memory, series driver)
+CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-result", "-I", str(INCLUDE),
+             "-I", str(CSRC)]
 
 
 def _nvcc() -> str:
@@ -61,6 +64,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     deps = _headers()
     cu = sorted(CSRC.glob("*.cu"))
     cc = sorted(CSRC.glob("*.c"))
+    cxx = sorted(CSRC.glob("*.cpp"))
     jobs_list = []
     objs = []
     for src in cu:
@@ -73,6 +77,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         objs.append(obj)
         if _stale(obj, src, deps):
             jobs_list.append(["gcc", *CC_FLAGS, "-c", str(src), "-o", str(obj)])
+    for src in cxx:
+        obj = BUILD / (src.stem + ".cpp.o")
+        objs.append(obj)
+        if _stale(obj, src, deps):
+            jobs_list.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)])
     n = jobs or max(1, min(len(jobs_list), os.cpu_count() or 4))
     if jobs_list:
         with cf.ThreadPoolExecutor(max_workers=n) as ex:

@@ -216,7 +216,7 @@ __global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __rest
     const int Nout = I.Nout, nb = I.nb;
     const long n = (long)Nout * Nout;
     const int step = d_step ? *d_step : 0;
-    float* pha = I.out_pha + (size_t)(step % I.ring) * n;
+    float* pha = I.out_pha + (size_t)(step % I.ring) * I.ostride;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const int jj = (int)(i / Nout), ii = (int)(i % Nout);
         const float peak = nb > 0 ? I.peak[I.binx[jj] * nb + I.binx[ii]] : 0.0f;

@@ -736,6 +736,7 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                 // the ring holds the frames of all instances contiguously per slot
                 d.out_pha = c->d_out_pha + c->frame_off[i];
                 d.out_amp = c->d_out_amp + c->frame_off[i];
+                d.ostride = (long)c->frame_floats;
                 CK(dalloc(c, (void**)&d.phisum, sizeof(float) * (size_t)No * No));
                 if (I.mode == ATMWFS_MODE_SCI) {
                     d.nb = No / 20;
@@ -852,33 +853,55 @@ atmwfs_status atmwfs_load_screen_dev(atmwfs_ctx* c, int layer, const float* dev,
 
 atmwfs_status atmwfs_normalize_screens(atmwfs_ctx* c, float lambda_ref, float seeing, double* r0_pix)
 {
+    return atmwfs_normalize_screens_ext(c, lambda_ref, seeing, nullptr, 0, r0_pix);
+}
+
+atmwfs_status atmwfs_normalize_screens_ext(atmwfs_ctx* c, float lambda_ref, float seeing, const float* const* extra,
+                                           long nextra, double* r0_pix)
+{
     if (!c) return fail(ATMWFS_ERR_INVALID, "null context");
+    if (nextra < 0 || (nextra > 0 && !extra)) return fail(ATMWFS_ERR_INVALID, "bad extra screens");
+    for (long e = 0; e < nextra; e++)
+        if (!extra[e]) return fail(ATMWFS_ERR_INVALID, "extra screen %ld is null", e);
     for (int l = 0; l < c->L; l++)
         if (!c->loaded[l]) return fail(ATMWFS_ERR_STATE, "screen of layer %d not loaded", l);
     const int dpix = 50;
     if (c->M <= dpix) return fail(ATMWFS_ERR_INVALID, "master_size must exceed 50 pixels");
+    // every master screen, layers first (ID_TM[0..NBMASTERS-1], :2246-2276)
+    const size_t M2 = (size_t)c->M * c->M;
+    const long nm = c->L + nextra;
+    std::vector<float*> scr(c->d_screen.begin(), c->d_screen.begin() + c->L);
     double* acc = nullptr;
-    AW_CUDA(cudaMalloc(&acc, sizeof(double) * c->L));
+    float* ext = nullptr;
+    atmwfs_status s = ATMWFS_OK;
+    if (cudaMalloc(&acc, sizeof(double) * nm) != cudaSuccess ||
+        (nextra > 0 && cudaMalloc(&ext, sizeof(float) * M2 * nextra) != cudaSuccess))
+        s = fail(ATMWFS_ERR_NOMEM, "cudaMalloc failed");
+    for (long e = 0; e < nextra && s == ATMWFS_OK; e++) {
+        scr.push_back(ext + M2 * e);
+        if (cudaMemcpyAsync(ext + M2 * e, extra[e], sizeof(float) * M2, cudaMemcpyHostToDevice, c->st) != cudaSuccess)
+            s = fail(ATMWFS_ERR_CUDA, "copy of extra screen %ld failed", e);
+    }
     auto measure = [&](double* r0) -> atmwfs_status {
-        AW_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * c->L, c->st));
-        for (int l = 0; l < c->L; l++) AW_CUDA(lag_sumsq(c->d_screen[l], (int)c->M, dpix, acc + l, c->st));
-        std::vector<double> h(c->L);
-        AW_CUDA(cudaMemcpyAsync(h.data(), acc, sizeof(double) * c->L, cudaMemcpyDeviceToHost, c->st));
+        AW_CUDA(cudaMemsetAsync(acc, 0, sizeof(double) * nm, c->st));
+        for (long k = 0; k < nm; k++) AW_CUDA(lag_sumsq(scr[k], (int)c->M, dpix, acc + k, c->st));
+        std::vector<double> h(nm);
+        AW_CUDA(cudaMemcpyAsync(h.data(), acc, sizeof(double) * nm, cudaMemcpyDeviceToHost, c->st));
         AW_CUDA(cudaStreamSynchronize(c->st));
         const double cnt = (double)(c->M - dpix) * (double)c->M;
         double tot = 0.0;
-        for (int l = 0; l < c->L; l++) tot += 1.0 * dpix * pow((h[l] / cnt) / 6.88, -3.0 / 5.0);
-        *r0 = tot / c->L;
+        for (long k = 0; k < nm; k++) tot += 1.0 * dpix * pow((h[k] / cnt) / 6.88, -3.0 / 5.0);
+        *r0 = tot / nm;
         return ATMWFS_OK;
     };
     double r0a = 0, r0b = 0;
-    atmwfs_status s = measure(&r0a);
+    if (s == ATMWFS_OK) s = measure(&r0a);
     if (s == ATMWFS_OK) {
         // r0 target (:2278-2285): lambda / seeing[rad] / pixel scale
         const double target = lambda_ref / (seeing / 3600.0 / 180.0 * kPi) / c->pupil * 1;
         const double tmp1 = pow(r0a / target, 5.0 / 6.0);
-        for (int l = 0; l < c->L && s == ATMWFS_OK; l++)
-            if (scale_screen(c->d_screen[l], c->M * c->M, tmp1, c->st) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "scale failed");
+        for (long k = 0; k < nm && s == ATMWFS_OK; k++)
+            if (scale_screen(scr[k], c->M * c->M, tmp1, c->st) != cudaSuccess) s = fail(ATMWFS_ERR_CUDA, "scale failed");
         if (s == ATMWFS_OK) s = measure(&r0b);
         // per-layer weight sqrt(Cn2 / cos(zenith)) (:2340-2363)
         for (int l = 0; l < c->L && s == ATMWFS_OK; l++)
@@ -887,6 +910,7 @@ atmwfs_status atmwfs_normalize_screens(atmwfs_ctx* c, float lambda_ref, float se
     }
     cudaStreamSynchronize(c->st);
     cudaFree(acc);
+    if (ext) cudaFree(ext);
     if (s != ATMWFS_OK) return s;
     if (r0_pix) { r0_pix[0] = r0a; r0_pix[1] = r0b; }
     c->normalized = true;

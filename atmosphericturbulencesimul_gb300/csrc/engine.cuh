@@ -23,8 +23,9 @@ struct InstDev {
     float2* fld[2];            // ping-pong N x N fields
     const float2* H;           // hop transfer tables, [P][N], 1-D, include 1/N
     float scoeff[kMaxLayers];  // per-layer phase multiplier
-    float* out_pha;            // output ring [ring][Nout*Nout]
+    float* out_pha;            // this instance's frame in output slot 0; slot k at + k * ostride
     float* out_amp;
+    long ostride;              // floats between output slots (the frames of all instances)
     float* phisum;             // geometric phase sum of the crop [Nout*Nout] (k_phasum)
     float* bins;               // science scratch: [2][nb*nb] (re, im) sums
     float* peak;               // science scratch: unwrapped bin phase [nb*nb]

@@ -1,0 +1,353 @@
+// host_mkwfs.cpp -- the series command on top of the GPU engine: the
+// reference's make_AtmosphericTurbulence_wavefront_series()
+// (src/AtmosphericTurbulence/AtmosphericTurbulence.c:1433-4455) as a host
+// driver that reads the same files, feeds atmwfs_run() and writes the same
+// FITS cubes and shared-memory streams.
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "atmwfs.h"
+#include "atmwfs_mkwfs.h"
+
+namespace atmwfs {
+void set_error_message(const char* msg);
+}
+
+namespace {
+
+atmwfs_status err(atmwfs_status s, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    atmwfs::set_error_message(buf);
+    return s;
+}
+
+#define MK_TRY(x)                                      \
+    do {                                               \
+        const atmwfs_status s_ = (x);                  \
+        if (s_ != ATMWFS_OK) return s_;                \
+    } while (0)
+
+bool file_exists(const std::string& name)
+{
+    FILE* f = fopen(name.c_str(), "r");
+    if (!f) return false;
+    fclose(f);
+    return true;
+}
+
+// `touch`: create the file if absent, else update its times (:4362-4375)
+atmwfs_status touch(const std::string& name)
+{
+    const int fd = open(name.c_str(), O_WRONLY | O_CREAT, 0666);
+    if (fd < 0) return err(ATMWFS_ERR_IO, "cannot touch \"%s\"", name.c_str());
+    futimens(fd, nullptr);
+    close(fd);
+    return ATMWFS_OK;
+}
+
+std::string fmt(const char* f, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, f);
+    vsnprintf(buf, sizeof buf, f, ap);
+    va_end(ap);
+    return buf;
+}
+
+// Dry standard air (Ciddor 1996, eq. 1; sigma in 1/um) thinned with an 8 km
+// exponential scale height: the refractivity used when the caller brings
+// no atmosphere model.
+float builtin_refractivity(float alt, float lambda, void*)
+{
+    double s2 = 1.0 / ((double)lambda * 1e6);
+    s2 *= s2;
+    const double nas = 1e-8 * (5792105.0 / (238.0185 - s2) + 167917.0 / (57.362 - s2));
+    return (float)(nas * exp(-(double)alt / 8000.0));
+}
+
+atmwfs_status write_cube(const std::string& name, const std::vector<float>& cube, long w, long nframes, long precision)
+{
+    const long ax[3] = {w, w, nframes};
+    if (precision == 0) return atmwfs_fits_write(name.c_str(), cube.data(), -32, 3, ax);
+    std::vector<double> d(cube.begin(), cube.end());
+    return atmwfs_fits_write(name.c_str(), d.data(), -64, 3, ax);
+}
+
+struct Resources {
+    atmwfs_ctx* ctx = nullptr;
+    atmwfs_shm* shm[4] = {nullptr, nullptr, nullptr, nullptr};
+    ~Resources()
+    {
+        for (atmwfs_shm* s : shm)
+            if (s) atmwfs_shm_close(s);
+        if (ctx) atmwfs_destroy(ctx);
+    }
+};
+
+}  // namespace
+
+extern "C" atmwfs_status atmwfs_mkwfs(const char* conf_file, float slambda_um, long precision,
+                                      const atmwfs_mkwfs_opts* o)
+{
+    atmwfs_mkwfs_opts opts;
+    memset(&opts, 0, sizeof opts);
+    if (o) opts = *o;
+    if (precision != 0 && precision != 1) return err(ATMWFS_ERR_INVALID, "precision must be 0 (float) or 1 (double)");
+    if (!(slambda_um > 0)) return err(ATMWFS_ERR_INVALID, "science wavelength must be > 0");
+    atmwfs_conf cf;
+    MK_TRY(atmwfs_conf_load(conf_file, &cf));
+    const double SLAMBDA = 1.0e-6 * slambda_um;                       // :1623
+    const long W = cf.wf_raw_size, Wout = cf.wfsize, M = cf.master_size;
+    if (W < 1 || Wout < 1 || Wout > W) return err(ATMWFS_ERR_INVALID, "WF_RAW_SIZE %ld / WFsize %ld", W, Wout);
+    const long ratio = W / Wout;                                       // :1855-1870
+    if (ratio != 1 && ratio != 2 && ratio != 4 && ratio != 8)
+        return err(ATMWFS_ERR_INVALID, "unknown contraction factor (WF_RAW_SIZE / WFsize = %ld)", ratio);
+    const long nframes = (long)(1.0 * cf.time_span / cf.wftime_step + 0.5);   // :1876
+    if (nframes < 1) return err(ATMWFS_ERR_INVALID, "TIME_SPAN / WFTIME_STEP gives %ld frames", nframes);
+    if (M < 64) return err(ATMWFS_ERR_INVALID, "MASTER_SIZE %ld", M);
+    const bool verbose = opts.verbose != 0;
+
+    // master screen files already present (:1925-1945)
+    const char sfx = precision == 0 ? 'f' : 'd';
+    auto master_name = [&](long i) { return fmt("t%03ld_%ld_%c.fits", i, M, sfx); };
+    long nmasters = 0;
+    while (file_exists(master_name(nmasters))) nmasters++;
+
+    // profile (:1946-2015)
+    long L = 0;
+    MK_TRY(atmwfs_profile_read(cf.prof_file, (double)cf.site_alt, nullptr, 0, &L));
+    if (L < 1) return err(ATMWFS_ERR_INVALID, "no layer in profile \"%s\"", cf.prof_file);
+    std::vector<double> prof((size_t)L * 8);
+    MK_TRY(atmwfs_profile_read(cf.prof_file, (double)cf.site_alt, prof.data(), L, &L));
+    std::vector<double> alt(L), cn2(L), spd(L), dir(L), outer(L), inner(L);
+    for (long l = 0; l < L; l++) {
+        alt[l] = prof[l * 8 + 0];
+        cn2[l] = prof[l * 8 + 1];
+        spd[l] = prof[l * 8 + 2];
+        dir[l] = prof[l * 8 + 3];
+        outer[l] = prof[l * 8 + 4];
+        inner[l] = prof[l * 8 + 5];
+    }
+    if (nmasters < L) nmasters = L;                                    // :2205-2206
+
+    // load, or synthesise and save, every master screen (:2207-2226)
+    const size_t M2 = (size_t)M * M;
+    std::vector<std::vector<float>> screens(nmasters);
+    for (long i = 0; i < nmasters; i++) {
+        screens[i].resize(M2);
+        const std::string fn = master_name(i);
+        if (file_exists(fn)) {
+            int nax = 0;
+            long ax[3];
+            MK_TRY(atmwfs_fits_read_f32(fn.c_str(), nullptr, 0, &nax, ax));
+            if (nax != 2 || ax[0] != M || ax[1] != M)
+                return err(ATMWFS_ERR_INVALID, "\"%s\" is %ld x %ld, MASTER_SIZE is %ld", fn.c_str(), ax[0], ax[1], M);
+            MK_TRY(atmwfs_fits_read_f32(fn.c_str(), screens[i].data(), (long)M2, &nax, ax));
+        } else {
+            if (verbose) printf("CREATING %s   (%f - %f)\n", fn.c_str(), outer[i] / cf.pupil_scale, inner[i] / cf.pupil_scale);
+            std::vector<float> second(M2);
+            double cfit[2];
+            MK_TRY(atmwfs_master_screen(opts.seed, (uint32_t)i, M, outer[i] / cf.pupil_scale, inner[i] / cf.pupil_scale,
+                                        screens[i].data(), second.data(), cfit));
+            const long ax[2] = {M, M};
+            if (precision == 0) {
+                MK_TRY(atmwfs_fits_write(fn.c_str(), screens[i].data(), -32, 2, ax));
+            } else {
+                std::vector<double> d(screens[i].begin(), screens[i].end());
+                MK_TRY(atmwfs_fits_write(fn.c_str(), d.data(), -64, 2, ax));
+            }
+        }
+    }
+
+    // chromatic phase scaling and refraction offsets per layer
+    const atmwfs_refractivity_fn N = opts.refractivity ? opts.refractivity : builtin_refractivity;
+    void* user = opts.refractivity ? opts.refractivity_user : nullptr;
+    std::vector<double> scoeff(L), roff(L);
+    for (long l = 0; l < L; l++) {
+        if (opts.scoeff) {
+            scoeff[l] = opts.scoeff[l];
+        } else {                                                       // :2661-2663
+            const double Nl = N((float)alt[l], cf.lambda, user);
+            const double Ns = N((float)alt[l], (float)SLAMBDA, user);
+            scoeff[l] = cf.lambda / SLAMBDA * Ns / Nl;
+        }
+        if (opts.roffset) {
+            roff[l] = opts.roffset[l];
+        } else {                                                       // :2159-2183
+            const double sz = sin(cf.zangle);
+            double off[2] = {0.0, 0.0};
+            if (sz != 0.0)
+                for (int w = 0; w < 2; w++)
+                    for (double h = cf.site_alt; h < alt[l]; h += 1.0) {
+                        const double n = 1.0 + N((float)h, w == 0 ? cf.lambda : (float)SLAMBDA, user);
+                        double t = sz / sqrt(n * n - sz * sz);
+                        t -= sz / sqrt(1.0 - sz * sz);
+                        off[w] += t;
+                    }
+            roff[l] = off[1] - off[0];
+        }
+    }
+
+    // instances: the reference wavelength (files or stream) and the science one
+    const bool amp = cf.wavefront_amplitude == 1;
+    const bool ref_on = cf.wfoutput == 1 || cf.shm_output == 1;
+    const bool sci_on = cf.make_swavefront == 1;
+    std::vector<float> sc_f(L);
+    for (long l = 0; l < L; l++) sc_f[l] = (float)scoeff[l];
+    atmwfs_instance inst[2];
+    memset(inst, 0, sizeof inst);
+    int ni = 0, iref = -1, isci = -1;
+    if (ref_on) {
+        // one set of window positions serves both wavelengths, so the
+        // reference wavelength also carries the refraction offsets (:2183)
+        inst[ni] = atmwfs_instance{(double)cf.lambda, amp ? ATMWFS_MODE_REF : ATMWFS_MODE_PHASE, cf.source_xpos,
+                                   cf.source_ypos, W, Wout, nullptr, roff.data()};
+        iref = ni++;
+    }
+    if (sci_on) {
+        inst[ni] = atmwfs_instance{SLAMBDA, amp ? ATMWFS_MODE_SCI : ATMWFS_MODE_PHASE, cf.source_xpos, cf.source_ypos,
+                                   W, Wout, sc_f.data(), roff.data()};
+        isci = ni++;
+    }
+
+    Resources R;
+    std::vector<float> hpha, hamp;
+    long ff = 0, off_ref = 0, off_sci = 0;
+    const bool stepwise = cf.realtime == 1 || cf.shm_output == 1 || cf.shm_soutput == 1 || cf.waitforsem == 1 ||
+                          cf.simtdelay > 0;
+    if (ni > 0) {
+        atmwfs_params p;
+        memset(&p, 0, sizeof p);
+        p.nlayers = (int)L;
+        p.alt = alt.data();
+        p.cn2 = cn2.data();
+        p.speed = spd.data();
+        p.dir = dir.data();
+        p.fresnel_bin = cf.fresnel_propagation_bin;
+        p.zangle = cf.zangle;
+        p.pupil_scale = cf.pupil_scale;
+        p.time_step = cf.wftime_step;
+        p.master_size = M;
+        p.amplitude = amp ? 1 : 0;
+        p.fresnel = cf.fresnel_propagation;
+        p.realtime = cf.realtime;
+        p.realtime_factor = cf.realtime_factor;
+        p.ninst = ni;
+        p.inst = inst;
+        p.ring = 2;
+        MK_TRY(atmwfs_create(&p, &R.ctx));
+        for (long l = 0; l < L; l++) MK_TRY(atmwfs_load_screen(R.ctx, (int)l, screens[l].data(), M));
+        std::vector<const float*> extra;
+        for (long i = L; i < nmasters; i++) extra.push_back(screens[i].data());
+        double r0[2];
+        MK_TRY(atmwfs_normalize_screens_ext(R.ctx, cf.lambda, cf.seeing, extra.data(), (long)extra.size(), r0));
+        if (verbose) printf("r0 = %g pix -> %g pix\n", r0[0], r0[1]);
+        ff = atmwfs_frame_floats(R.ctx);
+        if (iref >= 0) off_ref = atmwfs_frame_offset(R.ctx, iref);
+        if (isci >= 0) off_sci = atmwfs_frame_offset(R.ctx, isci);
+        hpha.resize((size_t)ff * nframes);
+        hamp.resize((size_t)ff * nframes);
+    }
+    screens.clear();
+
+    // shared-memory streams (:2425-2483)
+    const int dtype = precision == 0 ? 3 : 4;
+    if (cf.shm_output == 1) {
+        MK_TRY(atmwfs_shm_create("atmwfpha", Wout, Wout, dtype, &R.shm[0]));
+        MK_TRY(atmwfs_shm_create("atmwfamp", Wout, Wout, dtype, &R.shm[1]));
+    }
+    if (cf.shm_soutput == 1) {
+        MK_TRY(atmwfs_shm_create((std::string(cf.shm_sprefix) + "pha").c_str(), Wout, Wout, dtype, &R.shm[2]));
+        MK_TRY(atmwfs_shm_create((std::string(cf.shm_sprefix) + "amp").c_str(), Wout, Wout, dtype, &R.shm[3]));
+    }
+    // stream scale of the science phase (:4287-4300)
+    double coeff = 1.0;
+    if (cf.shm_soutputm == 1) coeff = SLAMBDA / 2.0 / M_PI;
+    if (cf.shm_soutputm == 2) coeff = SLAMBDA / 2.0 / M_PI * 1e6;
+    const size_t fr = (size_t)Wout * Wout;
+    std::vector<double> dbuf(fr);
+    std::vector<float> fbuf(fr);
+    auto stream = [&](atmwfs_shm* s, const float* src, double k, int bump) -> atmwfs_status {
+        if (!s) return ATMWFS_OK;
+        if (dtype == 3) {
+            for (size_t i = 0; i < fr; i++) fbuf[i] = (float)(src[i] * k);
+            return atmwfs_shm_write(s, fbuf.data(), bump);
+        }
+        for (size_t i = 0; i < fr; i++) dbuf[i] = src[i] * k;
+        return atmwfs_shm_write(s, dbuf.data(), bump);
+    };
+
+    const long lam_pm = (long)(1.0e12 * SLAMBDA + 0.5);
+    long start = 0;                                                    // :2489-2511
+    if (cf.skip_existing == 1)
+        while (file_exists(fmt("%s%08ld.%09ld.pha.fits", cf.swf_file_prefix, start, lam_pm))) start++;
+
+    std::vector<float> cube((size_t)fr * nframes);
+    auto gather = [&](const std::vector<float>& src, long off) {
+        for (long f = 0; f < nframes; f++)
+            memcpy(&cube[(size_t)f * fr], &src[(size_t)f * ff + off], sizeof(float) * fr);
+    };
+    for (long tspan = start; tspan < cf.nb_tspan; tspan++) {
+        if (ni > 0) {
+            if (stepwise) {
+                for (long f = 0; f < nframes; f++) {
+                    if (cf.simtdelay > 0) usleep((useconds_t)cf.simtdelay);
+                    if (cf.waitforsem == 1) MK_TRY(atmwfs_shm_semwait(cf.waitsemimname, 0, opts.semwait_timeout));
+                    atmwfs_sink sk{hpha.data() + (size_t)f * ff, hamp.data() + (size_t)f * ff, 1};
+                    MK_TRY(atmwfs_run(R.ctx, 1, &sk));
+                    if (iref >= 0) {
+                        MK_TRY(stream(R.shm[0], sk.pha + off_ref, 1.0, 0));
+                        MK_TRY(stream(R.shm[1], sk.amp + off_ref, 1.0, 0));
+                    }
+                    if (isci >= 0) {
+                        MK_TRY(stream(R.shm[2], sk.pha + off_sci, coeff, 1));
+                        MK_TRY(stream(R.shm[3], sk.amp + off_sci, 1.0, 1));
+                    }
+                }
+            } else {
+                atmwfs_sink sk{hpha.data(), hamp.data(), nframes};
+                MK_TRY(atmwfs_run(R.ctx, nframes, &sk));
+            }
+        }
+        if (verbose) printf("time span %ld / %ld: %ld frames\n", tspan, cf.nb_tspan, nframes);
+        // reference-wavelength files, named with the science wavelength (:4349-4376)
+        const std::string rp = fmt("%s%08ld.%09ld.pha.fits", cf.wf_file_prefix, tspan, lam_pm);
+        const std::string ra = fmt("%s%08ld.%09ld.amp.fits", cf.wf_file_prefix, tspan, lam_pm);
+        if (cf.wfoutput == 1) {
+            gather(hpha, off_ref);
+            MK_TRY(write_cube("!" + rp, cube, Wout, nframes, precision));
+            if (amp) {
+                gather(hamp, off_ref);
+                MK_TRY(write_cube("!" + ra, cube, Wout, nframes, precision));
+            }
+        } else if (cf.wfoutput == 0) {
+            MK_TRY(touch(rp));
+            if (amp) MK_TRY(touch(ra));
+        }
+        if (sci_on && cf.swf_write2disk == 1) {                        // :4380-4400
+            gather(hpha, off_sci);
+            MK_TRY(write_cube("!" + fmt("%s%08ld.%09ld.pha.fits", cf.swf_file_prefix, tspan, lam_pm), cube, Wout,
+                              nframes, precision));
+            if (amp) {
+                gather(hamp, off_sci);
+                MK_TRY(write_cube("!" + fmt("%s%08ld.%09ld.amp.fits", cf.swf_file_prefix, tspan, lam_pm), cube, Wout,
+                                  nframes, precision));
+            }
+        }
+    }
+    return ATMWFS_OK;
+}

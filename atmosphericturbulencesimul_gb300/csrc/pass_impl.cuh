@@ -337,8 +337,8 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         constexpr int CPT = (N + NT - 1) / NT;  // columns per thread
         const int off = I->off, Nout = I->Nout, mode = I->mode;
         const int slot = step % I->ring;
-        float* __restrict__ opha = I->out_pha + (size_t)slot * Nout * Nout;
-        float* __restrict__ oamp = I->out_amp + (size_t)slot * Nout * Nout;
+        float* __restrict__ opha = I->out_pha + (size_t)slot * I->ostride;
+        float* __restrict__ oamp = I->out_amp + (size_t)slot * I->ostride;
         const float* __restrict__ psum = I->phisum;
         __syncthreads();  // phasor reads of phi are done
 #pragma unroll

@@ -103,6 +103,12 @@ atmwfs_status atmwfs_load_screen_dev(atmwfs_ctx* ctx, int layer, const float* de
  * r0_pix[0..1] receives the mean r0 before and after renormalisation. */
 atmwfs_status atmwfs_normalize_screens(atmwfs_ctx* ctx, float lambda_ref, float seeing, double* r0_pix);
 
+/* The same with further M x M host screens that enter the mean r0 but are
+ * not layers: the reference averages r0 over every master file present in
+ * the directory (:2246-2285), also files beyond the number of layers. */
+atmwfs_status atmwfs_normalize_screens_ext(atmwfs_ctx* ctx, float lambda_ref, float seeing, const float* const* extra,
+                                           long nextra, double* r0_pix);
+
 /* Run nsteps time steps (the frame loop, :2561-4345).  Frames of step s of
  * this call are written at offset s * wf_size^2 of the sink buffers. */
 atmwfs_status atmwfs_run(atmwfs_ctx* ctx, long nsteps, const atmwfs_sink* sink);

@@ -16,6 +16,10 @@
  *   atmref stdN <conf> <lambda_model> <alt> <lambda> [<alt> <lambda> ...]
  *       AtmosphereModel_Create_from_CONF then AtmosphereModel_stdAtmModel_N
  *       (src/AtmosphereModel/AtmosphereModel.c:3212) for each pair.
+ *   atmref conf <conf> <keyword>...
+ *       read_config_parameter_exists and read_config_parameter
+ *       (src/COREMOD_tools/COREMOD_tools.c:596-666) for each keyword; one
+ *       line "CONF <keyword> <exists> <found> [<content>]" each.
  *   atmref roffset <conf> <lambda_model> <lambda_ref> <slambda> <zangle> <alt>...
  *       the per-layer refraction offset RoffsetS - Roffset [m] that
  *       make_AtmosphericTurbulence_wavefront_series adds to the start row
@@ -120,6 +124,21 @@ static int cmd_stdn(int argc, char **argv)
     return 0;
 }
 
+int read_config_parameter_exists(char *config_file, char *keyword);
+int read_config_parameter(char *config_file, char *keyword, char *content);
+
+static int cmd_conf(int argc, char **argv)
+{
+    if (argc < 4) return 2;
+    for (int i = 3; i < argc; i++) {
+        char content[1000];
+        const int ex = read_config_parameter_exists(argv[2], argv[i]);
+        const int rd = read_config_parameter(argv[2], argv[i], content);
+        printf("CONF\t%s\t%d\t%d\t%s\n", argv[i], ex, rd, content);
+    }
+    return 0;
+}
+
 extern float SiteAlt;
 
 static int cmd_roffset(int argc, char **argv)
@@ -159,5 +178,6 @@ int main(int argc, char **argv)
     }
     if (strcmp(argv[1], "stdN") == 0) return cmd_stdn(argc, argv);
     if (strcmp(argv[1], "roffset") == 0) return cmd_roffset(argc, argv);
+    if (strcmp(argv[1], "conf") == 0) return cmd_conf(argc, argv);
     return 2;
 }

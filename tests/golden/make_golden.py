@@ -18,7 +18,9 @@ Run from the repository root where the reference is mounted:
 """
 from __future__ import annotations
 
+import json
 import os
+import re
 import subprocess
 import sys
 import tempfile
@@ -54,6 +56,26 @@ MKWFS_CASES = {
                  (50.0, 0.2, 12.0, 1.0, 25.0, 0.01, 1.0, 10.0),
                  (5000.0, 0.3, 25.0, 3.0, 25.0, 0.01, 1.0, 10.0),
                  (12000.0, 0.1, 30.0, 5.5, 25.0, 0.01, 1.0, 10.0)]),
+    # phase only (WAVEFRONT_AMPLITUDE 0), a 64 crop of a 128 grid, two time
+    # spans; the profile file has comments, a blank line after a layer (the
+    # reference repeats that layer) and a short line (missing columns keep
+    # the previous line's values); PUPIL_SCALE appears twice (last wins)
+    "mkwfs_c": dict(
+        M=128, W=128, Wout=64, nframes=2, ntspan=2, amplitude=0, lam_ref_um=0.5, slam_um=1.25, seeing=0.6875,
+        pupil=0.01, dt=0.001, bin=100.0, seed=5, zangle=0.0, src=(0.0, 0.0),
+        conf_prefix="PUPIL_SCALE 0.05\n",
+        prof_text="# alt cn2 speed dir L0 l0 sigma Lwind\n0 0.5 10 0.5236 20 0.01 1 10\n\n"
+                  "2500 0.3 20 2.0 20 0.01 1 10\n  # indented comment\n8000.0 0.2 15 4.0 25\n",
+        profile=[(0.0, 0.5, 10.0, 0.5236, 20.0, 0.01, 1.0, 10.0),
+                 (0.0, 0.5, 10.0, 0.5236, 20.0, 0.01, 1.0, 10.0),
+                 (2500.0, 0.3, 20.0, 2.0, 20.0, 0.01, 1.0, 10.0),
+                 (8000.0, 0.2, 15.0, 4.0, 25.0, 0.01, 1.0, 10.0)]),
+    # double precision (mkwfs <lambda> 1): _d master screens and BITPIX -64 cubes
+    "mkwfs_d": dict(
+        M=128, W=64, Wout=32, nframes=2, lam_ref_um=0.5, slam_um=2.2, seeing=0.6875, pupil=0.01, dt=0.001,
+        bin=100.0, seed=11, zangle=0.0, src=(0.0, 0.0), precision=1,
+        profile=[(0.0, 0.6, 9.0, 1.0, 20.0, 0.01, 1.0, 10.0),
+                 (6000.0, 0.4, 21.0, 2.5, 20.0, 0.01, 1.0, 10.0)]),
 }
 
 
@@ -69,9 +91,9 @@ def conf_text(c: dict) -> str:
         ("SLAMBDA", f"{c['slam_um']:f}"), ("SWF_WRITE2DISK", "1"), ("SWF_FILE_PREFIX", "./WFS_files/wf_"),
         ("SHM_SOUTPUT", "0"), ("SHM_SPREFIX", "outwf"), ("SHM_SOUTPUTM", "2"), ("WFsize", str(c["Wout"])),
         ("PUPIL_SCALE", f"{c['pupil']:f}"), ("REALTIME", "0"), ("REALTIMEFACTOR", "1.0"),
-        ("WFTIME_STEP", f"{c['dt']:f}"), ("TIME_SPAN", f"{c['dt'] * c['nframes']:f}"), ("NB_TSPAN", "1"),
+        ("WFTIME_STEP", f"{c['dt']:f}"), ("TIME_SPAN", f"{c['dt'] * c['nframes']:f}"), ("NB_TSPAN", str(c.get("ntspan", 1))),
         ("SIMTDELAY", "0"), ("WAITFORSEM", "0"), ("WAITSEMIMNAME", "wfsimwait"),
-        ("WF_RAW_SIZE", str(c["W"])), ("MASTER_SIZE", str(c["M"])), ("WAVEFRONT_AMPLITUDE", "1"),
+        ("WF_RAW_SIZE", str(c["W"])), ("MASTER_SIZE", str(c["M"])), ("WAVEFRONT_AMPLITUDE", str(c.get("amplitude", 1))),
         ("FRESNEL_PROPAGATION", "1"), ("FRESNEL_PROPAGATION_BIN", f"{c['bin']:f}"),
     ]
     return "\n".join(f"{k:25s} {v:>20s}  # generated" for k, v in kv) + "\n"
@@ -100,16 +122,25 @@ def make_fresnel() -> dict:
     return out
 
 
+LAYER_LOG = re.compile(r"Turbulence layer (\d+) : alt = (\S+) m\s+CN2 = (\S+)\s+V = (\S+) m/s\s+Angle = (\S+) rad"
+                       r"\s+outerscale = (\S+) m\s+innerscale = (\S+) m\s+sigmaWind = (\S+) m/s\s+Lwind = (\S+) m")
+
+
 def make_mkwfs(c: dict) -> dict:
     M, L = c["M"], len(c["profile"])
+    prec = c.get("precision", 0)
+    ntspan = c.get("ntspan", 1)
+    amp = c.get("amplitude", 1)
     o64 = orc.Oracle(64)
+    conf = c.get("conf_prefix", "") + conf_text(c)
+    prof = c.get("prof_text") or ("# alt cn2 speed dir L0 l0 sigmawind Lwind\n" + "".join(
+        " ".join(f"{v:g}" for v in row) + "\n" for row in c["profile"]))
     with tempfile.TemporaryDirectory() as td:
         td = Path(td)
         (td / "WF_files").mkdir()
         (td / "WFS_files").mkdir()
-        (td / "WFsim.conf").write_text(conf_text(c))
-        (td / "turbul.prof").write_text("# alt cn2 speed dir L0 l0 sigmawind Lwind\n" + "".join(
-            " ".join(f"{v:g}" for v in row) + "\n" for row in c["profile"]))
+        (td / "WFsim.conf").write_text(conf)
+        (td / "turbul.prof").write_text(prof)
         # the wind-scatter series is unused by the loop: pre-create it
         for l in range(L):
             fitsio.write(td / f"wspeed_{l:03d}.fits", np.zeros((3, 8), np.float32))
@@ -119,13 +150,16 @@ def make_mkwfs(c: dict) -> dict:
             noise += [u, g]
         np.concatenate([x.ravel() for x in noise]).astype(np.float32).tofile(td / "noise.f32")
         env = dict(os.environ, ATMREF_NOISE=str(td / "noise.f32"), ATMREF_NOISE_M=str(M))
-        run([str(ATMREF), "mkwfs", f"{c['slam_um']}", "0"], td, env)
-        screens = [fitsio.read(td / f"t{l:03d}_{M}_f.fits") for l in range(L)]
+        log = run([str(ATMREF), "mkwfs", f"{c['slam_um']}", str(prec)], td, env)
+        logprof = np.array([[float(x) for x in m.groups()[1:]] for m in LAYER_LOG.finditer(log)])
+        sfx = "f" if prec == 0 else "d"
+        screens = [fitsio.read(td / f"t{l:03d}_{M}_{sfx}.fits") for l in range(L)]
         lam_pm = int(c["slam_um"] * 1e-6 * 1e12 + 0.5)
         cubes = {}
         for key, pre in (("ref", "WF_files/wf_"), ("sci", "WFS_files/wf_")):
-            for q in ("pha", "amp"):
-                cubes[f"{key}_{q}"] = fitsio.read(td / f"{pre}{0:08d}.{lam_pm:09d}.{q}.fits")
+            for q in ("pha", "amp") if amp else ("pha",):
+                cubes[f"{key}_{q}"] = np.concatenate(
+                    [fitsio.read(td / f"{pre}{t:08d}.{lam_pm:09d}.{q}.fits") for t in range(ntspan)])
         # Scoeff(h) = CONF_LAMBDA/SLAMBDA * N(h, SLAMBDA)/N(h, CONF_LAMBDA) from the
         # reference's atmosphere model, with its float operands (:2661-2663)
         lam_ref = np.float32(c["lam_ref_um"] * 1e-6)
@@ -144,11 +178,42 @@ def make_mkwfs(c: dict) -> dict:
                    repr(c["zangle"])] + [repr(row[0]) for row in c["profile"]], td)
         roffset = [float(line.split()[2]) for line in txt.splitlines() if line.startswith("ROFF")]
     out = dict(screens=np.stack(screens), scoeff=np.array(scoeff), roffset=np.array(roffset), **cubes,
-               profile=np.array(c["profile"]), params=np.array([M, c["W"], c["Wout"], c["nframes"], c["lam_ref_um"],
-                                                                c["slam_um"], c["seeing"], c["pupil"], c["dt"],
-                                                                c["bin"], c["seed"], c["zangle"], c["src"][0],
-                                                                c["src"][1]]))
+               profile=np.array(c["profile"]), logprof=logprof, conf=np.array(conf), prof=np.array(prof),
+               params=np.array([M, c["W"], c["Wout"], c["nframes"], c["lam_ref_um"], c["slam_um"], c["seeing"],
+                                c["pupil"], c["dt"], c["bin"], c["seed"], c["zangle"], c["src"][0], c["src"][1],
+                                prec, ntspan, amp]))
     return out
+
+
+# configuration-file reads: text with repeated keywords, a bare keyword
+# line, tabs, blank lines, comments and keyword prefixes
+CONF_TEXT = """# comment line
+PUPIL_SCALE 0.02
+WFsize\t\t64   # trailing comment
+
+TURBULENCE_SEEING 0.8
+TURBULENCE_SEEING
+  MASTER_SIZE 1024
+WFsizeX 9
+PUPIL_SCALE 0.01 extra tokens
+SLAMBDA 1.6
+SLAMBDA
+EMPTYVALUE
+"""
+CONF_KEYS = ["PUPIL_SCALE", "WFsize", "TURBULENCE_SEEING", "MASTER_SIZE", "WFsizeX", "SLAMBDA", "EMPTYVALUE",
+             "MISSING", "#", "comment"]
+
+
+def make_conf() -> dict:
+    with tempfile.TemporaryDirectory() as td:
+        (Path(td) / "t.conf").write_text(CONF_TEXT)
+        txt = run([str(ATMREF), "conf", "t.conf"] + CONF_KEYS, td)
+    rows = []
+    for line in txt.splitlines():
+        if line.startswith("CONF\t"):
+            f = line.split("\t")
+            rows.append([f[1], int(f[2]), int(f[3]), f[4] if len(f) > 4 else ""])
+    return {"text": CONF_TEXT, "reads": rows}
 
 
 def main():
@@ -156,10 +221,11 @@ def main():
         sys.path.insert(0, str(ROOT / "oracle" / "ref"))
         import build_ref
         build_ref.build()
+    (HERE / "conf.json").write_text(json.dumps(make_conf(), indent=1) + "\n")
     np.savez_compressed(HERE / "fresnel.npz", **make_fresnel())
     for name, case in MKWFS_CASES.items():
         np.savez_compressed(HERE / f"{name}.npz", **make_mkwfs(case))
-    print("wrote", ", ".join(["fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
+    print("wrote", ", ".join(["conf.json", "fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
 
 
 if __name__ == "__main__":

@@ -70,12 +70,12 @@ def instances(case: Case):
     return out
 
 
-def run_gpu(case: Case, screens, nsteps: int):
+def run_gpu(case: Case, screens, nsteps: int, ring: int = 1):
     from atmosphericturbulencesimul_gb300 import Series
     inst = instances(case)
     s = Series(case.alt, case.cn2, case.speed, case.direction, master_size=case.M, instances=inst,
                pupil_scale=case.pupil, time_step=case.dt, fresnel_bin=case.fresnel_bin, zangle=case.zangle,
-               amplitude=case.amplitude, fresnel=case.fresnel)
+               amplitude=case.amplitude, fresnel=case.fresnel, ring=ring)
     for l, sc in enumerate(screens):
         s.load_screen(l, sc)
     frames = s.run_frames(nsteps)

@@ -105,6 +105,18 @@ def test_series_large_grid(lib, oracle64):
     _compare(case, oracle64, 2)
 
 
+def test_output_ring_holds_every_instance(lib, oracle64):
+    """A device output ring of several slots with several instances of
+    different crops returns the same frames as a single slot."""
+    case = Case(alt=[0.0, 3000.0], cn2=[0.6, 0.4], speed=[10.0, 20.0], direction=[0.3, 2.0], M=256, W=128,
+                Wout=100, sci=[(1.25e-6, 0.0, 0.0), (2.2e-6, 4.85e-5, 0.0)])
+    screens = make_screens(case, oracle64)
+    _, f1, _, _ = run_gpu(case, screens, 5, ring=1)
+    _, f3, _, _ = run_gpu(case, screens, 5, ring=3)
+    for a, b in zip(f1, f3):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
 def test_master_screen_matches_oracle(lib, oracle64):
     from atmosphericturbulencesimul_gb300 import master_screen
     M = 256
