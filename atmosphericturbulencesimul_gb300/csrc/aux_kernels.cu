@@ -214,25 +214,30 @@ __global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __rest
 {
     const InstDev& I = insts[list[blockIdx.y]];
     const int Nout = I.Nout, nb = I.nb;
-    const long n = (long)Nout * Nout;
     const int step = d_step ? *d_step : 0;
     float* pha = I.out_pha + (size_t)(step % I.ring) * I.ostride;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        const int jj = (int)(i / Nout), ii = (int)(i % Nout);
-        const float peak = nb > 0 ? I.peak[I.binx[jj] * nb + I.binx[ii]] : 0.0f;
-        const float p = pha[i];
-        float d1, e1, d2, e2;
-        two_sum(I.phisum[i], -p, d1, e1);
-        two_sum(d1, -peak, d2, e2);
-        pha[i] = add_2pi_multiple(p, round_2pi(d2, e1 + e2));
+    const short* __restrict__ binx = I.binx;
+    const float* __restrict__ peakv = I.peak;
+    const float* __restrict__ psum = I.phisum;
+    // one row per block iteration, one column per thread
+    for (int jj = blockIdx.x; jj < Nout; jj += gridDim.x) {
+        const int bj = nb > 0 ? binx[jj] * nb : 0;
+        const size_t ro = (size_t)jj * Nout;
+        for (int ii = threadIdx.x; ii < Nout; ii += blockDim.x) {
+            const float peak = nb > 0 ? peakv[bj + binx[ii]] : 0.0f;
+            const float p = pha[ro + ii];
+            float d1, e1, d2, e2;
+            two_sum(psum[ro + ii], -p, d1, e1);
+            two_sum(d1, -peak, d2, e2);
+            pha[ro + ii] = add_2pi_multiple(p, round_2pi(d2, e1 + e2));
+        }
     }
 }
 
 cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxnout, const int* d_step, cudaStream_t st)
 {
     if (nsci <= 0) return cudaSuccess;
-    const long n = (long)maxnout * maxnout;
-    const int bx = (int)((n + 255) / 256 < 64 ? (n + 255) / 256 : 64);
+    const int bx = maxnout < 256 ? maxnout : 256;
     k_sci_apply<<<dim3(bx, nsci), 256, 0, st>>>(insts, list, d_step);
     return cudaGetLastError();
 }

@@ -169,6 +169,22 @@ __device__ __forceinline__ void prop_row(float2* v, float2* xrow, int t, const f
 // forward, +1 inverse; rev walks the radix sequence backwards (the inverse of
 // a propagation, which starts from the forward's register layout and ends in
 // the natural layout x[t + e T]).
+// Barrier of the threads that share one row's exchange buffer.  Thread
+// tid works on row tid / T, so rows of T <= 32 threads lie inside one warp
+// (a warp barrier suffices); rows of 64 threads use named barrier 1 + row.
+// Callers keep a CTA barrier wherever another row's data aliases the buffer.
+template <int T>
+__device__ __forceinline__ void row_sync()
+{
+    static_assert(T <= 32 ? (32 % T == 0) : (T % 32 == 0 && T <= 64 * 4), "rows must tile warps");
+    if constexpr (T <= 32) {
+        __syncwarp();
+    } else {
+        const int id = 1 + (int)threadIdx.x / T;
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(T) : "memory");
+    }
+}
+
 template <int N, int T, int E>
 __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev)
 {
@@ -177,9 +193,9 @@ __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const flo
     for (int st = 0; st < Stages<N>::S; st++) {
         const int r = stage_radix<N>(st, rev);
         if (st > 0) {
-            __syncthreads();
+            row_sync<T>();
             stage_exchange_store<N, T, E>(v, xrow, t, rp, nsp);
-            __syncthreads();
+            row_sync<T>();
             stage_exchange_load<N, T, E>(v, xrow, t, r);
         }
         stage_compute<N, T, E>(v, t, tw + tw_offset<N>(rev, st), r, ns, ds);
@@ -318,6 +334,9 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                     }
 #pragma unroll
                     for (int e = 0; e < E; e++) v[e] = cmul(v[e], phasor(phi[rr * N + t + e * T]));
+                    // phi spans the exchange rows of other threads: all reads
+                    // end before the next transform's row-local exchanges
+                    __syncthreads();
                 }
                 continue;
             }
