@@ -198,7 +198,7 @@ def cpu_port_sample(wl: dict, screens, threads: int, frames_per_class: int = 1, 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched")
@@ -237,6 +237,7 @@ def main():
         return
 
     import torch
+    from atmosphericturbulencesimul_gb300.replicas import aggregate
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -265,12 +266,8 @@ def main():
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
     barrier()
-    t = e0.elapsed_time(e1) / 1e3
-    tt = torch.tensor([t], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    t = float(tt.item())
-    value = args.steps * ninst * world / t
+    # max over ranks of the device time, frames of all ranks
+    t, _, value = aggregate(e0.elapsed_time(e1) / 1e3, args.steps * ninst, device="cuda")
 
     # end to end through the C ABI with host buffers
     ff = s.frame_floats
@@ -281,11 +278,7 @@ def main():
     w0 = time.perf_counter()
     s.run(args.steps, pha_ptr=pha_h.data_ptr(), amp_ptr=amp_h.data_ptr(), nslots=nslots)
     torch.cuda.synchronize()
-    we = time.perf_counter() - w0
-    te = torch.tensor([we], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e = args.steps * ninst * world / float(te.item())
+    _, _, e2e = aggregate(time.perf_counter() - w0, args.steps * ninst, device="cuda")
 
     # roofline of the dominant pass (timed live on the engine stream)
     npl = len(s.planes()[0])
