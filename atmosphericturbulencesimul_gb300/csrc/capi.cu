@@ -236,7 +236,7 @@ struct Class {
     std::vector<int> members;  // global instance indices
     int base = 0;              // first slot in the class-ordered InstDev array
     TmaSet maps[kNumTileCfg];  // per configuration: the box height is RR + 3
-    double tuned_ms[kNumTileCfg] = {0, 0};
+    double tuned_ms[kNumTileCfg] = {};
 };
 
 }  // namespace atmwfs

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "atmwfs.h"
 #include "fft_core.cuh"
 
 namespace atmwfs {
@@ -104,24 +105,29 @@ typedef cudaError_t (*PassLauncher)(int var, dim3 grid, const PassArgs& a, const
 typedef cudaError_t (*PassLauncherCfg)(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps,
                                        const float2* tw, cudaStream_t st);
 
-// Tile configurations compiled for every grid size: rows per CTA and the
-// minimum number of resident CTAs per SM the kernel is register-limited to.
-// Configuration 0 is the one-CTA-per-SM shape; configuration 1 trades
-// halo overhead (fewer rows per tile) for several resident CTAs per SM.
-// The engine's autotuner picks one per grid class at set-up.
+// Tile configurations compiled for every grid size: rows per CTA, the
+// minimum number of resident CTAs per SM the kernel is register-limited to,
+// and whether the screen tile overlays the exchange rows.  Configuration 0
+// is the one-CTA-per-SM shape; configuration 1 trades halo overhead (fewer
+// rows per tile) for several resident CTAs per SM; configuration 2 also
+// overlays the tile on the exchange buffer (the tile is then loaded after
+// the first propagation instead of during it), which cuts shared memory so
+// that one more CTA fits per SM.  The engine's autotuner picks one per grid
+// class at set-up.
 struct TileCfg {
     int rr, minb;
+    bool alias;
 };
-constexpr int kNumTileCfg = 2;
+constexpr int kNumTileCfg = ATMWFS_NUM_TILE_CFG;
 constexpr TileCfg tile_cfg(int N, int c)
 {
-    return N == 64    ? (c == 0 ? TileCfg{32, 1} : TileCfg{16, 2})
-         : N == 128   ? (c == 0 ? TileCfg{32, 1} : TileCfg{16, 2})
-         : N == 256   ? (c == 0 ? TileCfg{16, 1} : TileCfg{8, 3})
-         : N == 512   ? (c == 0 ? TileCfg{16, 1} : TileCfg{8, 3})
-         : N == 1024  ? (c == 0 ? TileCfg{8, 1} : TileCfg{4, 3})
-         : N == 2048  ? (c == 0 ? TileCfg{4, 1} : TileCfg{2, 3})
-                      : TileCfg{0, 0};
+    return N == 64    ? (c == 0 ? TileCfg{32, 1, false} : c == 1 ? TileCfg{16, 2, false} : TileCfg{16, 3, true})
+         : N == 128   ? (c == 0 ? TileCfg{32, 1, false} : c == 1 ? TileCfg{16, 2, false} : TileCfg{16, 3, true})
+         : N == 256   ? (c == 0 ? TileCfg{16, 1, false} : c == 1 ? TileCfg{8, 3, false} : TileCfg{8, 4, true})
+         : N == 512   ? (c == 0 ? TileCfg{16, 1, false} : c == 1 ? TileCfg{8, 3, false} : TileCfg{8, 4, true})
+         : N == 1024  ? (c == 0 ? TileCfg{8, 1, false} : c == 1 ? TileCfg{4, 3, false} : TileCfg{4, 4, true})
+         : N == 2048  ? (c == 0 ? TileCfg{4, 1, false} : c == 1 ? TileCfg{2, 3, false} : TileCfg{2, 3, true})
+                      : TileCfg{0, 0, false};
 }
 
 // Rows per CTA of configuration 0 (unit operators).

@@ -100,13 +100,25 @@ struct PassGeom {
     static constexpr size_t XBYTES = size_t(RR) * RS * 8;
     static constexpr size_t PHI_EPI_BYTES = size_t(RR) * RS * 8;
     static constexpr size_t TILE_BYTES = size_t(NBOX) * TROWS * kBoxW * 4;
+    static constexpr size_t PHI_BYTES = size_t(RR) * N * 4;          // phase of the plane's layers, [RR][N]
+    static constexpr int NJ = RR > 16 ? 3 : 2;                        // bin rows a tile can touch
+    static constexpr size_t COLSUM_BYTES = size_t(NJ) * N * 8;        // epilogue column sums, [NJ][N]
     AW_HD static constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
+    AW_HD static constexpr size_t mx(size_t a, size_t b) { return a > b ? a : b; }
     AW_HD static constexpr size_t region(bool epi) { return round128((epi && PHI_EPI_BYTES > XBYTES) ? PHI_EPI_BYTES : XBYTES); }
-    AW_HD static constexpr size_t smem(int ops)
+    // Separate layout: [exchange rows | tile]; the epilogue's column sums
+    // reuse the tile.  Overlaid layout (ALIAS): the tile sits after the phi
+    // rows inside the exchange region and the column sums after the staged
+    // exchange rows, so the region is max(phi + tile, rows + column sums).
+    AW_HD static constexpr size_t tile_offset(bool epi, bool alias) { return alias ? round128(PHI_BYTES) : region(epi); }
+    AW_HD static constexpr size_t smem(int ops, bool alias = false)
     {
-        return region((ops & OP_EPI) != 0) + (((ops & (OP_GATHER | OP_EPI)) != 0) ? TILE_BYTES + 128 : 0);
+        const bool gather = (ops & (OP_GATHER | OP_EPI)) != 0, epi = (ops & OP_EPI) != 0;
+        if (!alias || !gather) return region(epi) + (gather ? TILE_BYTES + 128 : 0);
+        return mx(round128(PHI_BYTES) + TILE_BYTES, epi ? round128(XBYTES) + COLSUM_BYTES : XBYTES) + 128;
     }
     static_assert(N % (RR) == 0, "rows per CTA must divide N");
+    static_assert(COLSUM_BYTES <= TILE_BYTES, "column sums must fit in the tile buffer");
 };
 
 template <int N, int RR>
@@ -266,7 +278,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // ---------------------------------------------------------------------------
 // the pass kernel
 // ---------------------------------------------------------------------------
-template <int N, int RR, int MINB, int OPS>
+template <int N, int RR, int MINB, int OPS, bool ALIAS>
 __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     k_pass(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps, const float2* __restrict__ tw)
 {
@@ -277,7 +289,8 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     extern __shared__ __align__(1024) unsigned char sm[];
     float2* xb = reinterpret_cast<float2*>(sm);
     // TMA destination: 128-byte aligned whatever the dynamic smem base
-    float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm + G::region(kEpi)) + 127) & ~uintptr_t(127));
+    float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm + G::tile_offset(kEpi, ALIAS)) + 127) &
+                                           ~uintptr_t(127));
     __shared__ __align__(8) uint64_t bar;
 
     const int tid = threadIdx.x;
@@ -296,7 +309,9 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     if constexpr (kGather) {
         if (tid == 0) mbar_init(&bar, 1);
         __syncthreads();
-        if (tid == 0 && ltop >= lbot) tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar);
+        // separate tile: its first copy overlaps the first propagation
+        if constexpr (!ALIAS)
+            if (tid == 0 && ltop >= lbot) tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar);
     }
 
     float2 v[E];
@@ -320,6 +335,13 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                 if constexpr (kGather) {
                     float* phi = reinterpret_cast<float*>(xb);  // [RR][N]
                     __syncthreads();
+                    if constexpr (ALIAS) {
+                        // overlaid tile: the exchange rows are free now
+                        if (tid == 0 && ltop >= lbot) {
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                            tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar);
+                        }
+                    }
                     for (int l = ltop; l >= lbot; l--) {
                         if (!cta_wait_tile(&bar, parity, a.d_status)) return;
                         parity ^= 1;
@@ -379,9 +401,9 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         const short* __restrict__ binx = I->binx;
         const int jb0 = bins ? binx[ya - off] : 0;
         // bins are at least 20 rows tall: RR rows touch at most NJ bin rows
-        constexpr int NJ = RR > 16 ? 3 : 2;
-        float2* colsum = reinterpret_cast<float2*>(tile);  // [NJ][N]: per bin row, per column
-        static_assert(size_t(NJ) * N * 8 <= G::TILE_BYTES, "column sums must fit in the tile buffer");
+        constexpr int NJ = G::NJ;
+        // [NJ][N]: per bin row, per column; clear of the staged rows in xb
+        float2* colsum = ALIAS ? reinterpret_cast<float2*>(sm + G::round128(G::XBYTES)) : reinterpret_cast<float2*>(tile);
 #pragma unroll
         for (int c = 0; c < CPT; c++) {
             const int x = off + tid + c * NT;
@@ -556,7 +578,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 2)
 }
 
 // host launcher for one (N, tile configuration)
-template <int N, int RR, int MINB>
+template <int N, int RR, int MINB, bool ALIAS>
 cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
 {
     using G = PassGeom<N, RR>;
@@ -565,14 +587,14 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
     dim3 block(G::NT);
 #define AW_CASE(VAR)                                                                                   \
     case VAR: {                                                                                        \
-        constexpr size_t sm = G::smem(VAR);                                                            \
+        constexpr size_t sm = G::smem(VAR, ALIAS);                                                     \
         static bool attr = false;                                                                      \
         if (!attr) {                                                                                   \
-            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
             if (e != cudaSuccess) return e;                                                            \
             attr = true;                                                                               \
         }                                                                                              \
-        k_pass<N, RR, MINB, VAR><<<grid, block, sm, st>>>(a, m, tw);                                   \
+        k_pass<N, RR, MINB, VAR, ALIAS><<<grid, block, sm, st>>>(a, m, tw);                            \
         return cudaGetLastError();                                                                     \
     }
     switch (var) {
@@ -603,16 +625,18 @@ template <int N>
 cudaError_t launch_pass_n(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
 {
     constexpr TileCfg c0 = tile_cfg(N, 0);
-    return launch_pass_t<N, c0.rr, c0.minb>(var, grid, a, maps, tw, st);
+    return launch_pass_t<N, c0.rr, c0.minb, c0.alias>(var, grid, a, maps, tw, st);
 }
 
 template <int N>
 cudaError_t launch_pass_nc(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
                            cudaStream_t st)
 {
-    constexpr TileCfg c0 = tile_cfg(N, 0), c1 = tile_cfg(N, 1);
-    if (cfg == 1) return launch_pass_t<N, c1.rr, c1.minb>(var, grid, a, maps, tw, st);
-    return launch_pass_t<N, c0.rr, c0.minb>(var, grid, a, maps, tw, st);
+    constexpr TileCfg c0 = tile_cfg(N, 0), c1 = tile_cfg(N, 1), c2 = tile_cfg(N, 2);
+    static_assert(kNumTileCfg == 3, "one branch per tile configuration");
+    if (cfg == 2) return launch_pass_t<N, c2.rr, c2.minb, c2.alias>(var, grid, a, maps, tw, st);
+    if (cfg == 1) return launch_pass_t<N, c1.rr, c1.minb, c1.alias>(var, grid, a, maps, tw, st);
+    return launch_pass_t<N, c0.rr, c0.minb, c0.alias>(var, grid, a, maps, tw, st);
 }
 
 }  // namespace atmwfs

@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import MODE_PHASE, MODE_REF, MODE_SCI, check
+from ._lib import MODE_PHASE, MODE_REF, MODE_SCI, NUM_TILE_CFG, check
 
 __all__ = ["Series", "InstanceSpec", "layer_planes", "fresnel", "fft2d", "master_screen", "MODE_REF", "MODE_SCI", "MODE_PHASE"]
 
@@ -172,10 +172,10 @@ class Series:
 
     def class_info(self, c: int) -> dict:
         n, no, cnt, rr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        t = (C.c_double * 2)()
+        t = (C.c_double * NUM_TILE_CFG)()
         check(self._lib.atmwfs_class_info(self._ctx, c, C.byref(n), C.byref(no), C.byref(cnt), C.byref(rr), t))
         return {"n": n.value, "nout": no.value, "count": cnt.value, "rows_per_cta": rr.value,
-                "tuned_ms": [t[0], t[1]]}
+                "tuned_ms": list(t)}
 
     def time_pass(self, k: int, c: int, reps: int = 10):
         """Mean duration [ms] and algorithmic bytes of pass k of grid class c."""

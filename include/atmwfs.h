@@ -151,9 +151,13 @@ atmwfs_status atmwfs_time_pass(atmwfs_ctx* ctx, int k, int c, int reps, double* 
                                int* count);
 int atmwfs_num_classes(const atmwfs_ctx* ctx);
 
+/* Tile configurations the engine compiles for every grid size. */
+#define ATMWFS_NUM_TILE_CFG 3
+
 /* Grid class ci (instances sharing wf_raw_size and wf_size): sizes, member
  * count, the rows per CTA the autotuner chose, and the mean time [ms] of the
- * tuned pass in each of the 2 tile configurations (0 if forced). */
+ * tuned pass in each of the ATMWFS_NUM_TILE_CFG tile configurations (0 if
+ * forced). */
 atmwfs_status atmwfs_class_info(const atmwfs_ctx* ctx, int ci, int* n, int* nout, int* count, int* rows_per_cta,
                                 double* tuned_ms);
 

@@ -16,7 +16,7 @@ def emul_output(tmp_path_factory):
     cuda_inc = "/usr/local/cuda/include"
     if not Path(cuda_inc).exists() or shutil.which("g++") is None:
         pytest.skip("g++ or CUDA headers unavailable")
-    subprocess.run(["g++", "-std=c++17", "-O2", f"-I{cuda_inc}", f"-I{ROOT / 'atmosphericturbulencesimul_gb300' / 'csrc'}",
+    subprocess.run(["g++", "-std=c++17", "-O2", f"-I{cuda_inc}", f"-I{ROOT / 'atmosphericturbulencesimul_gb300' / 'csrc'}", f"-I{ROOT / 'include'}",
                     str(ROOT / "tests" / "emul" / "pass_emul.cpp"), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     return dict((l.split()[0], float(l.split()[1])) for l in out.strip().splitlines())

@@ -79,6 +79,17 @@ def test_series_crop_and_grouped_layers(lib, oracle64):
     _compare(case, oracle64, 3)
 
 
+@pytest.mark.parametrize("cfg", [0, 1, 2])
+def test_series_every_tile_configuration(lib, oracle64, monkeypatch, cfg):
+    """Each compiled tile configuration (separate or overlaid screen tile,
+    1..32 rows per CTA) on grouped layers, a crop and two grid sizes."""
+    monkeypatch.setenv("ATMWFS_TILE_CFG", str(cfg))
+    case = Case(alt=[0.0, 50.0, 5000.0, 12000.0], cn2=[0.4, 0.2, 0.3, 0.1], speed=[8.0, 12.0, 25.0, 30.0],
+                direction=[0.1, 1.0, 3.0, 5.5], M=512, W=256, Wout=200, fresnel_bin=100.0,
+                sci=[(1.25e-6, 0.0, 0.0), (2.2e-6, 4.85e-5, -4.85e-5)])
+    _compare(case, oracle64, 2)
+
+
 def test_series_single_layer_no_hop(lib, oracle64):
     case = Case(alt=[5000.0], cn2=[1.0], speed=[10.0], direction=[0.5236], M=256, W=256, Wout=256)
     _compare(case, oracle64, 3)
