@@ -1,5 +1,5 @@
-"""ctypes binding of libatmwfs.so (the C ABI declared in include/atmwfs.h and
-include/atmwfs_mkwfs.h).
+"""ctypes binding of libatmwfs.so (the C ABI declared in include/atmwfs.h,
+include/atmwfs_mkwfs.h and include/atmwfs_fno.h).
 
 The library is the only compute path: if it is missing or cannot be loaded
 this module raises; there is no CPU fallback.
@@ -102,6 +102,10 @@ class Conf(C.Structure):
     ]
 
 
+class FnoCfg(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("nin", "width", "modes", "layers", "proj", "nout", "grid")]
+
+
 REFRACTIVITY_FN = C.CFUNCTYPE(C.c_float, C.c_float, C.c_float, C.c_void_p)
 
 
@@ -165,6 +169,28 @@ SIGNATURES = [
     ("atmwfs_shm_close", None, [C.c_void_p]),
     ("atmwfs_shm_semwait", C.c_int, [C.c_char_p, C.c_long, C.c_double]),
     ("atmwfs_mkwfs", C.c_int, [C.c_char_p, C.c_float, C.c_long, C.POINTER(MkwfsOpts)]),
+    ("atmwfs_windows_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_void_p]),
+    # include/atmwfs_fno.h
+    ("atmwfs_fno_create", C.c_int, [C.POINTER(FnoCfg), C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("atmwfs_fno_destroy", None, [C.c_void_p]),
+    ("atmwfs_fno_get_cfg", C.c_int, [C.c_void_p, C.POINTER(FnoCfg)]),
+    ("atmwfs_fno_num_params", C.c_long, [C.c_void_p]),
+    ("atmwfs_fno_get_params", C.c_int, [C.c_void_p, _fp]),
+    ("atmwfs_fno_set_params", C.c_int, [C.c_void_p, _fp]),
+    ("atmwfs_fno_get_grads", C.c_int, [C.c_void_p, _fp]),
+    ("atmwfs_fno_zero_grads", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("atmwfs_fno_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("atmwfs_fno_loss_grad", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, _dp, C.c_void_p]),
+    ("atmwfs_fno_adam", C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]),
+    ("atmwfs_fno_prepare", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
+    ("atmwfs_fno_target", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+    ("atmwfs_fno_assemble", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("atmwfs_fno_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("atmwfs_fno_load", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    ("atmwfs_gemm_bf16", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_int, C.c_void_p,
+                                   C.c_long, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_float, C.c_float, C.c_void_p,
+                                   C.c_int, C.c_long, C.c_long, C.c_long, C.c_void_p]),
 ]
 
 _lib = None

@@ -1,4 +1,6 @@
 // aux_kernels.cu -- setup and per-step helper kernels of the engine.
+#include <algorithm>
+
 #include "aux_kernels.cuh"
 #include "pass_impl.cuh"
 
@@ -343,6 +345,61 @@ __global__ void k_split_scale(const float2* __restrict__ F, long n, double s1, d
 cudaError_t split_scale(const float2* F, long n, double s1, double s2, float* o1, float* o2, cudaStream_t st)
 {
     k_split_scale<<<4 * 152, 256, 0, st>>>(F, n, s1, s2, o1, o2);
+    return cudaGetLastError();
+}
+
+}  // namespace atmwfs
+
+namespace atmwfs {
+
+// ---------------------------------------------------------------------------
+// per-layer phase windows of one instance at the last completed step: the
+// same Keys bicubic samples the passes form (horizontal taps first, then
+// the vertical ones), times the instance's Scoeff, in screen orientation
+// ---------------------------------------------------------------------------
+struct LayerScales {
+    float s[kMaxLayers];
+    const float* scr[kMaxLayers];
+};
+
+__global__ void k_windows(LayerScales ls, int M, const LayerPos* __restrict__ pos, int poscap, int ninst, int gidx,
+                          int L, const int* __restrict__ d_step, int W, float* __restrict__ out)
+{
+    const int l = blockIdx.y;
+    const int step = *d_step - 1;
+    const LayerPos p = pos[((size_t)(step % poscap) * ninst + gidx) * L + l];
+    float wx[4], wy[4];
+    keys_weights(p.fx, wx);
+    keys_weights(p.fy, wy);
+    const float* S = ls.scr[l];
+    const long n = (long)W * W;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(i / W), x = (int)(i % W);
+        float h[4];
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int sy = ((p.iy + y - 1 + b) % M + M) % M;
+            const float* r = S + (size_t)sy * M;
+            const int c0 = p.ix + x - 1;
+            h[b] = wx[0] * r[((c0) % M + M) % M] + wx[1] * r[((c0 + 1) % M + M) % M] +
+                   wx[2] * r[((c0 + 2) % M + M) % M] + wx[3] * r[((c0 + 3) % M + M) % M];
+        }
+        out[(size_t)l * n + i] = (wy[0] * h[0] + wy[1] * h[1] + wy[2] * h[2] + wy[3] * h[3]) * ls.s[l];
+    }
+}
+
+cudaError_t windows(const float* const* screens, const float* scoeff, int L, int M, const LayerPos* pos, int poscap,
+                    int ninst, int gidx, const int* d_step, int W, float* out, cudaStream_t st)
+{
+    if (L > kMaxLayers) return cudaErrorInvalidValue;
+    LayerScales ls;
+    for (int l = 0; l < L; l++) {
+        ls.s[l] = scoeff ? scoeff[l] : 1.0f;
+        ls.scr[l] = screens[l];
+    }
+    const long n = (long)W * W;
+    const unsigned bx = (unsigned)std::min<long>((n + 255) / 256, 1024);
+    k_windows<<<dim3(bx, L), 256, 0, st>>>(ls, M, pos, poscap, ninst, gidx, L, d_step, W, out);
     return cudaGetLastError();
 }
 

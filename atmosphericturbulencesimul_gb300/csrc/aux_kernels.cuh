@@ -35,4 +35,9 @@ cudaError_t launch_pass_cfg_1024(int cfg, int var, dim3 grid, const PassArgs& a,
 cudaError_t launch_pass_cfg_2048(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
                                 cudaStream_t st);
 
+// Per-layer phase windows (W x W, screen orientation) of global instance
+// gidx at the last completed step, scaled by the instance's Scoeff.
+cudaError_t windows(const float* const* screens, const float* scoeff, int L, int M, const LayerPos* pos, int poscap,
+                    int ninst, int gidx, const int* d_step, int W, float* out, cudaStream_t st);
+
 }  // namespace atmwfs

@@ -957,16 +957,27 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
                 const size_t ff = c->frame_floats;
                 if (sink->pha)
                     AW_CUDA(cudaMemcpyAsync(sink->pha + (size_t)hs * ff, c->d_out_pha + slot * ff, sizeof(float) * ff,
-                                            cudaMemcpyDeviceToHost, c->st));
+                                            cudaMemcpyDefault, c->st));
                 if (sink->amp)
                     AW_CUDA(cudaMemcpyAsync(sink->amp + (size_t)hs * ff, c->d_out_amp + slot * ff, sizeof(float) * ff,
-                                            cudaMemcpyDeviceToHost, c->st));
+                                            cudaMemcpyDefault, c->st));
             }
         }
         s += chunk;
         b ^= 1;
     }
     return check_status(c);
+}
+
+atmwfs_status atmwfs_windows_dev(atmwfs_ctx* c, int i, float* out, void* stream)
+{
+    if (!c || !out || i < 0 || i >= c->ninst) return fail(ATMWFS_ERR_INVALID, "bad instance or buffer");
+    if (c->steps == 0) return fail(ATMWFS_ERR_STATE, "no step computed yet");
+    std::vector<float> sc(c->L);
+    for (int l = 0; l < c->L; l++) sc[l] = c->scoeff[i][l];
+    AW_CUDA(windows(c->d_screen.data(), sc.data(), c->L, (int)c->M, c->d_pos, c->poscap, c->ninst, i, c->d_step,
+                    (int)c->inst[i].wf_raw_size, out, stream ? (cudaStream_t)stream : c->st));
+    return ATMWFS_OK;
 }
 
 atmwfs_status atmwfs_frame_dev(atmwfs_ctx* c, int i, const float** pha, const float** amp)

@@ -1,0 +1,81 @@
+// fno_gemm.cu -- tile choice, beta handling and the C-ABI test entry of the
+// surrogate's BF16 GEMM.
+#include <algorithm>
+
+#include "atmwfs.h"
+#include "atmwfs_fno.h"
+#include "fno_gemm.cuh"
+
+namespace atmwfs {
+
+void set_error_message(const char* msg);
+
+namespace {
+
+__global__ void k_scale_rows(float* C, long ldc, long sC, int M, int N, float beta)
+{
+    float* c = C + (size_t)blockIdx.z * sC;
+    for (int m = blockIdx.y; m < M; m += gridDim.y)
+        for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < N; n += gridDim.x * blockDim.x) {
+            float* p = c + (size_t)m * ldc + n;
+            *p = beta == 0.0f ? 0.0f : *p * beta;
+        }
+}
+
+}  // namespace
+
+cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
+{
+    GemmArgs g = g0;
+    if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
+    if (beta != 1.0f) {
+        const int nb = g.sC == 0 ? 1 : g.batch;  // a batch summed into one C scales it once
+        const dim3 grid((unsigned)std::min((g.N + 255) / 256, 64), (unsigned)std::min(g.M, 1024), (unsigned)nb);
+        k_scale_rows<<<grid, 256, 0, st>>>(g.C, g.ldc, g.sC, g.M, g.N, beta);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (g.K <= 0) return cudaSuccess;
+    const bool bm128 = g.M > 64, bn128 = g.N > 64;
+    const int BM = bm128 ? 128 : 64, BN = bn128 ? 128 : 64;
+    const long tiles = (long)((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN) * g.batch;
+    // split K until the grid covers the GPU a few times over (long, thin products)
+    const int kchunks = (g.K + gemm::BK - 1) / gemm::BK;
+    int split = 1;
+    while (split < 64 && tiles * split < 4 * 152 && kchunks / (split * 2) >= 4) split *= 2;
+    if (g.splitk < 1) g.splitk = split;
+    if ((long)g.batch * g.splitk > 65535) g.splitk = std::max(1, 65535 / g.batch);
+    const dim3 grid((unsigned)((g.M + BM - 1) / BM), (unsigned)((g.N + BN - 1) / BN), (unsigned)(g.batch * g.splitk));
+    if (bm128 && bn128) gemm::k_gemm<128, 128><<<grid, 256, 0, st>>>(g);
+    else if (!bm128 && bn128) gemm::k_gemm<64, 128><<<grid, 256, 0, st>>>(g);
+    else if (bm128 && !bn128) gemm::k_gemm<128, 64><<<grid, 256, 0, st>>>(g);
+    else gemm::k_gemm<64, 64><<<grid, 256, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+}  // namespace atmwfs
+
+extern "C" atmwfs_status atmwfs_gemm_bf16(int M, int N, int K, const void* A, long lda, int ta, int a_bf16,
+                                          const void* B, long ldb, int tb, int b_bf16, float* C, long ldc,
+                                          float alpha, float beta, const float* bias, int batch, long sA, long sB,
+                                          long sC, void* stream)
+{
+    using namespace atmwfs;
+    if (!A || !B || !C || M < 0 || N < 0 || K < 0 || batch < 1) {
+        set_error_message("atmwfs_gemm_bf16: bad arguments");
+        return ATMWFS_ERR_INVALID;
+    }
+    GemmArgs g{};
+    g.M = M; g.N = N; g.K = K;
+    g.A = A; g.B = B; g.C = C;
+    g.lda = lda; g.ldb = ldb; g.ldc = ldc;
+    g.sA = sA; g.sB = sB; g.sC = sC;
+    g.ta = ta; g.tb = tb; g.a_bf16 = a_bf16; g.b_bf16 = b_bf16;
+    g.alpha = alpha; g.bias = bias; g.bias_rows = 0; g.splitk = 0; g.batch = batch;
+    const cudaError_t e = gemm_launch(g, beta, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return ATMWFS_ERR_CUDA;
+    }
+    return ATMWFS_OK;
+}

@@ -113,8 +113,8 @@ class Series:
     def run(self, nsteps: int, pha: np.ndarray | None = None, amp: np.ndarray | None = None,
             pha_ptr: int | None = None, amp_ptr: int | None = None, nslots: int = 0) -> None:
         """Advance nsteps steps.  Frames go to host arrays (shape [nsteps, frame_floats])
-        or raw host pointers (nslots frames, reused round-robin); with neither
-        they stay on the device."""
+        or raw host or device pointers (nslots frames, reused round-robin);
+        with neither they stay on the device."""
         sink = None
         if pha is not None or amp is not None or pha_ptr or amp_ptr:
             sink = _lib.Sink()
@@ -138,6 +138,14 @@ class Series:
             o = self.frame_offsets[i]
             out.append((pha[:, o:o + n * n].reshape(nsteps, n, n), amp[:, o:o + n * n].reshape(nsteps, n, n)))
         return out
+
+    def frame_offset(self, i: int) -> int:
+        return int(self._lib.atmwfs_frame_offset(self._ctx, i))
+
+    def windows_dev(self, i: int, ptr: int, stream: int = 0) -> None:
+        """Per-layer phase windows of instance i at the last step into device memory
+        (nlayers x W x W floats), on `stream` (0: the engine's)."""
+        check(self._lib.atmwfs_windows_dev(self._ctx, i, C.c_void_p(ptr), C.c_void_p(stream) if stream else None))
 
     def frame_dev(self, i: int) -> tuple[int, int]:
         p, a = C.c_void_p(), C.c_void_p()

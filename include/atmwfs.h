@@ -75,11 +75,12 @@ typedef struct atmwfs_params {
 
 typedef struct atmwfs_ctx atmwfs_ctx;
 
-/* Where atmwfs_run() delivers frames: host buffers of
- * nslots * atmwfs_frame_floats() floats (NULL = not copied).  Step s of the
+/* Where atmwfs_run() delivers frames: buffers of nslots *
+ * atmwfs_frame_floats() floats (NULL = not copied), in host memory (pinned
+ * buffers keep the copies asynchronous) or device memory.  Step s of the
  * call goes to slot s % nslots (nslots <= 0 means nslots = nsteps).  The
  * frames of one step are contiguous; instance i starts at
- * atmwfs_frame_offset(i).  Pinned buffers keep the copies asynchronous. */
+ * atmwfs_frame_offset(i). */
 typedef struct atmwfs_sink {
     float* pha;
     float* amp;
@@ -116,6 +117,12 @@ atmwfs_status atmwfs_run(atmwfs_ctx* ctx, long nsteps, const atmwfs_sink* sink);
 /* Device pointers of the most recent frame of instance i (valid until the
  * next run call). */
 atmwfs_status atmwfs_frame_dev(atmwfs_ctx* ctx, int i, const float** pha, const float** amp);
+
+/* Per-layer phase windows of instance i at the last completed step: the
+ * bicubic screen samples the propagation uses (:2806-2917), times the
+ * instance's Scoeff, in screen orientation: nlayers x W x W floats into the
+ * device buffer `out` (W = wf_raw_size), on `stream` (NULL: the engine's). */
+atmwfs_status atmwfs_windows_dev(atmwfs_ctx* ctx, int i, float* out, void* stream);
 
 /* Layout of one step's frames: total floats, and the offset of instance i. */
 size_t atmwfs_frame_floats(const atmwfs_ctx* ctx);
