@@ -33,6 +33,12 @@ CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-u
              "-I", str(CSRC)]
 
 
+def _cuda_include() -> list[str]:
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    inc = Path(nvcc).resolve().parent.parent / "include"
+    return ["-I", str(inc)] if inc.exists() else []
+
+
 def _nvcc() -> str:
     cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not Path(cand).exists():
@@ -81,7 +87,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         obj = BUILD / (src.stem + ".cpp.o")
         objs.append(obj)
         if _stale(obj, src, deps):
-            jobs_list.append(["g++", *CXX_FLAGS, "-c", str(src), "-o", str(obj)])
+            jobs_list.append(["g++", *CXX_FLAGS, *_cuda_include(), "-c", str(src), "-o", str(obj)])
     n = jobs or max(1, min(len(jobs_list), os.cpu_count() or 4))
     if jobs_list:
         with cf.ThreadPoolExecutor(max_workers=n) as ex:

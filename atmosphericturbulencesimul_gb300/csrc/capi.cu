@@ -969,6 +969,33 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
     return check_status(c);
 }
 
+atmwfs_status atmwfs_advance(atmwfs_ctx* c, long nsteps)
+{
+    if (!c) return fail(ATMWFS_ERR_INVALID, "null context");
+    if (nsteps < 0) return fail(ATMWFS_ERR_INVALID, "nsteps < 0");
+    AW_TRY(commit(c));
+    const size_t per = (size_t)c->ninst * c->L;
+    for (long s = 0; s < nsteps; s++) {
+        // one step at a time: the host slot is reused once its copy is done
+        AW_CUDA(cudaEventSynchronize(c->ev[0]));
+        double tnow = 0.0;
+        if (c->realtime) {
+            struct timespec ts;
+            clock_gettime(CLOCK_REALTIME, &ts);
+            tnow = (1.0 * ts.tv_sec + 1.0e-9 * ts.tv_nsec) * c->rtfactor;
+        }
+        const long g = c->steps;
+        advance_positions(c, tnow, c->h_pos[0]);
+        c->steps++;
+        AW_CUDA(cudaMemcpyAsync(c->d_pos + (g % c->poscap) * per, c->h_pos[0], sizeof(LayerPos) * per,
+                                cudaMemcpyHostToDevice, c->st));
+        AW_CUDA(cudaEventRecord(c->ev[0], c->st));
+        AW_CUDA(step_advance(c->d_step, c->st));
+    }
+    AW_CUDA(cudaStreamSynchronize(c->st));
+    return ATMWFS_OK;
+}
+
 atmwfs_status atmwfs_windows_dev(atmwfs_ctx* c, int i, float* out, void* stream)
 {
     if (!c || !out || i < 0 || i >= c->ninst) return fail(ATMWFS_ERR_INVALID, "bad instance or buffer");

@@ -180,21 +180,29 @@ __global__ void k_modemix(const __nv_bfloat16* __restrict__ R, const float* __re
     const int k = blockIdx.x, ky = k / m, kx = k % m;
     const long plane = 2L * m * m;
     const long ore = (long)ky * m + kx, oim = (long)(m + ky) * m + kx;
-    extern __shared__ float zs[];  // [B][w][2]
+    extern __shared__ float sh[];
+    float* zs = sh;                  // [B][w][2]
+    float2* rs = reinterpret_cast<float2*>(sh + 2 * B * w);  // [w][w + 1]: R[o][c], padded rows
+    const __nv_bfloat16* Rk = R + (size_t)k * w * w * 2;
+    for (int i = threadIdx.x; i < w * w; i += blockDim.x) {
+        const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(Rk)[i];  // coalesced (re, im) pairs
+        rs[(i / w) * (w + 1) + i % w] = make_float2(__low2float(v), __high2float(v));
+    }
     for (int i = threadIdx.x; i < B * w; i += blockDim.x) {
         zs[2 * i] = z[i * plane + ore];
         zs[2 * i + 1] = z[i * plane + oim];
     }
     __syncthreads();
-    const __nv_bfloat16* Rk = R + (size_t)k * w * w * 2;
     for (int i = threadIdx.x; i < B * w; i += blockDim.x) {
         const int bq = i / w, o = i % w;
+        const float2* r = rs + o * (w + 1);
+        const float* zb = zs + 2 * bq * w;
         float sr = 0.0f, si = 0.0f;
         for (int c = 0; c < w; c++) {
-            const float rr = __bfloat162float(Rk[(o * w + c) * 2]), ri = __bfloat162float(Rk[(o * w + c) * 2 + 1]);
-            const float zr = zs[2 * (bq * w + c)], zi = zs[2 * (bq * w + c) + 1];
-            sr += rr * zr - ri * zi;
-            si += rr * zi + ri * zr;
+            const float2 rc = r[c];
+            const float zr = zb[2 * c], zi = zb[2 * c + 1];
+            sr += rc.x * zr - rc.y * zi;
+            si += rc.x * zi + rc.y * zr;
         }
         y[i * plane + ore] = sr;
         y[i * plane + oim] = si;
@@ -209,9 +217,16 @@ __global__ void k_modemix_bwd(const __nv_bfloat16* __restrict__ R, const float* 
     const int k = blockIdx.x, ky = k / m, kx = k % m;
     const long plane = 2L * m * m;
     const long ore = (long)ky * m + kx, oim = (long)(m + ky) * m + kx;
-    extern __shared__ float sh[];  // zs [B][w][2], dys [B][w][2]
-    float* zs = sh;
-    float* ds = sh + 2 * B * w;
+    extern __shared__ float sh[];
+    float* zs = sh;                  // [B][w][2]
+    float* ds = sh + 2 * B * w;      // [B][w][2]
+    float2* rs = reinterpret_cast<float2*>(sh + 4 * B * w);  // [w][w + 1]
+    const __nv_bfloat16* Rk = R + (size_t)k * w * w * 2;
+    float* dRk = dR + (size_t)k * w * w * 2;
+    for (int i = threadIdx.x; i < w * w; i += blockDim.x) {
+        const __nv_bfloat162 v = reinterpret_cast<const __nv_bfloat162*>(Rk)[i];
+        rs[(i / w) * (w + 1) + i % w] = make_float2(__low2float(v), __high2float(v));
+    }
     for (int i = threadIdx.x; i < B * w; i += blockDim.x) {
         zs[2 * i] = z[i * plane + ore];
         zs[2 * i + 1] = z[i * plane + oim];
@@ -219,22 +234,21 @@ __global__ void k_modemix_bwd(const __nv_bfloat16* __restrict__ R, const float* 
         ds[2 * i + 1] = dy[i * plane + oim];
     }
     __syncthreads();
-    const __nv_bfloat16* Rk = R + (size_t)k * w * w * 2;
-    float* dRk = dR + (size_t)k * w * w * 2;
     // dz[b][c] = sum_o conj(R[o][c]) dy[b][o]
     for (int i = threadIdx.x; i < B * w; i += blockDim.x) {
         const int bq = i / w, c = i % w;
+        const float* db = ds + 2 * bq * w;
         float sr = 0.0f, si = 0.0f;
         for (int o = 0; o < w; o++) {
-            const float rr = __bfloat162float(Rk[(o * w + c) * 2]), ri = __bfloat162float(Rk[(o * w + c) * 2 + 1]);
-            const float dr = ds[2 * (bq * w + o)], di = ds[2 * (bq * w + o) + 1];
-            sr += rr * dr + ri * di;
-            si += rr * di - ri * dr;
+            const float2 rc = rs[o * (w + 1) + c];
+            const float dr = db[2 * o], di = db[2 * o + 1];
+            sr += rc.x * dr + rc.y * di;
+            si += rc.x * di - rc.y * dr;
         }
         dz[i * plane + ore] = sr;
         dz[i * plane + oim] = si;
     }
-    // dR[o][c] += sum_b dy[b][o] conj(z[b][c])
+    // dR[o][c] += sum_b dy[b][o] conj(z[b][c]); consecutive threads walk c (coalesced)
     for (int i = threadIdx.x; i < w * w; i += blockDim.x) {
         const int o = i / w, c = i % w;
         float sr = 0.0f, si = 0.0f;
@@ -468,7 +482,10 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, int B, cudaStre
     FN_CUDA(gemm(2 * m, m, G, f->FyB, G, 0, 0, a + m, 2 * m, 0, 0, z, m, 1.0f, (int)bc, 0, (long)G * 2 * m, 2L * m * m,
                  nullptr, 0, st));
     // y = R z per mode
-    k_modemix<<<m * m, 256, sizeof(float) * 2 * B * w, st>>>(f->pbf + f->L.R[l], z, f->y, B, w, m);
+    const size_t smf = sizeof(float) * (2 * B * w + 2 * w * (w + 1));
+    if (smf > 227 * 1024) return err(ATMWFS_ERR_INVALID, "batch %d x width %d exceeds the mode-mixing shared memory", B, w);
+    if (smf > 48 * 1024) FN_CUDA(cudaFuncSetAttribute(k_modemix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+    k_modemix<<<m * m, 256, smf, st>>>(f->pbf + f->L.R[l], z, f->y, B, w, m);
     FN_CUDA(cudaGetLastError());
     // bb = Gy y per (b, o): bb_re = Gyr y_re + Gyin y_im; bb_im = Gyi y_re + Gyr y_im  ([G, m] x [m, m])
     const long ys = 2L * m * m, bs = (long)G * 2 * m;
@@ -500,7 +517,10 @@ atmwfs_status spectral_bwd(atmwfs_fno* f, int l, const float* ds, float* dh, int
     FN_CUDA(gemm(m, m, G, f->Gyr, m, 1, 0, f->dbb + m, 2 * m, 0, 0, f->dy + (long)m * m, m, 1.0f, (int)bc, 0, bs, ys,
                  nullptr, 0, st));
     // dz, dR
-    k_modemix_bwd<<<m * m, 256, sizeof(float) * 4 * B * w, st>>>(f->pbf + f->L.R[l], f->z[l], f->dy, f->dz,
+    const size_t smb = sizeof(float) * (4 * B * w + 2 * w * (w + 1));
+    if (smb > 227 * 1024) return err(ATMWFS_ERR_INVALID, "batch %d x width %d exceeds the mode-mixing shared memory", B, w);
+    if (smb > 48 * 1024) FN_CUDA(cudaFuncSetAttribute(k_modemix_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    k_modemix_bwd<<<m * m, 256, smb, st>>>(f->pbf + f->L.R[l], f->z[l], f->dy, f->dz,
                                                                  f->grads + f->L.R[l], B, w, m);
     FN_CUDA(cudaGetLastError());
     // da_re = FyA^T dz; da_im = FyB^T dz  ([G, 2m] x [2m, m])
@@ -587,8 +607,9 @@ atmwfs_status atmwfs_fno_create(const atmwfs_fno_cfg* cfg, uint64_t seed, atmwfs
     if (!cfg || !out) return err(ATMWFS_ERR_INVALID, "null argument");
     *out = nullptr;
     const atmwfs_fno_cfg& c = *cfg;
-    if (c.nin < 1 || c.width < 1 || c.modes < 2 || (c.modes & 1) || c.layers < 1 || c.proj < 1 || c.nout < 1 ||
-        c.grid < 8 || c.modes > c.grid / 2)
+    // an even width keeps every parameter tensor's offset even (paired BF16 loads)
+    if (c.nin < 1 || c.width < 2 || (c.width & 1) || c.modes < 2 || (c.modes & 1) || c.layers < 1 || c.proj < 1 ||
+        c.nout < 1 || c.grid < 8 || c.modes > c.grid / 2)
         return err(ATMWFS_ERR_INVALID, "bad FNO configuration");
     atmwfs_fno* f = new atmwfs_fno;
     f->cfg = c;

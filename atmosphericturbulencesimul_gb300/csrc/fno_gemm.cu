@@ -28,14 +28,6 @@ cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
 {
     GemmArgs g = g0;
     if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
-    if (beta != 1.0f) {
-        const int nb = g.sC == 0 ? 1 : g.batch;  // a batch summed into one C scales it once
-        const dim3 grid((unsigned)std::min((g.N + 255) / 256, 64), (unsigned)std::min(g.M, 1024), (unsigned)nb);
-        k_scale_rows<<<grid, 256, 0, st>>>(g.C, g.ldc, g.sC, g.M, g.N, beta);
-        const cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-    }
-    if (g.K <= 0) return cudaSuccess;
     const bool bm128 = g.M > 64, bn128 = g.N > 64;
     const int BM = bm128 ? 128 : 64, BN = bn128 ? 128 : 64;
     const long tiles = (long)((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN) * g.batch;
@@ -45,6 +37,17 @@ cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
     while (split < 64 && tiles * split < 4 * 152 && kchunks / (split * 2) >= 4) split *= 2;
     if (g.splitk < 1) g.splitk = split;
     if ((long)g.batch * g.splitk > 65535) g.splitk = std::max(1, 65535 / g.batch);
+    const bool atomic = g.splitk > 1 || (g.batch > 1 && g.sC == 0);
+    g.beta = beta;
+    if ((atomic || g.K <= 0) && beta != 1.0f) {
+        // shared accumulation (or no product): scale or clear C once
+        const int nb = g.sC == 0 ? 1 : g.batch;
+        const dim3 grid((unsigned)std::min((g.N + 255) / 256, 64), (unsigned)std::min(g.M, 1024), (unsigned)nb);
+        k_scale_rows<<<grid, 256, 0, st>>>(g.C, g.ldc, g.sC, g.M, g.N, beta);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (g.K <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((g.M + BM - 1) / BM), (unsigned)((g.N + BN - 1) / BN), (unsigned)(g.batch * g.splitk));
     if (bm128 && bn128) gemm::k_gemm<128, 128><<<grid, 256, 0, st>>>(g);
     else if (!bm128 && bn128) gemm::k_gemm<64, 128><<<grid, 256, 0, st>>>(g);

@@ -3,9 +3,10 @@
 // with BF16 tensor-core products (mma.sync m16n8k16) and FP32
 // accumulation.  Operands are read as FP32 or BF16 from global memory and
 // rounded to BF16 while they are staged in shared memory; C is FP32.
-// Split-K over grid.z, and batches summed into one C (batch stride 0 for
-// C, as weight gradients are), accumulate with atomics into a C that
-// gemm_launch has prepared (beta applied once).
+// The epilogue applies beta itself (C is read only when beta != 0), except
+// for split-K over grid.z and batches summed into one C (batch stride 0
+// for C, as weight gradients are): those accumulate with atomics into a C
+// that gemm_launch has scaled by beta beforehand.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -24,6 +25,7 @@ struct GemmArgs {
     int ta, tb;           // 1: A stored K x M / B stored N x K
     int a_bf16, b_bf16;   // storage type of A / B (else FP32)
     float alpha;
+    float beta;           // applied in the epilogue unless the C is shared (atomic accumulation)
     const float* bias;    // added once (first split) or NULL
     int bias_rows;        // 1: bias[m] per row, else bias[n] per column
     int splitk;           // K ranges over grid.z % splitk
@@ -62,10 +64,42 @@ struct Shape {
     static_assert(TM >= 1 && TN >= 1 && WM * WN == 8, "256 threads");
 };
 
+// Four consecutive elements along the operand's contiguous dimension:
+// one vector load when they are in range and aligned, else element loads
+// with zero fill.
+__device__ __forceinline__ float4 ld4(const char* base, long i, long lim, int bf, bool vec)
+{
+    if (vec && i + 3 < lim) {
+        if (bf) {
+            const uint2 u = *reinterpret_cast<const uint2*>(base + i * 2);
+            const __nv_bfloat162 lo = *reinterpret_cast<const __nv_bfloat162*>(&u.x);
+            const __nv_bfloat162 hi = *reinterpret_cast<const __nv_bfloat162*>(&u.y);
+            return make_float4(__low2float(lo), __high2float(lo), __low2float(hi), __high2float(hi));
+        }
+        return *reinterpret_cast<const float4*>(base + i * 4);
+    }
+    float4 r;
+    r.x = i + 0 < lim ? ld_elem(base, i + 0, bf) : 0.0f;
+    r.y = i + 1 < lim ? ld_elem(base, i + 1, bf) : 0.0f;
+    r.z = i + 2 < lim ? ld_elem(base, i + 2, bf) : 0.0f;
+    r.w = i + 3 < lim ? ld_elem(base, i + 3, bf) : 0.0f;
+    return r;
+}
+
+__device__ __forceinline__ uint2 pack4(float4 v)
+{
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+    uint2 u;
+    u.x = *reinterpret_cast<const uint32_t*>(&lo);
+    u.y = *reinterpret_cast<const uint32_t*>(&hi);
+    return u;
+}
+
 template <int BM, int BN>
 __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
 {
     using S = Shape<BM, BN>;
+    constexpr int NA = BM * BK / 1024, NB = BN * BK / 1024;  // 4-element groups per thread
     __shared__ __align__(16) __nv_bfloat16 As[BM][BK + PADK];
     __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + PADK];  // n-major: k contiguous
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -73,13 +107,78 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
     const int gq = lane >> 2, tq = lane & 3;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
     const int bz = blockIdx.z / g.splitk, sk = blockIdx.z % g.splitk;
-    const char* Ab = reinterpret_cast<const char*>(g.A) + (size_t)bz * g.sA * (g.a_bf16 ? 2 : 4);
-    const char* Bb = reinterpret_cast<const char*>(g.B) + (size_t)bz * g.sB * (g.b_bf16 ? 2 : 4);
+    const int esa = g.a_bf16 ? 2 : 4, esb = g.b_bf16 ? 2 : 4;
+    const char* Ab = reinterpret_cast<const char*>(g.A) + (size_t)bz * g.sA * esa;
+    const char* Bb = reinterpret_cast<const char*>(g.B) + (size_t)bz * g.sB * esb;
     float* Cb = g.C + (size_t)bz * g.sC;
+    // vector loads need the contiguous dimension's stride and the base aligned
+    const bool va = (g.lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(Ab) & (4 * esa - 1)) == 0);
+    const bool vb = (g.ldb % 4 == 0) && ((reinterpret_cast<uintptr_t>(Bb) & (4 * esb - 1)) == 0);
     // K range of this split, a multiple of BK
     const int kchunks = (g.K + BK - 1) / BK;
     const int per = (kchunks + g.splitk - 1) / g.splitk;
     const int kc0 = sk * per, kc1 = min(kchunks, kc0 + per);
+
+    float4 ra[NA], rb[NB];
+    auto load = [&](int kc) {
+        const int k0 = kc * BK;
+#pragma unroll
+        for (int j = 0; j < NA; j++) {
+            const int e = (tid + 256 * j) * 4;
+            if (g.ta) {  // stored K x M: 4 consecutive m
+                const int kk = e / BM, mm = e % BM, k = k0 + kk;
+                ra[j] = (k < g.K) ? ld4(Ab + (size_t)k * g.lda * esa, m0 + mm, g.M, g.a_bf16, va)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {     // stored M x K: 4 consecutive k
+                const int mm = e / BK, kk = e % BK, m = m0 + mm;
+                ra[j] = (m < g.M) ? ld4(Ab + (size_t)m * g.lda * esa, k0 + kk, g.K, g.a_bf16, va)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            const int e = (tid + 256 * j) * 4;
+            if (g.tb) {  // stored N x K: 4 consecutive k
+                const int nn = e / BK, kk = e % BK, n = n0 + nn;
+                rb[j] = (n < g.N) ? ld4(Bb + (size_t)n * g.ldb * esb, k0 + kk, g.K, g.b_bf16, vb)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {     // stored K x N: 4 consecutive n
+                const int kk = e / BN, nn = e % BN, k = k0 + kk;
+                rb[j] = (k < g.K) ? ld4(Bb + (size_t)k * g.ldb * esb, n0 + nn, g.N, g.b_bf16, vb)
+                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+    };
+    auto store = [&]() {
+#pragma unroll
+        for (int j = 0; j < NA; j++) {
+            const int e = (tid + 256 * j) * 4;
+            if (g.ta) {
+                const int kk = e / BM, mm = e % BM;
+                As[mm + 0][kk] = __float2bfloat16_rn(ra[j].x);
+                As[mm + 1][kk] = __float2bfloat16_rn(ra[j].y);
+                As[mm + 2][kk] = __float2bfloat16_rn(ra[j].z);
+                As[mm + 3][kk] = __float2bfloat16_rn(ra[j].w);
+            } else {
+                const int mm = e / BK, kk = e % BK;
+                *reinterpret_cast<uint2*>(&As[mm][kk]) = pack4(ra[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NB; j++) {
+            const int e = (tid + 256 * j) * 4;
+            if (g.tb) {
+                const int nn = e / BK, kk = e % BK;
+                *reinterpret_cast<uint2*>(&Bs[nn][kk]) = pack4(rb[j]);
+            } else {
+                const int kk = e / BN, nn = e % BN;
+                Bs[nn + 0][kk] = __float2bfloat16_rn(rb[j].x);
+                Bs[nn + 1][kk] = __float2bfloat16_rn(rb[j].y);
+                Bs[nn + 2][kk] = __float2bfloat16_rn(rb[j].z);
+                Bs[nn + 3][kk] = __float2bfloat16_rn(rb[j].w);
+            }
+        }
+    };
 
     float acc[S::TM][S::TN][4];
 #pragma unroll
@@ -89,30 +188,12 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
 #pragma unroll
             for (int q = 0; q < 4; q++) acc[i][j][q] = 0.0f;
 
+    if (kc0 < kc1) load(kc0);
     for (int kc = kc0; kc < kc1; kc++) {
-        const int k0 = kc * BK;
+        __syncthreads();  // the previous chunk's fragments are read
+        store();
         __syncthreads();
-        // stage A: BM x BK elements, op(A)[m][k]
-        for (int e = tid; e < BM * BK; e += 256) {
-            int mm, kk;
-            if (g.ta) { mm = e % BM; kk = e / BM; }   // stored K x M: m contiguous
-            else { kk = e % BK; mm = e / BK; }        // stored M x K: k contiguous
-            const int m = m0 + mm, k = k0 + kk;
-            float v = 0.0f;
-            if (m < g.M && k < g.K) v = ld_elem(Ab, g.ta ? (long)k * g.lda + m : (long)m * g.lda + k, g.a_bf16);
-            As[mm][kk] = __float2bfloat16_rn(v);
-        }
-        // stage B: BK x BN elements, op(B)[k][n] stored n-major
-        for (int e = tid; e < BN * BK; e += 256) {
-            int nn, kk;
-            if (g.tb) { kk = e % BK; nn = e / BK; }   // stored N x K: k contiguous
-            else { nn = e % BN; kk = e / BN; }        // stored K x N: n contiguous
-            const int n = n0 + nn, k = k0 + kk;
-            float v = 0.0f;
-            if (n < g.N && k < g.K) v = ld_elem(Bb, g.tb ? (long)n * g.ldb + k : (long)k * g.ldb + n, g.b_bf16);
-            Bs[nn][kk] = __float2bfloat16_rn(v);
-        }
-        __syncthreads();
+        if (kc + 1 < kc1) load(kc + 1);  // next chunk's global loads overlap this chunk's products
 #pragma unroll
         for (int ks = 0; ks < BK; ks += 16) {
             uint32_t af[S::TM][4], bfr[S::TN][2];
@@ -151,8 +232,9 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
                 if (g.bias && sk == 0 && (bz == 0 || g.sC != 0)) v += g.bias_rows ? g.bias[m] : g.bias[n];
                 float* c = Cb + (size_t)m * g.ldc + n;
                 // split K, or a batch summed into one C: several CTAs add here
+                // (gemm_launch scaled C by beta beforehand)
                 if (g.splitk > 1 || (g.batch > 1 && g.sC == 0)) atomicAdd(c, v);
-                else *c += v;
+                else *c = g.beta == 0.0f ? v : fmaf(g.beta, *c, v);
             }
 }
 

@@ -14,7 +14,10 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "atmwfs.h"
+#include "atmwfs_fno.h"
 #include "atmwfs_mkwfs.h"
 
 namespace atmwfs {
@@ -90,13 +93,53 @@ atmwfs_status write_cube(const std::string& name, const std::vector<float>& cube
 struct Resources {
     atmwfs_ctx* ctx = nullptr;
     atmwfs_shm* shm[4] = {nullptr, nullptr, nullptr, nullptr};
+    atmwfs_fno* fno = nullptr;
+    std::vector<void*> dev;
     ~Resources()
     {
         for (atmwfs_shm* s : shm)
             if (s) atmwfs_shm_close(s);
+        for (void* p : dev) cudaFree(p);
+        if (fno) atmwfs_fno_destroy(fno);
         if (ctx) atmwfs_destroy(ctx);
     }
+    float* alloc(size_t n)
+    {
+        void* p = nullptr;
+        if (cudaMalloc(&p, n * sizeof(float)) != cudaSuccess) return nullptr;
+        dev.push_back(p);
+        return (float*)p;
+    }
 };
+
+// Surrogate frame: windows of every instance -> network -> amplitude and
+// phase (phi + arg(1 + D)), cropped to Wout into the host frame block.
+struct SurrogateStep {
+    float *win, *lam, *in, *phi, *out, *amp, *pha;
+};
+
+atmwfs_status surrogate_frame(Resources& R, const SurrogateStep& b, int ni, int L, long W, long Wout, const long* off,
+                              float* hpha, float* hamp)
+{
+    const long P = W * W;
+    MK_TRY(atmwfs_advance(R.ctx, 1));
+    for (int i = 0; i < ni; i++) MK_TRY(atmwfs_windows_dev(R.ctx, i, b.win + (size_t)i * L * P, nullptr));
+    void* st = atmwfs_stream(R.ctx);
+    MK_TRY(atmwfs_fno_prepare(b.win, b.lam, ni, L, (int)W, b.in, b.phi, st));
+    MK_TRY(atmwfs_fno_forward(R.fno, b.in, b.out, ni, st));
+    MK_TRY(atmwfs_fno_assemble(b.out, b.phi, ni, (int)W, b.amp, b.pha, st));
+    const long c0 = (W - Wout) / 2;
+    for (int i = 0; i < ni; i++) {
+        const size_t src = (size_t)i * P + (size_t)c0 * W + c0;
+        if (cudaMemcpy2DAsync(hpha + off[i], Wout * sizeof(float), b.pha + src, W * sizeof(float), Wout * sizeof(float),
+                              Wout, cudaMemcpyDeviceToHost, (cudaStream_t)st) != cudaSuccess ||
+            cudaMemcpy2DAsync(hamp + off[i], Wout * sizeof(float), b.amp + src, W * sizeof(float), Wout * sizeof(float),
+                              Wout, cudaMemcpyDeviceToHost, (cudaStream_t)st) != cudaSuccess)
+            return err(ATMWFS_ERR_CUDA, "surrogate frame copy failed");
+    }
+    if (cudaStreamSynchronize((cudaStream_t)st) != cudaSuccess) return err(ATMWFS_ERR_CUDA, "surrogate frame failed");
+    return ATMWFS_OK;
+}
 
 }  // namespace
 
@@ -261,6 +304,42 @@ extern "C" atmwfs_status atmwfs_mkwfs(const char* conf_file, float slambda_um, l
         if (isci >= 0) off_sci = atmwfs_frame_offset(R.ctx, isci);
         hpha.resize((size_t)ff * nframes);
         hamp.resize((size_t)ff * nframes);
+        // learned surrogate in real-time mode (SURROGATE_MODEL, a keyword of
+        // this engine): it stands in for the propagation when the model fits
+        // the run; otherwise the plain path runs
+        char mpath[200];
+        if (cf.realtime == 1 && atmwfs_conf_read(conf_file ? conf_file : "WFsim.conf", "SURROGATE_MODEL", mpath,
+                                                 sizeof mpath) == 1) {
+            atmwfs_fno* f = nullptr;
+            atmwfs_fno_cfg fc;
+            if (atmwfs_fno_load(mpath, &f) == ATMWFS_OK && atmwfs_fno_get_cfg(f, &fc) == ATMWFS_OK && fc.grid == W &&
+                fc.nin == L + 1 && fc.nout == 2 && amp) {
+                R.fno = f;
+            } else {
+                if (f) atmwfs_fno_destroy(f);
+                if (verbose) printf("surrogate \"%s\" does not fit this run: plain propagation\n", mpath);
+            }
+        }
+    }
+    SurrogateStep sb{};
+    long offs[2] = {off_ref, off_sci};
+    if (R.fno) {
+        const size_t P = (size_t)W * W;
+        sb.win = R.alloc((size_t)ni * L * P);
+        sb.lam = R.alloc(ni);
+        sb.in = R.alloc((size_t)ni * (L + 1) * P);
+        sb.phi = R.alloc((size_t)ni * P);
+        sb.out = R.alloc((size_t)ni * 2 * P);
+        sb.amp = R.alloc((size_t)ni * P);
+        sb.pha = R.alloc((size_t)ni * P);
+        if (!sb.win || !sb.lam || !sb.in || !sb.phi || !sb.out || !sb.amp || !sb.pha)
+            return err(ATMWFS_ERR_NOMEM, "surrogate buffers");
+        float lams[2];
+        for (int i = 0; i < ni; i++) lams[i] = (float)inst[i].lambda;
+        if (cudaMemcpy(sb.lam, lams, sizeof(float) * ni, cudaMemcpyHostToDevice) != cudaSuccess)
+            return err(ATMWFS_ERR_CUDA, "surrogate wavelength copy");
+        if (iref < 0) offs[0] = off_sci;  // instance order: the science instance comes first
+        if (verbose) printf("real-time frames from the surrogate model\n");
     }
     screens.clear();
 
@@ -308,7 +387,10 @@ extern "C" atmwfs_status atmwfs_mkwfs(const char* conf_file, float slambda_um, l
                     if (cf.simtdelay > 0) usleep((useconds_t)cf.simtdelay);
                     if (cf.waitforsem == 1) MK_TRY(atmwfs_shm_semwait(cf.waitsemimname, 0, opts.semwait_timeout));
                     atmwfs_sink sk{hpha.data() + (size_t)f * ff, hamp.data() + (size_t)f * ff, 1};
-                    MK_TRY(atmwfs_run(R.ctx, 1, &sk));
+                    if (R.fno)
+                        MK_TRY(surrogate_frame(R, sb, ni, (int)L, W, Wout, offs, sk.pha, sk.amp));
+                    else
+                        MK_TRY(atmwfs_run(R.ctx, 1, &sk));
                     if (iref >= 0) {
                         MK_TRY(stream(R.shm[0], sk.pha + off_ref, 1.0, 0));
                         MK_TRY(stream(R.shm[1], sk.amp + off_ref, 1.0, 0));

@@ -139,6 +139,10 @@ class Series:
             out.append((pha[:, o:o + n * n].reshape(nsteps, n, n), amp[:, o:o + n * n].reshape(nsteps, n, n)))
         return out
 
+    def advance(self, nsteps: int) -> None:
+        """Move the windows nsteps steps without propagating (for the surrogate)."""
+        check(self._lib.atmwfs_advance(self._ctx, int(nsteps)))
+
     def frame_offset(self, i: int) -> int:
         return int(self._lib.atmwfs_frame_offset(self._ctx, i))
 

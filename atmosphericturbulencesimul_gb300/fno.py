@@ -263,3 +263,65 @@ def train(model: Surrogate, src: PairSource, pairs: int, batch: int = 8, lr: flo
             if log and step % 50 == 0:
                 log(f"step {step}: pairs {seen}, loss {loss:.4e}")
     return losses
+
+
+def frame_flops(cfg: FnoConfig) -> float:
+    """Floating-point operations of one inference frame, as the products execute them."""
+    G, m, w, P = cfg.grid, cfg.modes, cfg.width, cfg.grid * cfg.grid
+    f = 2.0 * w * cfg.nin * P
+    per_layer = (2.0 * w * G * 2 * m * G            # DFT along x
+                 + 2 * 2.0 * 2 * m * m * G * w      # DFT along y (two real products)
+                 + 8.0 * w * w * m * m              # complex mode mixing
+                 + 4 * 2.0 * G * m * m * w          # inverse along y (four real products)
+                 + 2.0 * w * G * 2 * m * G          # inverse along x
+                 + 2.0 * w * w * P)                 # pointwise mixing
+    f += cfg.layers * per_layer
+    f += 2.0 * cfg.proj * w * P + 2.0 * cfg.nout * cfg.proj * P
+    return f
+
+
+def main(argv=None) -> int:
+    """Train the surrogate on plain-path pairs and report its error on held-out seeds.
+
+    python -m atmosphericturbulencesimul_gb300.fno --pairs 50000 --test 5000 --out fno256.bin --report r.json
+    """
+    import argparse
+    import json
+    import time
+
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--pairs", type=int, default=50000)
+    ap.add_argument("--test", type=int, default=5000)
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--count", type=int, default=64, help="plain-path instances per engine step")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--report", default=None)
+    a = ap.parse_args(argv)
+    cfg = FnoConfig(grid=a.grid)
+    src = PairSource(count=a.count, grid=a.grid, seed=a.seed)
+    test = PairSource(count=a.count, grid=a.grid, seed=a.seed + 1000)
+    model = Surrogate(cfg, seed=a.seed)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    losses = train(model, src, a.pairs, batch=a.batch, lr=a.lr, log=print)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    ev = evaluate(model, test, steps=max(1, a.test // a.count), batch=a.batch)
+    rep = {"config": asdict(cfg), "params": model.num_params, "pairs": a.pairs, "test_pairs": a.test,
+           "train_s": t_train, "pairs_per_s": a.pairs / t_train, "final_loss": float(np.mean(losses[-50:])),
+           "held_out": ev}
+    print(json.dumps(rep))
+    if a.out:
+        model.save(a.out)
+    if a.report:
+        with open(a.report, "w") as f:
+            json.dump(rep, f, indent=1)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

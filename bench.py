@@ -139,8 +139,71 @@ def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def surrogate_section(pairs: int = 4096) -> dict:
+    """The learned surrogate at 256^2 (7 layers): inference frames/s and
+    tensor-core roofline, and its held-out error against the plain Fresnel
+    path beside that of the geometric field.  Uses the model file named by
+    ATMWFS_FNO_MODEL when present, else trains one on `pairs` plain-path pairs."""
+    import torch
+    from atmosphericturbulencesimul_gb300 import fno as F
+    t0 = time.time()
+    path = os.environ.get("ATMWFS_FNO_MODEL")
+    src = None
+    if path and os.path.exists(path):
+        model = F.Surrogate(path=path)
+        how = f"model file {os.path.basename(path)}"
+    else:
+        model = F.Surrogate(F.FnoConfig(), seed=0)
+        src = F.PairSource(count=32, grid=256, seed=1)
+        F.train(model, src, pairs, batch=8, lr=1e-3)
+        how = f"trained here on {pairs} plain-path pairs"
+    t_train = time.time() - t0
+    test = F.PairSource(count=32, grid=256, seed=1001)
+    ev = F.evaluate(model, test, steps=2, batch=8)
+    # inference throughput on resident inputs, batch 16
+    x, *_ = test.step()
+    xb = torch.cat([x, x])[:16].contiguous()
+    out = torch.empty((16, 2, 256, 256), device="cuda")
+    for _ in range(3):
+        model.forward(xb, out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    reps = 10
+    for _ in range(reps):
+        model.forward(xb, out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    fps = 16 / (ms * 1e-3)
+    # the plain path on the same 32 instances at 256^2
+    s = test.series
+    s.run(3)
+    e0.record(torch.cuda.ExternalStream(s.stream))
+    s.run(20)
+    e1.record(torch.cuda.ExternalStream(s.stream))
+    torch.cuda.synchronize()
+    plain_fps = 20 * test.count / (e0.elapsed_time(e1) * 1e-3)
+    pk = peaks()
+    tflops = F.frame_flops(model.cfg) * fps / 1e12
+    roof = {"bound": "tensor", "achieved": round(tflops, 2), "peak": pk.get("bf16_tflops"), "unit": "TFLOP/s",
+            "frac": round(tflops / pk["bf16_tflops"], 4) if pk.get("bf16_tflops") else None,
+            "flops_per_frame": F.frame_flops(model.cfg), "peak_source": pk["source"]}
+    res = {"value": round(fps, 1), "unit": "frames/s", "grid": 256, "batch": 16, "ms_per_batch": round(ms, 3),
+           "model": {k: v for k, v in model.cfg.__dict__.items()}, "params": model.num_params, "weights": "bf16 (fp32 master)",
+           "how": how, "setup_s": round(t_train, 1), "roofline": roof, "plain_same_grid_fps": round(plain_fps, 1),
+           "error_vs_plain": {k: {m: round(v, 5) for m, v in d.items()} for k, d in ev.items()},
+           "error_note": "held-out seeds; 'model' = surrogate, 'geometric' = exp(i phi) without diffraction; "
+                         "opd_wrms_nm weights the wrapped phase error by the plain path's intensity"}
+    test.close()
+    if src:
+        src.close()
+    model.close()
+    return res
 
 
 def cpu_screens(wl: dict, threads: int):
@@ -203,6 +266,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -333,6 +397,8 @@ def main():
         line["cpu_baseline"] = {"value": round(fps, 4), "unit": "frames/s", "cores": threads, "kind": "port",
                                 "sample": sample + "; extrapolated to the workload mix"}
     s.close()
+    if rank == 0 and not args.no_surrogate:
+        line["surrogate"] = surrogate_section()
     if rank == 0:
         print(json.dumps(line))
     if dist:

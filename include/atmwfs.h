@@ -114,6 +114,11 @@ atmwfs_status atmwfs_normalize_screens_ext(atmwfs_ctx* ctx, float lambda_ref, fl
  * this call are written at offset s * wf_size^2 of the sink buffers. */
 atmwfs_status atmwfs_run(atmwfs_ctx* ctx, long nsteps, const atmwfs_sink* sink);
 
+/* Advance nsteps time steps (window positions and the step counter) without
+ * propagating: for callers that compute the frames another way, such as
+ * the learned surrogate, from atmwfs_windows_dev(). */
+atmwfs_status atmwfs_advance(atmwfs_ctx* ctx, long nsteps);
+
 /* Device pointers of the most recent frame of instance i (valid until the
  * next run call). */
 atmwfs_status atmwfs_frame_dev(atmwfs_ctx* ctx, int i, const float** pha, const float** amp);

@@ -162,3 +162,37 @@ def test_mkwfs_science_stream(lib, tmp_path, monkeypatch):
             for k in range(10):
                 libc.sem_unlink(f"{prefix}{q}_sem{k:02d}".encode())
             libc.sem_unlink(f"{prefix}{q}_semlog".encode())
+
+
+def test_mkwfs_realtime_surrogate_and_fallback(lib, tmp_path, monkeypatch):
+    """SURROGATE_MODEL in real-time mode: frames come from the network
+    (phase = geometric phase + arg(1 + D)); a model that does not fit the run
+    (another grid) leaves the plain propagation in place, bit for bit."""
+    from atmosphericturbulencesimul_gb300 import fno as F
+    from atmosphericturbulencesimul_gb300.mkwfs import cube_name, fits_read, mkwfs
+    gc = gcm.load("mkwfs")
+    monkeypatch.chdir(tmp_path)
+    _stage(gc, tmp_path)
+    # real time with factor 0: every frame at t = 0, so runs are comparable
+    rt = gc.conf + "REALTIME 1\nREALTIMEFACTOR 0\n"
+    sci = lambda q: fits_read(tmp_path / cube_name("WFS_files/wf_", 0, gc.slam, q))
+    (tmp_path / "WFsim.conf").write_text(rt)
+    mkwfs(gc.slam_um, 0, scoeff=gc.scoeff, roffset=gc.roffset)
+    plain_pha, plain_amp = sci("pha"), sci("amp")
+    # geometric phase of the same windows: the phase-only run
+    (tmp_path / "WFsim.conf").write_text(rt + "WAVEFRONT_AMPLITUDE 0\n")
+    mkwfs(gc.slam_um, 0, scoeff=gc.scoeff, roffset=gc.roffset)
+    geo = sci("pha")
+    # a fitting model (3 layers + wavelength, 64 grid)
+    F.Surrogate(F.FnoConfig(nin=4, width=8, modes=8, layers=1, proj=8, grid=64), seed=2).save(tmp_path / "m.bin")
+    (tmp_path / "WFsim.conf").write_text(rt + "SURROGATE_MODEL m.bin\n")
+    mkwfs(gc.slam_um, 0, scoeff=gc.scoeff, roffset=gc.roffset)
+    pha, amp = sci("pha"), sci("amp")
+    assert np.all(np.isfinite(pha)) and np.all(np.isfinite(amp))
+    assert not np.array_equal(amp, plain_amp)
+    assert np.median(np.abs(pha - geo)) < 0.5          # an untrained network keeps D small
+    # a model for another grid: the plain path runs
+    F.Surrogate(F.FnoConfig(nin=4, width=8, modes=8, layers=1, proj=8, grid=32), seed=2).save(tmp_path / "m32.bin")
+    (tmp_path / "WFsim.conf").write_text(rt + "SURROGATE_MODEL m32.bin\n")
+    mkwfs(gc.slam_um, 0, scoeff=gc.scoeff, roffset=gc.roffset)
+    assert np.array_equal(sci("pha"), plain_pha) and np.array_equal(sci("amp"), plain_amp)
