@@ -57,6 +57,7 @@ class Params(C.Structure):
         ("ninst", C.c_int),
         ("inst", C.POINTER(Instance)),
         ("ring", C.c_int),
+        ("fft_fp16", C.c_int),
     ]
 
 

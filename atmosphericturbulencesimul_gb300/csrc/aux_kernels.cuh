@@ -35,6 +35,13 @@ cudaError_t launch_pass_cfg_1024(int cfg, int var, dim3 grid, const PassArgs& a,
 cudaError_t launch_pass_cfg_2048(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw,
                                 cudaStream_t st);
 
+cudaError_t launch_pass_half_64(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st);
+cudaError_t launch_pass_half_128(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st);
+cudaError_t launch_pass_half_256(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st);
+cudaError_t launch_pass_half_512(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st);
+cudaError_t launch_pass_half_1024(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st);
+cudaError_t launch_pass_half_2048(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st);
+
 // Per-layer phase windows (W x W, screen orientation) of global instance
 // gidx at the last completed step, scaled by the instance's Scoeff.
 cudaError_t windows(const float* const* screens, const float* scoeff, int L, int M, const LayerPos* pos, int poscap,

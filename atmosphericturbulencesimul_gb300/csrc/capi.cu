@@ -3,6 +3,7 @@
 // src/AtmosphericTurbulence/AtmosphericTurbulence.c:1433-2560), the per-step
 // launch graph, and the unit-level operators.
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 
 #include <cmath>
 #include <cstdarg>
@@ -80,6 +81,19 @@ PassLauncherCfg pass_launcher_cfg(int N)
     }
 }
 
+PassLauncherHalf pass_launcher_half(int N)
+{
+    switch (N) {
+        case 64: return launch_pass_half_64;
+        case 128: return launch_pass_half_128;
+        case 256: return launch_pass_half_256;
+        case 512: return launch_pass_half_512;
+        case 1024: return launch_pass_half_1024;
+        case 2048: return launch_pass_half_2048;
+        default: return nullptr;
+    }
+}
+
 static bool pow2_in(long n, long lo, long hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; }
 
 // Concatenated stage twiddle tables of grid size N (build_twiddles).
@@ -142,6 +156,27 @@ static const float2* twiddles(int N)
     float2* d = nullptr;
     if (cudaMalloc(&d, sizeof(float2) * h.size()) != cudaSuccess) return nullptr;
     if (cudaMemcpy(d, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    cache[key] = d;
+    return d;
+}
+
+// The same tables rounded to FP16 for the FP16-transform passes.
+static const __half2* twiddles_half(int N)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, __half2*> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    auto key = std::make_pair(dev, N);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    const std::vector<float2> h = host_twiddles(N);
+    std::vector<__half2> hh(h.size());
+    for (size_t i = 0; i < h.size(); i++) hh[i] = __floats2half2_rn(h[i].x, h[i].y);
+    __half2* d = nullptr;
+    if (cudaMalloc(&d, sizeof(__half2) * hh.size()) != cudaSuccess) return nullptr;
+    if (cudaMemcpy(d, hh.data(), sizeof(__half2) * hh.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
     cache[key] = d;
     return d;
 }
@@ -246,6 +281,7 @@ using namespace atmwfs;
 struct atmwfs_ctx {
     // configuration
     int L = 0, ninst = 0, ring = 1;
+    bool fp16 = false;                   // FP16 transforms in the series passes
     long M = 0;
     float pupil = 0, zangle = 0, tstep = 0;
     int amplitude = 1, fresnel = 1, realtime = 0;
@@ -454,7 +490,10 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
                 if (var & OP_EPI) b += (double)cl.Nout * cl.Nout * 12.0;  // phase sum in, pha + amp out
                 *bytes = b * cnt;
             }
-            AW_CUDA(pass_launcher_cfg(cl.N)(cl.cfg, var, grid, a, &cl.maps[cl.cfg], twiddles(cl.N), st));
+            if (c->fp16 && var != kVarSingle)
+                AW_CUDA(pass_launcher_half(cl.N)(var, grid, a, &cl.maps[cl.cfg], twiddles_half(cl.N), st));
+            else
+                AW_CUDA(pass_launcher_cfg(cl.N)(cl.cfg, var, grid, a, &cl.maps[cl.cfg], twiddles(cl.N), st));
         }
     }
     return ATMWFS_OK;
@@ -507,7 +546,9 @@ atmwfs_status autotune(atmwfs_ctx* c)
     AW_CUDA(cudaEventCreate(&e1));
     atmwfs_status s = ATMWFS_OK;
     for (Class& cl : c->classes) {
-        if (force) {
+        if (c->fp16) {
+            cl.cfg = 2;  // the FP16-transform passes are compiled for configuration 2
+        } else if (force) {
             const int g = atoi(force);
             cl.cfg = (g >= 0 && g < kNumTileCfg) ? g : 0;
         } else {
@@ -624,6 +665,7 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
     c->L = p->nlayers;
     c->ninst = p->ninst;
     c->ring = p->ring < 1 ? 1 : p->ring;
+    c->fp16 = p->fft_fp16 != 0;
     c->M = p->master_size;
     c->pupil = p->pupil_scale;
     c->zangle = p->zangle;
@@ -732,6 +774,15 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                     CK(dalloc(c, (void**)&dh, sizeof(float2) * h.size()));
                     CKC(cudaMemcpy(dh, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice));
                     d.H = dh;
+                    if (c->fp16) {
+                        // N H (unit modulus) for the FP16 transforms
+                        std::vector<__half2> hh(h.size());
+                        for (size_t q = 0; q < h.size(); q++) hh[q] = __floats2half2_rn(h[q].x * N, h[q].y * N);
+                        __half2* dhh = nullptr;
+                        CK(dalloc(c, (void**)&dhh, sizeof(__half2) * hh.size()));
+                        CKC(cudaMemcpy(dhh, hh.data(), sizeof(__half2) * hh.size(), cudaMemcpyHostToDevice));
+                        d.Hh = dhh;
+                    }
                 }
                 // the ring holds the frames of all instances contiguously per slot
                 d.out_pha = c->d_out_pha + c->frame_off[i];

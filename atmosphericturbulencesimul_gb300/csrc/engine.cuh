@@ -23,6 +23,7 @@ struct LayerPos {
 struct InstDev {
     float2* fld[2];            // ping-pong N x N fields
     const float2* H;           // hop transfer tables, [P][N], 1-D, include 1/N
+    const void* Hh;            // the same as N H in FP16 (__half2), for FP16 transforms
     float scoeff[kMaxLayers];  // per-layer phase multiplier
     float* out_pha;            // this instance's frame in output slot 0; slot k at + k * ostride
     float* out_amp;
@@ -135,5 +136,9 @@ inline int rows_per_cta(int N) { return tile_cfg(N, 0).rr; }
 
 PassLauncher pass_launcher(int N);
 PassLauncherCfg pass_launcher_cfg(int N);
+// FP16-transform series passes (tile configuration 2); tw = FP16 twiddles
+typedef cudaError_t (*PassLauncherHalf)(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw,
+                                        cudaStream_t st);
+PassLauncherHalf pass_launcher_half(int N);
 
 }  // namespace atmwfs

@@ -9,6 +9,7 @@
 // gather + phasor, 1-D propagation]: a frame with P hops costs P + 1 passes.
 #pragma once
 #include "engine.cuh"
+#include "fft_half.cuh"
 #include "gather_core.cuh"
 
 namespace atmwfs {
@@ -181,22 +182,6 @@ __device__ __forceinline__ void prop_row(float2* v, float2* xrow, int t, const f
 // forward, +1 inverse; rev walks the radix sequence backwards (the inverse of
 // a propagation, which starts from the forward's register layout and ends in
 // the natural layout x[t + e T]).
-// Barrier of the threads that share one row's exchange buffer.  Thread
-// tid works on row tid / T, so rows of T <= 32 threads lie inside one warp
-// (a warp barrier suffices); rows of 64 threads use named barrier 1 + row.
-// Callers keep a CTA barrier wherever another row's data aliases the buffer.
-template <int T>
-__device__ __forceinline__ void row_sync()
-{
-    static_assert(T <= 32 ? (32 % T == 0) : (T % 32 == 0 && T <= 64 * 4), "rows must tile warps");
-    if constexpr (T <= 32) {
-        __syncwarp();
-    } else {
-        const int id = 1 + (int)threadIdx.x / T;
-        asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(T) : "memory");
-    }
-}
-
 template <int N, int T, int E>
 __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev)
 {
@@ -278,7 +263,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // ---------------------------------------------------------------------------
 // the pass kernel
 // ---------------------------------------------------------------------------
-template <int N, int RR, int MINB, int OPS, bool ALIAS>
+template <int N, int RR, int MINB, int OPS, bool ALIAS, bool HP = false>
 __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     k_pass(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps, const float2* __restrict__ tw)
 {
@@ -365,8 +350,14 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
             const bool run = ph == 0 ? ((OPS & OP_PROP1) != 0) : ((OPS & OP_PROP2) != 0);
             if (!run) continue;
             const int hop = ph == 0 ? a.hop1 : a.hop2;
-            const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
-            prop_row_rt<N, T, E>(v, xrow, t, tw, h);
+            if constexpr (HP) {
+                // FP16 transforms: tw is the FP16 twiddle table, Hh holds N H
+                prop_row_h<N, T, E>(v, xrow, t, reinterpret_cast<const __half2*>(tw),
+                                    reinterpret_cast<const __half2*>(I->Hh) + (size_t)hop * N);
+            } else {
+                const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
+                prop_row_rt<N, T, E>(v, xrow, t, tw, h);
+            }
         }
     }
 
@@ -578,7 +569,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 2)
 }
 
 // host launcher for one (N, tile configuration)
-template <int N, int RR, int MINB, bool ALIAS>
+template <int N, int RR, int MINB, bool ALIAS, bool HP = false>
 cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
 {
     using G = PassGeom<N, RR>;
@@ -590,12 +581,22 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         constexpr size_t sm = G::smem(VAR, ALIAS);                                                     \
         static bool attr = false;                                                                      \
         if (!attr) {                                                                                   \
-            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS, HP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
             if (e != cudaSuccess) return e;                                                            \
             attr = true;                                                                               \
         }                                                                                              \
-        k_pass<N, RR, MINB, VAR, ALIAS><<<grid, block, sm, st>>>(a, m, tw);                            \
+        k_pass<N, RR, MINB, VAR, ALIAS, HP><<<grid, block, sm, st>>>(a, m, tw);                        \
         return cudaGetLastError();                                                                     \
+    }
+    if constexpr (HP) {
+        // FP16 transforms: the series passes only
+        switch (var) {
+            AW_CASE(kVarFirst)
+            AW_CASE(kVarMid)
+            AW_CASE(kVarLast)
+            AW_CASE(kVarSingle)
+            default: return cudaErrorInvalidValue;
+        }
     }
     switch (var) {
         AW_CASE(kVarFirst)
@@ -626,6 +627,14 @@ cudaError_t launch_pass_n(int var, dim3 grid, const PassArgs& a, const TmaSet* m
 {
     constexpr TileCfg c0 = tile_cfg(N, 0);
     return launch_pass_t<N, c0.rr, c0.minb, c0.alias>(var, grid, a, maps, tw, st);
+}
+
+// FP16-transform passes: tile configuration 2, tw = the FP16 twiddle table
+template <int N>
+cudaError_t launch_pass_hn(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw, cudaStream_t st)
+{
+    constexpr TileCfg c2 = tile_cfg(N, 2);
+    return launch_pass_t<N, c2.rr, c2.minb, c2.alias, true>(var, grid, a, maps, reinterpret_cast<const float2*>(tw), st);
 }
 
 template <int N>

@@ -12,4 +12,10 @@ cudaError_t launch_pass_cfg_1024(int cfg, int var, dim3 grid, const PassArgs& a,
 {
     return launch_pass_nc<1024>(cfg, var, grid, a, maps, tw, st);
 }
+
+cudaError_t launch_pass_half_1024(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const void* tw,
+                                cudaStream_t st)
+{
+    return launch_pass_hn<1024>(var, grid, a, maps, tw, st);
+}
 }  // namespace atmwfs

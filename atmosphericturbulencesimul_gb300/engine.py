@@ -49,7 +49,7 @@ class Series:
     def __init__(self, alt, cn2, speed, direction, *, master_size: int, instances: list[InstanceSpec],
                  pupil_scale: float, time_step: float, fresnel_bin: float = 0.0, zangle: float = 0.0,
                  amplitude: int = 1, fresnel: int = 1, realtime: int = 0, realtime_factor: float = 1.0,
-                 ring: int = 1):
+                 ring: int = 1, fft_fp16: int = 0):
         self._lib = _lib.load()
         self.L = len(alt)
         self._keep = []
@@ -84,6 +84,7 @@ class Series:
         p.ninst = len(instances)
         p.inst = insts
         p.ring = int(ring)
+        p.fft_fp16 = int(fft_fp16)
         ctx = C.c_void_p()
         check(self._lib.atmwfs_create(C.byref(p), C.byref(ctx)))
         self._ctx = ctx

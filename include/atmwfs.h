@@ -71,6 +71,8 @@ typedef struct atmwfs_params {
     int ninst;
     const atmwfs_instance* inst;
     int ring;                 /* output frames kept on the device per instance (>= 1) */
+    int fft_fp16;             /* 1: FFT stages of the propagation in FP16 with per-stage power-of-two
+                                 scaling (precision study); 0: FP32                               */
 } atmwfs_params;
 
 typedef struct atmwfs_ctx atmwfs_ctx;
