@@ -170,6 +170,7 @@ SIGNATURES = [
     ("atmwfs_shm_close", None, [C.c_void_p]),
     ("atmwfs_shm_semwait", C.c_int, [C.c_char_p, C.c_long, C.c_double]),
     ("atmwfs_mkwfs", C.c_int, [C.c_char_p, C.c_float, C.c_long, C.POINTER(MkwfsOpts)]),
+    ("atmwfs_make_hv_profile", C.c_int, [C.c_double, C.c_double, C.c_double, C.c_long, C.c_char_p, _dp]),
     ("atmwfs_windows_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_void_p]),
     ("atmwfs_advance", C.c_int, [_ctx, C.c_long]),
     # include/atmwfs_fno.h

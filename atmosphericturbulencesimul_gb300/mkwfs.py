@@ -59,6 +59,15 @@ def read_profile(path, site_alt: float = 0.0) -> np.ndarray:
     return out
 
 
+def make_hv_profile(outfile, wspeed: float, r0: float, sitealt: float, nlayers: int) -> float:
+    """The reference's mkHVturbprof: writes `outfile` (and conf_turb.txt in the
+    current directory); returns the seeing [arcsec]."""
+    see = C.c_double()
+    _lib.check(_lib.load().atmwfs_make_hv_profile(float(wspeed), float(r0), float(sitealt), int(nlayers),
+                                                  _b(outfile), C.byref(see)))
+    return see.value
+
+
 def fits_write(name, a: np.ndarray) -> None:
     """Write a float32 / float64 image of 1-3 axes (numpy order (z, y, x));
     a leading '!' in the name overwrites."""
@@ -151,5 +160,5 @@ def cube_name(prefix: str, tspan: int, slambda_m: float, kind: str) -> str:
     return f"{prefix}{tspan:08d}.{int(1.0e12 * slambda_m + 0.5):09d}.{kind}.fits"
 
 
-__all__ = ["conf_read", "conf_exists", "load_conf", "read_profile", "fits_write", "fits_read", "ShmImage",
+__all__ = ["conf_read", "conf_exists", "load_conf", "read_profile", "make_hv_profile", "fits_write", "fits_read", "ShmImage",
            "shm_semwait", "mkwfs", "cube_name"]

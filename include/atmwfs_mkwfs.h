@@ -98,6 +98,16 @@ atmwfs_status atmwfs_conf_load(const char* conf_file, atmwfs_conf* conf);
  * returned as read (atmwfs_create normalises it). */
 atmwfs_status atmwfs_profile_read(const char* path, double site_alt, double* layers, long cap, long* nlayers);
 
+/* Replaces AtmosphericTurbulence_makeHV_CN2prof (the mkHVturbprof command,
+ * AtmosphericTurbulence.c:7841-7940): a Hufnagel-Valley profile of
+ * `nlayers` layers from the site altitude to 30 km whose ground-layer
+ * strength is tuned so that r0 at 550 nm is r0 [m], for wind speed wspeed
+ * [m/s].  Writes `outfile` in the profile format above and, as the
+ * reference does, the seeing [arcsec] to conf_turb.txt in the current
+ * directory (also returned in *seeing if not NULL). */
+atmwfs_status atmwfs_make_hv_profile(double wspeed, double r0, double sitealt, long nlayers, const char* outfile,
+                                     double* seeing);
+
 /* ------------------------------------------------------------------ */
 /* FITS images                                                          */
 /* ------------------------------------------------------------------ */

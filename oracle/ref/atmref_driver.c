@@ -20,6 +20,9 @@
  *       read_config_parameter_exists and read_config_parameter
  *       (src/COREMOD_tools/COREMOD_tools.c:596-666) for each keyword; one
  *       line "CONF <keyword> <exists> <found> [<content>]" each.
+ *   atmref hv <wspeed> <r0> <sitealt> <nlayers> <outfile>
+ *       AtmosphericTurbulence_makeHV_CN2prof (AtmosphericTurbulence.c:7841),
+ *       which also writes conf_turb.txt in the current directory.
  *   atmref roffset <conf> <lambda_model> <lambda_ref> <slambda> <zangle> <alt>...
  *       the per-layer refraction offset RoffsetS - Roffset [m] that
  *       make_AtmosphericTurbulence_wavefront_series adds to the start row
@@ -179,5 +182,7 @@ int main(int argc, char **argv)
     if (strcmp(argv[1], "stdN") == 0) return cmd_stdn(argc, argv);
     if (strcmp(argv[1], "roffset") == 0) return cmd_roffset(argc, argv);
     if (strcmp(argv[1], "conf") == 0) return cmd_conf(argc, argv);
+    if (strcmp(argv[1], "hv") == 0 && argc >= 7)
+        return AtmosphericTurbulence_makeHV_CN2prof(atof(argv[2]), atof(argv[3]), atof(argv[4]), atol(argv[5]), argv[6]);
     return 2;
 }

@@ -216,16 +216,31 @@ def make_conf() -> dict:
     return {"text": CONF_TEXT, "reads": rows}
 
 
+# Hufnagel-Valley profiles: (wind speed, r0 at 550 nm, site altitude, layers)
+HV_CASES = [(10.0, 0.15, 4200.0, 10), (25.0, 0.08, 0.0, 7), (5.0, 0.3, 2500.0, 20)]
+
+
+def make_hv() -> dict:
+    out = []
+    with tempfile.TemporaryDirectory() as td:
+        for ws, r0, site, n in HV_CASES:
+            run([str(ATMREF), "hv", repr(ws), repr(r0), repr(site), str(n), "prof.txt"], td)
+            out.append({"args": [ws, r0, site, n], "profile": (Path(td) / "prof.txt").read_text(),
+                        "conf_turb": (Path(td) / "conf_turb.txt").read_text()})
+    return {"cases": out}
+
+
 def main():
     if not ATMREF.exists():
         sys.path.insert(0, str(ROOT / "oracle" / "ref"))
         import build_ref
         build_ref.build()
     (HERE / "conf.json").write_text(json.dumps(make_conf(), indent=1) + "\n")
+    (HERE / "hv.json").write_text(json.dumps(make_hv(), indent=1) + "\n")
     np.savez_compressed(HERE / "fresnel.npz", **make_fresnel())
     for name, case in MKWFS_CASES.items():
         np.savez_compressed(HERE / f"{name}.npz", **make_mkwfs(case))
-    print("wrote", ", ".join(["conf.json", "fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
+    print("wrote", ", ".join(["conf.json", "hv.json", "fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
 
 
 if __name__ == "__main__":

@@ -221,3 +221,24 @@ def test_mkwfs_rejects_bad_configuration_before_device_work(mk, tmp_path, monkey
     with pytest.raises(_lib.AtmwfsError) as e:
         mk.mkwfs(1.6)
     assert e.value.status == 1 and "site altitude" in str(e.value)
+
+
+def test_hv_profile_matches_reference(mk, tmp_path, monkeypatch):
+    """mkHVturbprof: the profile file and conf_turb.txt the reference wrote
+    (tests/golden/hv.json), to the printed digits."""
+    monkeypatch.chdir(tmp_path)
+    g = json.loads((gcm.GOLDEN / "hv.json").read_text())
+    for case in g["cases"]:
+        ws, r0, site, n = case["args"]
+        see = mk.make_hv_profile("prof.txt", ws, r0, site, n)
+        got = (tmp_path / "prof.txt").read_text().splitlines()
+        want = case["profile"].splitlines()
+        assert got[:2] == want[:2] and len(got) == len(want)
+        for a, b in zip(got[2:], want[2:]):
+            va, vb = np.array(a.split(), float), np.array(b.split(), float)
+            assert np.allclose(va, vb, rtol=0, atol=2e-6), (a, b)
+        assert abs(float((tmp_path / "conf_turb.txt").read_text()) - float(case["conf_turb"])) < 2e-6
+        assert abs(see - float(case["conf_turb"])) < 1e-6
+        # the profile reader accepts it
+        prof = mk.read_profile(tmp_path / "prof.txt", site)
+        assert prof.shape == (n, 8) and abs(prof[:, 1].sum() - 1.0) < 1e-5
