@@ -15,6 +15,11 @@ cudaError_t screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, do
 cudaError_t strf_lags(const float2* F, int M, double* acc, cudaStream_t st);
 cudaError_t split_scale(const float2* F, long n, double s1, double s2, float* o1, float* o2, cudaStream_t st);
 
+// Unnormalised 2-D DFT of an M x M grid for M = 4096 or 8192 (fft_large.cu);
+// tmp holds M x M complex values; in may equal out.
+bool fft2d_large_supported(long M);
+cudaError_t fft2d_large(const float2* in, float2* out, float2* tmp, int M, int sign, cudaStream_t st);
+
 cudaError_t launch_pass_64(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
 cudaError_t launch_pass_128(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);
 cudaError_t launch_pass_256(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);

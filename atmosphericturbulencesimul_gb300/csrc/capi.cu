@@ -1226,14 +1226,28 @@ atmwfs_status atmwfs_fft2d_dev(const void* in, void* out, long n, int sign, void
 {
     if (!in || !out) return fail(ATMWFS_ERR_INVALID, "null buffer");
     if (sign != -1 && sign != 1) return fail(ATMWFS_ERR_INVALID, "sign must be -1 or +1");
+    if (fft2d_large_supported(n)) {
+        cudaStream_t st = (cudaStream_t)stream;
+        float2* tmp = nullptr;
+        AW_CUDA(cudaMallocAsync((void**)&tmp, sizeof(float2) * n * n, st));
+        const cudaError_t e = fft2d_large((const float2*)in, (float2*)out, tmp, (int)n, sign, st);
+        cudaFreeAsync(tmp, st);
+        AW_CUDA(e);
+        return ATMWFS_OK;
+    }
     return two_pass(in, out, n, sign < 0 ? kVarUnitFwd : kVarUnitInv, nullptr, (cudaStream_t)stream);
 }
+
+static atmwfs_status fft_thunk(const void* in, void* out, long n, void* st, const void* arg);
 
 static atmwfs_status host_unit(const float* in, float* out, long n,
                                atmwfs_status (*fn)(const void*, void*, long, void*, const void*), const void* arg)
 {
     if (!in || !out) return fail(ATMWFS_ERR_INVALID, "null buffer");
-    if (!pow2_in(n, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "size %ld unsupported (power of two 64..2048)", n);
+    const bool big = fn == fft_thunk && fft2d_large_supported(n);
+    if (!pow2_in(n, 64, 2048) && !big)
+        return fail(ATMWFS_ERR_INVALID, "size %ld unsupported (power of two 64..2048%s)", n,
+                    fn == fft_thunk ? ", 4096 or 8192" : "");
     const size_t bytes = sizeof(float2) * n * n;
     void *din = nullptr, *dout = nullptr;
     AW_CUDA(cudaMalloc(&din, bytes));
@@ -1280,7 +1294,7 @@ atmwfs_status atmwfs_fft2d(const float* in, float* out, long n, int sign)
 atmwfs_status atmwfs_master_screen(uint64_t seed, uint32_t stream, long M, double outer_pix, double inner_pix,
                                    float* out1, float* out2, double* cfit)
 {
-    if (!pow2_in(M, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "M=%ld unsupported (power of two 64..2048)", M);
+    if (!pow2_in(M, 64, 8192)) return fail(ATMWFS_ERR_INVALID, "M=%ld unsupported (power of two 64..8192)", M);
     if (!(outer_pix > 0) || !(inner_pix > 0)) return fail(ATMWFS_ERR_INVALID, "scales must be > 0");
     const size_t n = (size_t)M * M;
     float2 *C = nullptr, *F = nullptr;

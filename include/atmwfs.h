@@ -202,14 +202,16 @@ atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long n, double d
                                      void* stream);
 
 /* do2dfft / do2dffti (src/fft/fft.c:1298-1315): unnormalised 2-D complex
- * DFT, sign -1 forward, +1 inverse. */
+ * DFT, sign -1 forward, +1 inverse.  n is a power of two in 64..2048, or
+ * 4096 / 8192 (rows in shared memory, columns through a transpose). */
 atmwfs_status atmwfs_fft2d(const float* in, float* out, long n, int sign);
 atmwfs_status atmwfs_fft2d_dev(const void* in, void* out, long n, int sign, void* stream);
 
 /* make_master_turbulence_screen (AtmosphericTurbulence.c:643-855) with a
  * seeded Philox4x32-10 noise source instead of the clock-seeded libc/GSL
  * generators.  Writes two M x M screens (either may be NULL) and the two
- * structure-function constants C1, C2 (may be NULL). */
+ * structure-function constants C1, C2 (may be NULL).  M is a power of two
+ * in 64..8192. */
 atmwfs_status atmwfs_master_screen(uint64_t seed, uint32_t stream, long M, double outer_pix, double inner_pix,
                                    float* out1, float* out2, double* cfit);
 
