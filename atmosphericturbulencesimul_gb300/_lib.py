@@ -1,5 +1,5 @@
 """ctypes binding of libatmwfs.so (the C ABI declared in include/atmwfs.h,
-include/atmwfs_mkwfs.h and include/atmwfs_fno.h).
+include/atmwfs_mkwfs.h, include/atmwfs_fno.h and include/atmwfs_psf.h).
 
 The library is the only compute path: if it is missing or cannot be loaded
 this module raises; there is no CPU fallback.
@@ -191,6 +191,19 @@ SIGNATURES = [
     ("atmwfs_fno_assemble", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("atmwfs_fno_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("atmwfs_fno_load", C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    # include/atmwfs_psf.h
+    ("atmwfs_psf_expo_accumulate_dev", C.c_int, [C.c_void_p, C.c_long, C.c_void_p, C.c_long, C.c_long, C.c_void_p,
+                                                 C.c_void_p]),
+    ("atmwfs_psf_expo_image_dev", C.c_int, [C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]),
+    ("atmwfs_psf_expo_load_dev", C.c_int, [C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]),
+    ("atmwfs_psf_expo_accumulate", C.c_int, [_fp, C.c_long, _fp, C.c_long, C.c_long, _fp]),
+    ("atmwfs_chromat_psf", C.c_int, [_fp, _fp, C.c_long, C.c_float, C.c_float, C.c_long, C.c_float, _fp]),
+    ("atmwfs_psf_measure", C.c_int, [_fp, C.c_long, _dp, _dp, _dp, _dp]),
+    ("atmwfs_gauss_filter", C.c_int, [_fp, C.c_long, C.c_long, C.c_float, C.c_int, _fp]),
+    ("atmwfs_center_psf", C.c_int, [_fp, C.c_long, C.c_long, _dp, _dp]),
+    ("atmwfs_measure_fwhm", C.c_int, [_fp, C.c_long, C.c_long, C.c_float, C.c_float, C.c_float, C.c_long, _fp]),
+    ("atmwfs_measure_enc_nrj", C.c_int, [_fp, C.c_long, C.c_long, C.c_float, C.c_float, C.c_float, _fp]),
+    ("atmwfs_expoframes", C.c_int, [C.c_char_p, C.c_float, C.c_char_p, _fp, C.c_long, C.c_int, _dp]),
     ("atmwfs_gemm_bf16", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_int, C.c_void_p,
                                    C.c_long, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_float, C.c_float, C.c_void_p,
                                    C.c_int, C.c_long, C.c_long, C.c_long, C.c_void_p]),

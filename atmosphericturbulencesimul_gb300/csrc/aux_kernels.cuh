@@ -18,6 +18,19 @@ cudaError_t split_scale(const float2* F, long n, double s1, double s2, float* o1
 // Unnormalised 2-D DFT of an M x M grid for M = 4096 or 8192 (fft_large.cu);
 // tmp holds M x M complex values; in may equal out.
 bool fft2d_large_supported(long M);
+
+// Concatenated stage twiddle tables of the in-CTA transform of size N
+// (64..2048), device memory owned by the library.
+const float2* stage_twiddles(int N);
+
+// PSF consumers (psf.cu): row and column passes of zero-padded fields and
+// the chromatic zoom sum.
+cudaError_t psf_rows(int N, const float* amp, long amp_fstride, const float* pha, long pha_fstride, const float* cscale,
+                     int W, int off, int B, float2* G, const float2* tw, cudaStream_t st);
+cudaError_t psf_cols(int N, const float2* G, int B, int W, int off, int mode, float* out, const float2* tw,
+                     cudaStream_t st);
+cudaError_t chromat_sum(const float* I, int S, int n, const float* coeff, const float* mcoeff, float* out,
+                        cudaStream_t st);
 cudaError_t fft2d_large(const float2* in, float2* out, float2* tmp, int M, int sign, cudaStream_t st);
 
 cudaError_t launch_pass_64(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st);

@@ -160,6 +160,8 @@ static const float2* twiddles(int N)
     return d;
 }
 
+const float2* stage_twiddles(int N) { return twiddles(N); }
+
 // The same tables rounded to FP16 for the FP16-transform passes.
 static const __half2* twiddles_half(int N)
 {

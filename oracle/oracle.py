@@ -63,6 +63,15 @@ class Oracle:
         L.or_philox.argtypes = [C.c_uint64, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32)]
         L.or_philox4.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
         L.or_screen_noise.argtypes = [C.c_uint64, C.c_uint32, C.c_long, _vp, _vp]
+        # PSF consumers (psf_oracle.c)
+        L.or_psf_expo_add.argtypes = [_vp, _vp, C.c_long, _vp]
+        L.or_chromat_psf.argtypes = [_vp, _vp, C.c_long, C.c_float, C.c_float, C.c_long, C.c_float, _vp]
+        L.or_gauss_filter.argtypes = [_vp, C.c_long, C.c_long, C.c_float, C.c_int, _vp]
+        L.or_center_psf.argtypes = [_vp, C.c_long, C.c_long, _dp, _dp]
+        L.or_measure_fwhm.argtypes = [_vp, C.c_long, C.c_long, C.c_double, C.c_double, C.c_double, C.c_long]
+        L.or_measure_fwhm.restype = C.c_double
+        L.or_measure_enc_nrj.argtypes = [_vp, C.c_long, C.c_long, C.c_double, C.c_double, C.c_double]
+        L.or_measure_enc_nrj.restype = C.c_double
 
     # -- basic operators -------------------------------------------------
     def set_threads(self, n: int) -> None:
@@ -174,6 +183,54 @@ class Oracle:
 
 
 # -- reference-semantics helpers in pure Python (small, exact restatements) --
+
+    # -- PSF consumers ---------------------------------------------------
+    def psf_expo(self, amp, pha):
+        """Exposure PSF (2W x 2W, centred) of the frames pha[f] with the
+        amplitude amp (one W x W image, or one per frame)."""
+        pha = np.asarray(pha)
+        if pha.ndim == 2:
+            pha = pha[None]
+        W = pha.shape[-1]
+        psf = np.zeros((2 * W, 2 * W), self.real)
+        for f in range(pha.shape[0]):
+            a = np.ascontiguousarray(amp[f] if np.ndim(amp) == 3 else amp, self.real)
+            p = np.ascontiguousarray(pha[f], self.real)
+            self.lib.or_psf_expo_add(_ptr(a), _ptr(p), W, _ptr(psf))
+        return psf
+
+    def chromat_psf(self, amp, pha, coeff1, coeff2, nbstep, apo):
+        a, p = (np.ascontiguousarray(x, self.real) for x in (amp, pha))
+        out = np.zeros_like(a)
+        self.lib.or_chromat_psf(_ptr(a), _ptr(p), a.shape[0], coeff1, coeff2, nbstep, apo, _ptr(out))
+        return out
+
+    def gauss_filter(self, img, sigma=3.0, size=10):
+        a = np.ascontiguousarray(img, self.real)
+        out = np.zeros_like(a)
+        self.lib.or_gauss_filter(_ptr(a), a.shape[1], a.shape[0], sigma, size, _ptr(out))
+        return out
+
+    def center_psf(self, img):
+        a = np.ascontiguousarray(img, self.real)
+        x, y = C.c_double(), C.c_double()
+        self.lib.or_center_psf(_ptr(a), a.shape[1], a.shape[0], C.byref(x), C.byref(y))
+        return x.value, y.value
+
+    def measure_fwhm(self, img, xc, yc, step=1.0, nb=None):
+        a = np.ascontiguousarray(img, self.real)
+        return self.lib.or_measure_fwhm(_ptr(a), a.shape[1], a.shape[0], xc, yc, step, nb or a.shape[1] // 2)
+
+    def measure_enc_nrj(self, img, xc, yc, fraction=0.5):
+        a = np.ascontiguousarray(img, self.real)
+        return self.lib.or_measure_enc_nrj(_ptr(a), a.shape[1], a.shape[0], xc, yc, fraction)
+
+    def psf_measure(self, psf):
+        """The exposure loop's measures: (xc, yc, fwhm, ee50) in pixels."""
+        g = self.gauss_filter(psf)
+        xc, yc = self.center_psf(g)
+        return xc, yc, self.measure_fwhm(g, xc, yc), self.measure_enc_nrj(psf, xc, yc)
+
 
 def scoeff_from_n(lam_ref_f32: float, lam_sci: float, n_sci_f32: float, n_ref_f32: float) -> float:
     """Scoeff = CONF_LAMBDA/SLAMBDA * Nslambda/Nlambda with the reference's

@@ -23,6 +23,17 @@
  *   atmref hv <wspeed> <r0> <sitealt> <nlayers> <outfile>
  *       AtmosphericTurbulence_makeHV_CN2prof (AtmosphericTurbulence.c:7841),
  *       which also writes conf_turb.txt in the current directory.
+ *   atmref expo <etime> <outfile>
+ *       measure_wavefront_series_expoframes (AtmosphericTurbulence.c:6592)
+ *       in the current directory (WFsim.conf with PUPIL_AMPL_FILE, the
+ *       science cubes under the fixed 1.65 um name).
+ *   atmref chromat <n> <amp.f32> <pha.f32> <coeff1> <coeff2> <nbstep> <apo> <out.f32>
+ *       PSF_makeChromatPSF (src/psf/psf.c:54) on raw n x n float images.
+ *   atmref measure <n> <in.f32> <gauss.f32>
+ *       the exposure loop's measures of a raw n x n float image:
+ *       gauss_filter(in, 3, 10) (written out), center_PSF, measure_FWHM on
+ *       the filtered image, measure_enc_NRJ(in, 0.5); one line
+ *       "MEAS <xc> <yc> <fwhm> <ee50>".
  *   atmref roffset <conf> <lambda_model> <lambda_ref> <slambda> <zangle> <alt>...
  *       the per-layer refraction offset RoffsetS - Roffset [m] that
  *       make_AtmosphericTurbulence_wavefront_series adds to the start row
@@ -40,6 +51,8 @@
 #include "AtmosphericTurbulence/AtmosphericTurbulence.h"
 #include "COREMOD_memory/COREMOD_memory.h"
 #include "WFpropagate/WFpropagate.h"
+#include "image_filter/image_filter.h"
+#include "psf/psf.h"
 
 DATA data;
 pid_t CLIPID;
@@ -167,6 +180,50 @@ static int cmd_roffset(int argc, char **argv)
     return 0;
 }
 
+static long read_raw(const char *path, const char *name, long n)
+{
+    long ID = create_2Dimage_ID(name, n, n);
+    FILE *f = fopen(path, "rb");
+    if (!f) return -1;
+    size_t got = fread(data.image[ID].array.F, sizeof(float), (size_t)(n * n), f);
+    fclose(f);
+    return got == (size_t)(n * n) ? ID : -1;
+}
+
+static int write_raw(const char *path, const char *name, long n)
+{
+    long ID = image_ID(name);
+    FILE *f = fopen(path, "wb");
+    if (!f || ID < 0) return 4;
+    fwrite(data.image[ID].array.F, sizeof(float), (size_t)(n * n), f);
+    fclose(f);
+    return 0;
+}
+
+static int cmd_chromat(int argc, char **argv)
+{
+    if (argc < 10) return 2;
+    long n = atol(argv[2]);
+    if (read_raw(argv[3], "amp", n) < 0 || read_raw(argv[4], "pha", n) < 0) return 3;
+    PSF_makeChromatPSF("amp", "pha", (float)atof(argv[5]), (float)atof(argv[6]), atol(argv[7]), (float)atof(argv[8]),
+                       "cpsf");
+    return write_raw(argv[9], "cpsf", n);
+}
+
+static int cmd_measure(int argc, char **argv)
+{
+    if (argc < 5) return 2;
+    long n = atol(argv[2]);
+    double xc = 0.0, yc = 0.0;
+    if (read_raw(argv[3], "PSF", n) < 0) return 3;
+    gauss_filter("PSF", "PSFg", 3, 10);
+    center_PSF("PSFg", &xc, &yc, n / 2);
+    float fw = measure_FWHM("PSFg", xc, yc, 1.0, n / 2);
+    float ee = measure_enc_NRJ("PSF", xc, yc, 0.5);
+    printf("MEAS %.17g %.17g %.9g %.9g\n", xc, yc, fw, ee);
+    return write_raw(argv[4], "PSFg", n);
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 2) {
@@ -182,6 +239,9 @@ int main(int argc, char **argv)
     if (strcmp(argv[1], "stdN") == 0) return cmd_stdn(argc, argv);
     if (strcmp(argv[1], "roffset") == 0) return cmd_roffset(argc, argv);
     if (strcmp(argv[1], "conf") == 0) return cmd_conf(argc, argv);
+    if (strcmp(argv[1], "expo") == 0 && argc >= 4) return measure_wavefront_series_expoframes((float)atof(argv[2]), argv[3]);
+    if (strcmp(argv[1], "chromat") == 0) return cmd_chromat(argc, argv);
+    if (strcmp(argv[1], "measure") == 0) return cmd_measure(argc, argv);
     if (strcmp(argv[1], "hv") == 0 && argc >= 7)
         return AtmosphericTurbulence_makeHV_CN2prof(atof(argv[2]), atof(argv[3]), atof(argv[4]), atol(argv[5]), argv[6]);
     return 2;

@@ -18,7 +18,7 @@ HERE = Path(__file__).resolve().parent
 REF = Path("/root/reference/src")
 OUT = HERE.parent / "_ref"
 
-# modules on the mkwfs path and their direct dependencies
+# modules on the mkwfs path, the PSF consumers and their direct dependencies
 REF_SOURCES = [
     "AtmosphericTurbulence/AtmosphericTurbulence.c",
     "WFpropagate/WFpropagate.c",
@@ -33,6 +33,9 @@ REF_SOURCES = [
     "statistic/statistic.c",
     "info/info.c",
     "00CORE/00CORE.c",
+    # the PSF consumers after the path and their image measures
+    "psf/psf.c",
+    "image_filter/image_filter.c",
 ]
 SHIMS = ["shim_fftw.c", "shim_fitsio.c", "shim_rng_stubs.c", "atmref_driver.c"]
 CFLAGS = ["-std=gnu99", "-O2", "-U_FORTIFY_SOURCE", "-D_FORTIFY_SOURCE=0", "-fcommon", "-w", "-ffp-contract=off", "-fno-builtin-rand",

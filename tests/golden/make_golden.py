@@ -13,8 +13,13 @@ sources by oracle/ref/build_ref.py) on small seeded cases.
                refraction offsets from its atmosphere model, and its
                lambda_ref and science phase/amplitude cubes.
 
+  psf.npz      the PSF consumers: measure_wavefront_series_expoframes
+               (AtmosphericTurbulence.c:6592), PSF_makeChromatPSF
+               (psf.c:54) and the image measures of the exposure loop.
+
 Run from the repository root where the reference is mounted:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          (every fixture)
+    python tests/golden/make_golden.py psf      (psf.npz only)
 """
 from __future__ import annotations
 
@@ -230,14 +235,112 @@ def make_hv() -> dict:
     return {"cases": out}
 
 
+def _pupil(n: int, rin: float = 0.0) -> np.ndarray:
+    y, x = np.mgrid[0:n, 0:n] - (n / 2 - 0.5)
+    r = np.hypot(x, y) / (n / 2)
+    return ((r < 1.0) & (r >= rin)).astype(np.float32)
+
+
+def _phase(n: int, seed: int, rms: float) -> np.ndarray:
+    """A smooth seeded phase screen (k^-11/6 filtered noise), rad."""
+    rng = np.random.default_rng(seed)
+    k = np.hypot(*np.meshgrid(np.fft.fftfreq(n), np.fft.fftfreq(n)))
+    k[0, 0] = 1.0
+    f = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * k ** (-11 / 6)
+    f[0, 0] = 0.0
+    p = np.fft.ifft2(f).real
+    return (p / p.std() * rms).astype(np.float32)
+
+
+PSF_EXPO = dict(W=64, nframes=8, ntspan=2, etime=0.003, dt=0.001)
+
+
+def make_psf() -> dict:
+    """PSF consumers: the exposure measures on three images, the chromatic
+    PSF on two pupils, and the exposure command on a two-span series whose
+    amplitude cube equals the pupil in every frame (so that the reference's
+    uninitialised amplitude_on selects the same field either way)."""
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        d = Path(td)
+        # measures
+        imgs = []
+        pup = _pupil(64)
+        f = np.zeros((128, 128), np.complex128)
+        f[32:96, 32:96] = pup * np.exp(1j * _phase(64, 1, 1.0))
+        imgs.append(np.abs(np.fft.fftshift(np.fft.fft2(f))) ** 2)
+        y, x = np.mgrid[0:64, 0:64]
+        imgs.append(np.exp(-((x - 37.3) ** 2 + (y - 28.6) ** 2) / (2 * 3.1 ** 2)) * 100.0 +
+                    np.random.default_rng(3).uniform(0.0, 0.5, (64, 64)))
+        f = np.zeros((128, 128), np.complex128)
+        f[32:96, 32:96] = _pupil(64, 0.3) * np.exp(1j * _phase(64, 2, 2.5))
+        imgs.append(np.abs(np.fft.fftshift(np.fft.fft2(f))) ** 2)
+        for k, im in enumerate(imgs):
+            im = im.astype(np.float32)
+            n = im.shape[0]
+            im.tofile(d / "in.f32")
+            txt = run([str(ATMREF), "measure", str(n), "in.f32", "g.f32"], td)
+            xc, yc, fw, ee = [float(v) for v in next(l for l in txt.splitlines() if l.startswith("MEAS")).split()[1:]]
+            out[f"meas_in{k}"] = im
+            out[f"meas_gauss{k}"] = np.fromfile(d / "g.f32", np.float32).reshape(n, n)
+            out[f"meas_val{k}"] = np.array([xc, yc, fw, ee])
+        # chromatic PSF
+        for k, (n, c1, c2, ns, apo, rms) in enumerate([(64, 0.8, 1.25, 5, 0.2, 0.7), (128, 1.0, 1.6, 4, 0.0, 1.5)]):
+            amp, pha = _pupil(n // 2 if n == 128 else n), None
+            amp = np.pad(amp, (n - amp.shape[0]) // 2) if amp.shape[0] < n else amp
+            pha = (_phase(n, 10 + k, rms) * (amp > 0)).astype(np.float32)
+            amp.astype(np.float32).tofile(d / "amp.f32")
+            pha.tofile(d / "pha.f32")
+            run([str(ATMREF), "chromat", str(n), "amp.f32", "pha.f32", repr(c1), repr(c2), str(ns), repr(apo),
+                 "cpsf.f32"], td)
+            out[f"chromat_amp{k}"] = amp.astype(np.float32)
+            out[f"chromat_pha{k}"] = pha
+            out[f"chromat_par{k}"] = np.array([n, c1, c2, ns, apo])
+            out[f"chromat_out{k}"] = np.fromfile(d / "cpsf.f32", np.float32).reshape(n, n)
+        # exposure command
+        c = PSF_EXPO
+        W = c["W"]
+        (d / "WFS_files").mkdir()
+        pup = _pupil(W)
+        fitsio.write(d / "pupil.fits", pup)
+        cube_cfg = dict(MKWFS_CASES["mkwfs"], Wout=W, W=W, nframes=c["nframes"], ntspan=c["ntspan"], dt=c["dt"])
+        (d / "WFsim.conf").write_text(conf_text(cube_cfg) + "PUPIL_AMPL_FILE pupil.fits\n")
+        phs = []
+        for t in range(c["ntspan"]):
+            ph = np.stack([_phase(W, 100 * t + f, 1.2) * pup for f in range(c["nframes"])]).astype(np.float32)
+            phs.append(ph)
+            fitsio.write(d / "WFS_files" / f"wf_{t:08d}.{1650000:09d}.pha.fits", ph)
+            fitsio.write(d / "WFS_files" / f"wf_{t:08d}.{1650000:09d}.amp.fits",
+                         np.repeat(pup[None], c["nframes"], 0))
+        txt = run([str(ATMREF), "expo", repr(c["etime"]), "expo.log"], td)
+        m = re.search(r"FWHM = (\S+) arcseconds", txt.splitlines()[-1] if txt else "")
+        out["expo_pupil"] = pup
+        out["expo_pha"] = np.stack(phs)
+        out["expo_conf"] = np.array(conf_text(cube_cfg) + "PUPIL_AMPL_FILE pupil.fits\n")
+        out["expo_log"] = np.array((d / "expo.log").read_text())
+        out["expo_final_fwhm"] = np.array(float(m.group(1)) if m else np.nan)
+        k = 0
+        while (d / f"PSF{k:04d}.fits").exists():
+            out[f"expo_psf{k}"] = fitsio.read(d / f"PSF{k:04d}.fits").astype(np.float32)
+            k += 1
+        out["expo_final"] = fitsio.read(d / "PSF").astype(np.float32)
+        out["expo_par"] = np.array([c["etime"], c["dt"], W, c["nframes"], c["ntspan"]])
+    return out
+
+
 def main():
     if not ATMREF.exists():
         sys.path.insert(0, str(ROOT / "oracle" / "ref"))
         import build_ref
         build_ref.build()
+    if sys.argv[1:] == ["psf"]:
+        np.savez_compressed(HERE / "psf.npz", **make_psf())
+        print("wrote psf.npz")
+        return
     (HERE / "conf.json").write_text(json.dumps(make_conf(), indent=1) + "\n")
     (HERE / "hv.json").write_text(json.dumps(make_hv(), indent=1) + "\n")
     np.savez_compressed(HERE / "fresnel.npz", **make_fresnel())
+    np.savez_compressed(HERE / "psf.npz", **make_psf())
     for name, case in MKWFS_CASES.items():
         np.savez_compressed(HERE / f"{name}.npz", **make_mkwfs(case))
     print("wrote", ", ".join(["conf.json", "hv.json", "fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
