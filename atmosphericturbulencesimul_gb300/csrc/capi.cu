@@ -331,6 +331,11 @@ struct atmwfs_ctx {
     std::vector<cudaStream_t> cls_st;
     cudaStream_t sum_st = nullptr;
     std::vector<cudaEvent_t> gev;
+    // copies to the caller's sink: their own stream, so that step g + 1
+    // computes while step g's frames leave; per device ring slot, the event
+    // after the step that wrote it and the event after its copy
+    cudaStream_t out_st = nullptr;
+    std::vector<cudaEvent_t> ev_written, ev_copied;
 };
 
 namespace {
@@ -875,6 +880,14 @@ void atmwfs_destroy(atmwfs_ctx* c)
     if (c->sum_st) cudaStreamDestroy(c->sum_st);
     for (auto e : c->gev)
         if (e) cudaEventDestroy(e);
+    if (c->out_st) {
+        cudaStreamSynchronize(c->out_st);
+        cudaStreamDestroy(c->out_st);
+    }
+    for (auto e : c->ev_written)
+        if (e) cudaEventDestroy(e);
+    for (auto e : c->ev_copied)
+        if (e) cudaEventDestroy(e);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
 }
@@ -977,6 +990,16 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
     if (nsteps < 0) return fail(ATMWFS_ERR_INVALID, "nsteps < 0");
     AW_TRY(commit(c));
     const size_t per = (size_t)c->ninst * c->L;
+    const bool copies = sink && (sink->pha || sink->amp);
+    if (copies && !c->out_st) {
+        AW_CUDA(cudaStreamCreateWithFlags(&c->out_st, cudaStreamNonBlocking));
+        c->ev_written.assign(c->ring, nullptr);
+        c->ev_copied.assign(c->ring, nullptr);
+        for (long r = 0; r < c->ring; r++) {
+            AW_CUDA(cudaEventCreateWithFlags(&c->ev_written[r], cudaEventDisableTiming));
+            AW_CUDA(cudaEventCreateWithFlags(&c->ev_copied[r], cudaEventDisableTiming));
+        }
+    }
     long s = 0;
     int b = 0;
     while (s < nsteps) {
@@ -1003,22 +1026,30 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
                                     cudaMemcpyHostToDevice, c->st));
         AW_CUDA(cudaEventRecord(c->ev[b], c->st));
         for (long i = 0; i < chunk; i++) {
+            const long slot = (g0 + i) % c->ring;
+            // the slot is free once its previous copy is done (a no-op for a
+            // slot never copied); with ring >= 2 this copy overlaps the next step
+            if (copies) AW_CUDA(cudaStreamWaitEvent(c->st, c->ev_copied[slot], 0));
             AW_CUDA(cudaGraphLaunch(c->gexec, c->st));
-            if (sink) {
-                const long slot = (g0 + i) % c->ring;
+            if (copies) {
+                AW_CUDA(cudaEventRecord(c->ev_written[slot], c->st));
+                AW_CUDA(cudaStreamWaitEvent(c->out_st, c->ev_written[slot], 0));
                 const long hs = sink->nslots > 0 ? (s + i) % sink->nslots : (s + i);
                 const size_t ff = c->frame_floats;
                 if (sink->pha)
                     AW_CUDA(cudaMemcpyAsync(sink->pha + (size_t)hs * ff, c->d_out_pha + slot * ff, sizeof(float) * ff,
-                                            cudaMemcpyDefault, c->st));
+                                            cudaMemcpyDefault, c->out_st));
                 if (sink->amp)
                     AW_CUDA(cudaMemcpyAsync(sink->amp + (size_t)hs * ff, c->d_out_amp + slot * ff, sizeof(float) * ff,
-                                            cudaMemcpyDefault, c->st));
+                                            cudaMemcpyDefault, c->out_st));
+                AW_CUDA(cudaEventRecord(c->ev_copied[slot], c->out_st));
             }
         }
         s += chunk;
         b ^= 1;
     }
+    // the caller's buffers hold every frame on return
+    if (copies) AW_CUDA(cudaStreamSynchronize(c->out_st));
     return check_status(c);
 }
 

@@ -174,10 +174,12 @@ def surrogate_section(pairs: int = 4096) -> dict:
     torch.cuda.synchronize()
     e0.record()
     reps = 10
+    torch.cuda.nvtx.range_push("timed")  # profilers can select the timed batches
     for _ in range(reps):
         model.forward(xb, out)
     e1.record()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1) / reps
     fps = 16 / (ms * 1e-3)
     # the plain path on the same 32 instances at 256^2
@@ -267,7 +269,13 @@ def main():
     ap.add_argument("--workload", default="batched")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate-only", action="store_true",
+                    help="time only the surrogate section (profiling); prints its JSON object")
+    ap.add_argument("--surrogate-pairs", type=int, default=4096, help="training pairs of the surrogate section")
     args = ap.parse_args()
+    if args.surrogate_only:
+        print(json.dumps(surrogate_section(args.surrogate_pairs)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -307,7 +315,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    s, screens = make_series(wl)
+    # two device output slots: the e2e copies of a step overlap the next step
+    s, screens = make_series(wl, ring=2)
     ninst = len(wl["inst"])
     L = len(wl["alt"])
     # warm-up (also captures the step graph)
@@ -398,7 +407,7 @@ def main():
                                 "sample": sample + "; extrapolated to the workload mix"}
     s.close()
     if rank == 0 and not args.no_surrogate:
-        line["surrogate"] = surrogate_section()
+        line["surrogate"] = surrogate_section(args.surrogate_pairs)
     if rank == 0:
         print(json.dumps(line))
     if dist:

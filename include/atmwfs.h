@@ -113,7 +113,10 @@ atmwfs_status atmwfs_normalize_screens_ext(atmwfs_ctx* ctx, float lambda_ref, fl
                                            long nextra, double* r0_pix);
 
 /* Run nsteps time steps (the frame loop, :2561-4345).  Frames of step s of
- * this call are written at offset s * wf_size^2 of the sink buffers. */
+ * this call are written at offset s * wf_size^2 of the sink buffers.  The
+ * copies into the sink run on a stream of their own: with ring >= 2 the
+ * copy of step s overlaps the computation of step s + 1 (with ring = 1 they
+ * alternate).  Every frame is in the sink when the call returns. */
 atmwfs_status atmwfs_run(atmwfs_ctx* ctx, long nsteps, const atmwfs_sink* sink);
 
 /* Advance nsteps time steps (window positions and the step counter) without
