@@ -108,6 +108,7 @@ class FnoCfg(C.Structure):
 
 
 REFRACTIVITY_FN = C.CFUNCTYPE(C.c_float, C.c_float, C.c_float, C.c_void_p)
+ABSORPTION_FN = C.CFUNCTYPE(C.c_double, C.c_float, C.c_float, C.c_void_p)
 
 
 class MkwfsOpts(C.Structure):
@@ -171,6 +172,10 @@ SIGNATURES = [
     ("atmwfs_shm_semwait", C.c_int, [C.c_char_p, C.c_long, C.c_double]),
     ("atmwfs_mkwfs", C.c_int, [C.c_char_p, C.c_float, C.c_long, C.POINTER(MkwfsOpts)]),
     ("atmwfs_make_hv_profile", C.c_int, [C.c_double, C.c_double, C.c_double, C.c_long, C.c_char_p, _dp]),
+    ("atmwfs_refraction_path", C.c_int, [C.c_double, C.c_double, C.c_double, REFRACTIVITY_FN, ABSORPTION_FN,
+                                         C.c_void_p, C.c_char_p, _dp, _dp]),
+    ("atmwfs_refraction_table", C.c_int, [_dp, C.c_long, _dp, C.c_long, C.c_double, _fp, _dp, C.c_long, C.c_double,
+                                          _dp, _dp]),
     ("atmwfs_windows_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_void_p]),
     ("atmwfs_advance", C.c_int, [_ctx, C.c_long]),
     # include/atmwfs_fno.h

@@ -67,7 +67,7 @@ struct atmwfs_fno {
     // activations for one batch size
     int cap = 0;
     std::vector<float*> h, u, a, z;     // h[0..nl], u[0..nl-1], a/z per layer
-    float *y = nullptr, *bb = nullptr, *spec = nullptr, *qpre = nullptr, *q = nullptr;
+    float *y = nullptr, *bb = nullptr, *qpre = nullptr, *q = nullptr;
     float *dh = nullptr, *dh2 = nullptr, *du = nullptr, *dq = nullptr, *dz = nullptr, *dy = nullptr, *da = nullptr, *dbb = nullptr;
     float* dout = nullptr;               // gradient of the loss at the output, [B][nout][G][G]
     double* d_loss = nullptr;
@@ -111,12 +111,7 @@ atmwfs_status dalloc(atmwfs_fno* f, void** p, size_t bytes)
 // ---------------------------------------------------------------------------
 // elementwise kernels
 // ---------------------------------------------------------------------------
-// GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 x (1 + tanh(c (x + 0.044715 x^3))), c = sqrt(2 / pi)
-__device__ __forceinline__ float gelu_f(float x)
-{
-    const float c = 0.7978845608028654f;
-    return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
-}
+// GELU (gelu_f, fno_gemm.cuh) and its derivative
 __device__ __forceinline__ float gelu_d(float x)
 {
     const float c = 0.7978845608028654f;
@@ -345,9 +340,10 @@ unsigned grid_for(long n) { return (unsigned)std::min<long>((n + 255) / 256, 152
 // ---------------------------------------------------------------------------
 cudaError_t gemm(int M, int N, int K, const void* A, long lda, int ta, int abf, const void* B, long ldb, int tb,
                  int bbf, float* C, long ldc, float beta, int batch = 1, long sA = 0, long sB = 0, long sC = 0,
-                 const float* bias = nullptr, int bias_rows = 0, cudaStream_t st = 0)
+                 const float* bias = nullptr, int bias_rows = 0, cudaStream_t st = 0, float* C2 = nullptr)
 {
     GemmArgs g{};
+    g.C2 = C2;
     g.M = M; g.N = N; g.K = K;
     g.A = A; g.B = B; g.C = C;
     g.lda = lda; g.ldb = ldb; g.ldc = ldc;
@@ -357,11 +353,12 @@ cudaError_t gemm(int M, int N, int K, const void* A, long lda, int ta, int abf, 
     return gemm_launch(g, beta, st);
 }
 
-// Pointwise channel mixing per sample: C[b] (o x P) = W (o x c) X[b] (c x P) (+ row bias)
+// Pointwise channel mixing per sample: C[b] (o x P) = W (o x c) X[b] (c x P)
+// (+ row bias, + beta C); act, if given, receives gelu(C) in the same pass.
 cudaError_t pointwise(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                      const float* bias, cudaStream_t st)
+                      const float* bias, cudaStream_t st, float* act = nullptr)
 {
-    return gemm(o, (int)P, c, W, c, 0, 1, X, P, 0, 0, C, P, beta, B, 0, (long)c * P, (long)o * P, bias, 1, st);
+    return gemm(o, (int)P, c, W, c, 0, 1, X, P, 0, 0, C, P, beta, B, 0, (long)c * P, (long)o * P, bias, 1, st, act);
 }
 
 // dW (o x c) += sum_b dC[b] (o x P) X[b]^T
@@ -433,7 +430,7 @@ atmwfs_status ensure_batch(atmwfs_fno* f, int B)
     for (auto& p : f->u) drop(p);
     for (auto& p : f->a) drop(p);
     for (auto& p : f->z) drop(p);
-    for (float** p : {&f->y, &f->bb, &f->spec, &f->qpre, &f->q, &f->dh, &f->dh2, &f->du, &f->dq, &f->dz, &f->dy,
+    for (float** p : {&f->y, &f->bb, &f->qpre, &f->q, &f->dh, &f->dh2, &f->du, &f->dq, &f->dz, &f->dy,
                       &f->da, &f->dbb, &f->dout})
         drop(*p);
     const atmwfs_fno_cfg& c = f->cfg;
@@ -450,7 +447,6 @@ atmwfs_status ensure_batch(atmwfs_fno* f, int B)
     for (auto& p : f->z) FN_TRY(dalloc(f, (void**)&p, mod));
     FN_TRY(dalloc(f, (void**)&f->y, mod));
     FN_TRY(dalloc(f, (void**)&f->bb, spa));
-    FN_TRY(dalloc(f, (void**)&f->spec, act));
     FN_TRY(dalloc(f, (void**)&f->qpre, prj));
     FN_TRY(dalloc(f, (void**)&f->q, prj));
     FN_TRY(dalloc(f, (void**)&f->dh, act));
@@ -467,7 +463,7 @@ atmwfs_status ensure_batch(atmwfs_fno* f, int B)
 }
 
 // spectral convolution of layer l: spec = S_l(h)
-atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, int B, cudaStream_t st)
+atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, float* spec, int B, cudaStream_t st)
 {
     const atmwfs_fno_cfg& c = f->cfg;
     const int G = c.grid, m = c.modes, w = c.width;
@@ -496,7 +492,7 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, int B, cudaStre
     FN_CUDA(gemm(G, m, m, f->Gyr, m, 0, 0, f->y + (long)m * m, m, 0, 0, f->bb + m, 2 * m, 1.0f, (int)bc, 0, ys, bs,
                  nullptr, 0, st));
     // spec = bb Gx: [B w G, 2m] x [2m, G]
-    FN_CUDA(gemm((int)rows, G, 2 * m, f->bb, 2 * m, 0, 0, f->Gx, G, 0, 0, f->spec, G, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
+    FN_CUDA(gemm((int)rows, G, 2 * m, f->bb, 2 * m, 0, 0, f->Gx, G, 0, 0, spec, G, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
     return ATMWFS_OK;
 }
 
@@ -532,25 +528,26 @@ atmwfs_status spectral_bwd(atmwfs_fno* f, int l, const float* ds, float* dh, int
     return ATMWFS_OK;
 }
 
+// Input of the projection: the last Fourier layer's output, which has no
+// activation, so it is that layer's u.
+const float* last_h(const atmwfs_fno* f) { return f->u[f->cfg.layers - 1]; }
+
 atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st)
 {
     const atmwfs_fno_cfg& c = f->cfg;
     const long P = (long)c.grid * c.grid;
-    const long nact = (long)B * c.width * P;
     FN_TRY(ensure_batch(f, B));
     const __nv_bfloat16* pb = f->pbf;
     const float* pf = f->params;
     FN_CUDA(pointwise(pb + f->L.lift_W, c.width, c.nin, x, f->h[0], B, P, 0.0f, pf + f->L.lift_b, st));
     for (int l = 0; l < c.layers; l++) {
-        FN_TRY(spectral_fwd(f, l, f->h[l], B, st));
-        FN_CUDA(cudaMemcpyAsync(f->u[l], f->spec, sizeof(float) * nact, cudaMemcpyDeviceToDevice, st));
-        FN_CUDA(pointwise(pb + f->L.W[l], c.width, c.width, f->h[l], f->u[l], B, P, 1.0f, pf + f->L.b[l], st));
-        if (l + 1 < c.layers) k_gelu<<<grid_for(nact), 256, 0, st>>>(f->u[l], f->h[l + 1], nact);
-        else FN_CUDA(cudaMemcpyAsync(f->h[l + 1], f->u[l], sizeof(float) * nact, cudaMemcpyDeviceToDevice, st));
+        // u = S_l(h) + W_l h + b_l; h' = gelu(u) from the same epilogue
+        // (the last layer has no activation: its u is the projection's input)
+        FN_TRY(spectral_fwd(f, l, f->h[l], f->u[l], B, st));
+        FN_CUDA(pointwise(pb + f->L.W[l], c.width, c.width, f->h[l], f->u[l], B, P, 1.0f, pf + f->L.b[l], st,
+                          l + 1 < c.layers ? f->h[l + 1] : nullptr));
     }
-    const long nq = (long)B * c.proj * P;
-    FN_CUDA(pointwise(pb + f->L.proj1_W, c.proj, c.width, f->h[c.layers], f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st));
-    k_gelu<<<grid_for(nq), 256, 0, st>>>(f->qpre, f->q, nq);
+    FN_CUDA(pointwise(pb + f->L.proj1_W, c.proj, c.width, last_h(f), f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st, f->q));
     FN_CUDA(pointwise(pb + f->L.proj2_W, c.nout, c.proj, f->q, out, B, P, 0.0f, pf + f->L.proj2_b, st));
     return ATMWFS_OK;
 }
@@ -568,7 +565,7 @@ atmwfs_status backward(atmwfs_fno* f, const float* x, const float* dout, int B, 
     k_rowsum<<<dim3(rs.x, c.nout), 256, 0, st>>>(dout, g + f->L.proj2_b, B, c.nout, P);
     FN_CUDA(pointwise_dx(pb + f->L.proj2_W, c.nout, c.proj, dout, f->dq, B, P, 0.0f, st));
     k_gelu_bwd<<<grid_for(nq), 256, 0, st>>>(f->dq, f->qpre, f->dq, nq);
-    FN_CUDA(pointwise_dw(c.proj, c.width, f->dq, f->h[c.layers], g + f->L.proj1_W, B, P, st));
+    FN_CUDA(pointwise_dw(c.proj, c.width, f->dq, last_h(f), g + f->L.proj1_W, B, P, st));
     k_rowsum<<<dim3(rs.x, c.proj), 256, 0, st>>>(f->dq, g + f->L.proj1_b, B, c.proj, P);
     FN_CUDA(pointwise_dx(pb + f->L.proj1_W, c.proj, c.width, f->dq, f->dh, B, P, 0.0f, st));
     // Fourier layers, last to first: dh holds dL/dh[l+1]

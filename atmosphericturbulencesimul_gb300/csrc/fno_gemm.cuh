@@ -30,7 +30,15 @@ struct GemmArgs {
     int bias_rows;        // 1: bias[m] per row, else bias[n] per column
     int splitk;           // K ranges over grid.z % splitk
     int batch;
+    float* C2;            // optional: gelu of the final C value, same layout (not with shared accumulation)
 };
+
+// GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 x (1 + tanh(c (x + 0.044715 x^3))), c = sqrt(2 / pi)
+__device__ __forceinline__ float gelu_f(float x)
+{
+    const float c = 0.7978845608028654f;
+    return 0.5f * x * (1.0f + tanhf(c * (x + 0.044715f * x * x * x)));
+}
 
 namespace gemm {
 
@@ -218,23 +226,72 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
                     mma_bf16(acc[i][j], af[i][0], af[i][1], af[i][2], af[i][3], bfr[j][0], bfr[j][1]);
         }
     }
-    // epilogue: C (already scaled by beta) += alpha * acc (+ bias once)
+    // epilogue.  Each thread owns pairs of adjacent columns (n, n + 1) in
+    // rows m and m + 8 of its m16 x n8 tiles.  With a private C, the old
+    // values the beta term needs are all loaded before the first store, and
+    // pairs move as float2 when the row stride and base allow.
+    const bool shared = g.splitk > 1 || (g.batch > 1 && g.sC == 0);
+    const bool v2 = !shared && (g.ldc % 2 == 0) && ((reinterpret_cast<uintptr_t>(Cb) & 7) == 0);
+    float2 old[S::TM][S::TN][2];
+    if (!shared && g.beta != 0.0f) {
+#pragma unroll
+        for (int i = 0; i < S::TM; i++)
+#pragma unroll
+            for (int j = 0; j < S::TN; j++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + 8 * h;
+                    const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq;
+                    float2 o = make_float2(0.0f, 0.0f);
+                    if (m < g.M) {
+                        const float* c = Cb + (size_t)m * g.ldc + n;
+                        if (v2 && n + 1 < g.N) o = *reinterpret_cast<const float2*>(c);
+                        else {
+                            if (n < g.N) o.x = c[0];
+                            if (n + 1 < g.N) o.y = c[1];
+                        }
+                    }
+                    old[i][j][h] = o;
+                }
+    }
 #pragma unroll
     for (int i = 0; i < S::TM; i++)
 #pragma unroll
         for (int j = 0; j < S::TN; j++)
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + (q >= 2 ? 8 : 0);
-                const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq + (q & 1);
+            for (int h = 0; h < 2; h++) {
+                const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + 8 * h;
+                const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq;
                 if (m >= g.M || n >= g.N) continue;
-                float v = g.alpha * acc[i][j][q];
-                if (g.bias && sk == 0 && (bz == 0 || g.sC != 0)) v += g.bias_rows ? g.bias[m] : g.bias[n];
+                float v0 = g.alpha * acc[i][j][2 * h], v1 = g.alpha * acc[i][j][2 * h + 1];
+                if (g.bias && sk == 0 && (bz == 0 || g.sC != 0)) {
+                    v0 += g.bias_rows ? g.bias[m] : g.bias[n];
+                    if (n + 1 < g.N) v1 += g.bias_rows ? g.bias[m] : g.bias[n + 1];
+                }
                 float* c = Cb + (size_t)m * g.ldc + n;
-                // split K, or a batch summed into one C: several CTAs add here
-                // (gemm_launch scaled C by beta beforehand)
-                if (g.splitk > 1 || (g.batch > 1 && g.sC == 0)) atomicAdd(c, v);
-                else *c = g.beta == 0.0f ? v : fmaf(g.beta, *c, v);
+                if (shared) {
+                    // split K, or a batch summed into one C: several CTAs add
+                    // here (gemm_launch scaled C by beta beforehand)
+                    atomicAdd(c, v0);
+                    if (n + 1 < g.N) atomicAdd(c + 1, v1);
+                    continue;
+                }
+                if (g.beta != 0.0f) {
+                    v0 = fmaf(g.beta, old[i][j][h].x, v0);
+                    v1 = fmaf(g.beta, old[i][j][h].y, v1);
+                }
+                float* c2 = g.C2 ? g.C2 + (size_t)bz * g.sC + (size_t)m * g.ldc + n : nullptr;
+                if (v2 && n + 1 < g.N) {
+                    *reinterpret_cast<float2*>(c) = make_float2(v0, v1);
+                    if (c2) *reinterpret_cast<float2*>(c2) = make_float2(gelu_f(v0), gelu_f(v1));
+                } else {
+                    c[0] = v0;
+                    if (c2) c2[0] = gelu_f(v0);
+                    if (n + 1 < g.N) {
+                        c[1] = v1;
+                        if (c2) c2[1] = gelu_f(v1);
+                    }
+                }
             }
 }
 

@@ -162,3 +162,63 @@ def cube_name(prefix: str, tspan: int, slambda_m: float, kind: str) -> str:
 
 __all__ = ["conf_read", "conf_exists", "load_conf", "read_profile", "make_hv_profile", "fits_write", "fits_read", "ShmImage",
            "shm_semwait", "mkwfs", "cube_name"]
+
+
+def table_model(Ntab: np.ndarray, Ktab: np.ndarray | None, dh: float):
+    """N(alt, lam) and K(alt, lam) callables reading tables at altitudes
+    k * dh with the reference's interpolation (AtmosphereModel.c:3240-3250)."""
+    n = len(Ntab)
+
+    def pos(alt):
+        a = float(np.float32(alt))      # the model's float argument, divided in double
+        i = int(a / dh)
+        if i > n - 3:
+            i = n - 2
+        i = max(i, 0)
+        f = float(np.float32(a / dh - i))
+        return i, min(max(f, 0.0), 1.0)
+
+    def N(alt, lam):
+        i, f = pos(alt)
+        return float(np.float32((1.0 - f) * float(Ntab[i]) + f * float(Ntab[i + 1])))
+
+    def K(alt, lam):
+        if Ktab is None:
+            return 0.0
+        i, f = pos(alt)
+        return (1.0 - f) * float(Ktab[i]) + f * float(Ktab[i + 1])
+
+    return N, K
+
+
+def refraction_path(lam: float, zangle: float, site_alt: float, refractivity, absorption=None,
+                    path_file=None) -> tuple[float, float]:
+    """AtmosphereModel_RefractionPath on the host with model callables
+    refractivity(alt, lam) -> N and absorption(alt, lam) -> 1/m:
+    (refraction [arcsec], transmission)."""
+    lib = _lib.load()
+    ncb = _lib.REFRACTIVITY_FN(lambda a, l, u: float(refractivity(a, l)))
+    kcb = _lib.ABSORPTION_FN(lambda a, l, u: float(absorption(a, l))) if absorption else _lib.ABSORPTION_FN()
+    r, t = C.c_double(), C.c_double()
+    _lib.check(lib.atmwfs_refraction_path(lam, zangle, site_alt, ncb, kcb, None,
+                                          os.fsencode(path_file) if path_file else None, C.byref(r), C.byref(t)))
+    return r.value, t.value
+
+
+def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: np.ndarray | None, dh: float):
+    """Refraction [arcsec] and transmission of every (wavelength, zenith
+    angle) pair, one GPU thread per ray; Ntab[i] / Ktab[i] tabulate the model
+    of wavelength i at altitudes k * dh.  Returns two [nlambda, nzangle] arrays."""
+    lib = _lib.load()
+    lam = np.ascontiguousarray(lambdas, np.float64)
+    za = np.ascontiguousarray(zangles, np.float64)
+    N = np.ascontiguousarray(Ntab, np.float32).reshape(len(lam), -1)
+    K = None if Ktab is None else np.ascontiguousarray(Ktab, np.float64).reshape(len(lam), -1)
+    r = np.empty((len(lam), len(za)))
+    t = np.empty_like(r)
+    dp = C.POINTER(C.c_double)
+    _lib.check(lib.atmwfs_refraction_table(lam.ctypes.data_as(dp), len(lam), za.ctypes.data_as(dp), len(za), site_alt,
+                                           N.ctypes.data_as(C.POINTER(C.c_float)),
+                                           None if K is None else K.ctypes.data_as(dp), N.shape[1], dh,
+                                           r.ctypes.data_as(dp), t.ctypes.data_as(dp)))
+    return r, t

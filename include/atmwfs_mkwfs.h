@@ -191,6 +191,41 @@ typedef struct atmwfs_mkwfs_opts {
  * reduction either way).  opts may be NULL. */
 atmwfs_status atmwfs_mkwfs(const char* conf_file, float slambda_um, long precision, const atmwfs_mkwfs_opts* opts);
 
+/* ------------------------------------------------------------------ */
+/* Atmospheric refraction                                              */
+/* ------------------------------------------------------------------ */
+
+/* Absorption coefficient [1/m] of air at altitude alt [m] and wavelength
+ * lambda [m]: the value the reference's AtmosphereModel_stdAtmModel_N
+ * leaves in v_ABSCOEFF (AtmosphereModel.c:3210, 3293). */
+typedef double (*atmwfs_absorption_fn)(float alt, float lambda, void* user);
+
+/* Replaces AtmosphereModel_RefractionPath (AtmosphereModel.c:4215-4291):
+ * traces a ray from the site altitude upward in 20 m steps over a
+ * spherical Earth (R = 6371 km) with Snell's law between consecutive steps,
+ * until 99 km, and iterates the launch angle (at most 20 times, until the
+ * exit angle matches zangle to 1e-5 arcsec).  Returns the refraction
+ * [arcsec] and the transmission of the last pass (absorption NULL: 1).
+ * path_file (may be NULL) receives the reference's refractpath.txt lines
+ * of the last pass.  N and K receive the same float arguments as the
+ * reference's model calls.  A ray that has not reached 99 km after 10^6
+ * steps is ATMWFS_ERR_INVALID. */
+atmwfs_status atmwfs_refraction_path(double lambda, double zangle, double site_alt, atmwfs_refractivity_fn N,
+                                     atmwfs_absorption_fn K, void* user, const char* path_file,
+                                     double* refraction_arcsec, double* transmission);
+
+/* The same for every (wavelength, zenith angle) pair on the GPU, one ray
+ * per thread in FP64, from tabulated models: Ntab[i][k] and Ktab[i][k]
+ * (Ktab may be NULL) are N and the absorption coefficient of wavelength i
+ * at altitude k * dh, k < ntab, read with the reference's interpolation
+ * (index (long)(alt / dh), float fraction clamped to [0, 1], the last
+ * interval repeated above the table, as stdAtmModel_N reads its 10 m
+ * density tables, AtmosphereModel.c:3240-3250).  Outputs
+ * [nlambda][nzangle]; host buffers. */
+atmwfs_status atmwfs_refraction_table(const double* lambdas, long nlambda, const double* zangles, long nzangle,
+                                      double site_alt, const float* Ntab, const double* Ktab, long ntab, double dh,
+                                      double* refraction_arcsec, double* transmission);
+
 #ifdef __cplusplus
 }
 #endif

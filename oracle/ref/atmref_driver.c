@@ -34,6 +34,13 @@
  *       gauss_filter(in, 3, 10) (written out), center_PSF, measure_FWHM on
  *       the filtered image, measure_enc_NRJ(in, 0.5); one line
  *       "MEAS <xc> <yc> <fwhm> <ee50>".
+ *   atmref refract <conf> <lambda_model> <lambda> <zangle> <writepath>
+ *       AtmosphereModel_RefractionPath (src/AtmosphereModel/AtmosphereModel.c:4215);
+ *       one line "REFR <refraction arcsec> <v_TRANSM> <SiteAlt>"; writepath 1
+ *       leaves refractpath.txt in the current directory.
+ *   atmref ntable <conf> <lambda_model> <lambda> <dh> <n> <out.bin>
+ *       AtmosphereModel_stdAtmModel_N at altitudes k * dh, k < n: n floats
+ *       (N) then n doubles (v_ABSCOEFF after each call).
  *   atmref roffset <conf> <lambda_model> <lambda_ref> <slambda> <zangle> <alt>...
  *       the per-layer refraction offset RoffsetS - Roffset [m] that
  *       make_AtmosphericTurbulence_wavefront_series adds to the start row
@@ -224,6 +231,40 @@ static int cmd_measure(int argc, char **argv)
     return write_raw(argv[4], "PSFg", n);
 }
 
+extern double v_TRANSM, v_ABSCOEFF;
+
+static int cmd_refract(int argc, char **argv)
+{
+    if (argc < 7) return 2;
+    AtmosphereModel_Create_from_CONF(argv[2], (float)atof(argv[3]));
+    const double r = AtmosphereModel_RefractionPath(atof(argv[4]), atof(argv[5]), atoi(argv[6]));
+    printf("\nREFR %.17g %.17g %.9g\n", r, v_TRANSM, (double)SiteAlt);
+    return 0;
+}
+
+static int cmd_ntable(int argc, char **argv)
+{
+    if (argc < 8) return 2;
+    AtmosphereModel_Create_from_CONF(argv[2], (float)atof(argv[3]));
+    const float lam = (float)atof(argv[4]);
+    const double dh = atof(argv[5]);
+    const long n = atol(argv[6]);
+    float *N = (float *)malloc(sizeof(float) * n);
+    double *K = (double *)malloc(sizeof(double) * n);
+    for (long k = 0; k < n; k++) {
+        N[k] = AtmosphereModel_stdAtmModel_N((float)(k * dh), lam, 0);
+        K[k] = v_ABSCOEFF;
+    }
+    FILE *f = fopen(argv[7], "wb");
+    if (!f) return 4;
+    fwrite(N, sizeof(float), (size_t)n, f);
+    fwrite(K, sizeof(double), (size_t)n, f);
+    fclose(f);
+    free(N);
+    free(K);
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
     if (argc < 2) {
@@ -241,6 +282,8 @@ int main(int argc, char **argv)
     if (strcmp(argv[1], "conf") == 0) return cmd_conf(argc, argv);
     if (strcmp(argv[1], "expo") == 0 && argc >= 4) return measure_wavefront_series_expoframes((float)atof(argv[2]), argv[3]);
     if (strcmp(argv[1], "chromat") == 0) return cmd_chromat(argc, argv);
+    if (strcmp(argv[1], "refract") == 0) return cmd_refract(argc, argv);
+    if (strcmp(argv[1], "ntable") == 0) return cmd_ntable(argc, argv);
     if (strcmp(argv[1], "measure") == 0) return cmd_measure(argc, argv);
     if (strcmp(argv[1], "hv") == 0 && argc >= 7)
         return AtmosphericTurbulence_makeHV_CN2prof(atof(argv[2]), atof(argv[3]), atof(argv[4]), atol(argv[5]), argv[6]);

@@ -16,10 +16,14 @@ sources by oracle/ref/build_ref.py) on small seeded cases.
   psf.npz      the PSF consumers: measure_wavefront_series_expoframes
                (AtmosphericTurbulence.c:6592), PSF_makeChromatPSF
                (psf.c:54) and the image measures of the exposure loop.
+  refract.npz  AtmosphereModel_RefractionPath (AtmosphereModel.c:4215) with
+               the reference's atmosphere model, and that model's N and
+               absorption at the 10 m nodes of its density tables.
 
 Run from the repository root where the reference is mounted:
     python tests/golden/make_golden.py          (every fixture)
     python tests/golden/make_golden.py psf      (psf.npz only)
+    python tests/golden/make_golden.py refract  (refract.npz only)
 """
 from __future__ import annotations
 
@@ -328,6 +332,35 @@ def make_psf() -> dict:
     return out
 
 
+# (lambda, zenith angle, site altitude): refraction ray traces
+REFRACT_CASES = [(0.55e-6, 0.5, 0.0), (1.6e-6, 1.0, 4200.0), (0.4e-6, 1.2, 0.0)]
+REFRACT_DH, REFRACT_N = 10.0, 10001
+
+
+def make_refract() -> dict:
+    """AtmosphereModel_RefractionPath with the reference's atmosphere model,
+    and that model's N and absorption at the nodes of its 10 m density
+    tables (what a caller's table model reproduces), plus the path file of
+    the first case."""
+    out = {}
+    with tempfile.TemporaryDirectory() as td:
+        d = Path(td)
+        for k, (lam, za, site) in enumerate(REFRACT_CASES):
+            conf = re.sub(r"^SITE_ALT\s+\S+", f"SITE_ALT {site:.1f}", conf_text(MKWFS_CASES["mkwfs"]), flags=re.M)
+            (d / "WFsim.conf").write_text(conf)
+            txt = run([str(ATMREF), "refract", "WFsim.conf", repr(lam), repr(lam), repr(za), "1" if k == 0 else "0"], td)
+            r, tr, sa = [float(v) for v in next(l for l in txt.splitlines() if l.startswith("REFR")).split()[1:]]
+            if k == 0:   # before the next model set-up renames the file
+                out["path0"] = np.array((d / "refractpath.txt").read_text())
+            run([str(ATMREF), "ntable", "WFsim.conf", repr(lam), repr(lam), repr(REFRACT_DH), str(REFRACT_N), "t.bin"], td)
+            raw = (d / "t.bin").read_bytes()
+            out[f"N{k}"] = np.frombuffer(raw[:4 * REFRACT_N], np.float32).copy()
+            out[f"K{k}"] = np.frombuffer(raw[4 * REFRACT_N:], np.float64).copy()
+            out[f"case{k}"] = np.array([lam, za, sa, r, tr])
+    out["table"] = np.array([REFRACT_DH, REFRACT_N])
+    return out
+
+
 def main():
     if not ATMREF.exists():
         sys.path.insert(0, str(ROOT / "oracle" / "ref"))
@@ -337,10 +370,15 @@ def main():
         np.savez_compressed(HERE / "psf.npz", **make_psf())
         print("wrote psf.npz")
         return
+    if sys.argv[1:] == ["refract"]:
+        np.savez_compressed(HERE / "refract.npz", **make_refract())
+        print("wrote refract.npz")
+        return
     (HERE / "conf.json").write_text(json.dumps(make_conf(), indent=1) + "\n")
     (HERE / "hv.json").write_text(json.dumps(make_hv(), indent=1) + "\n")
     np.savez_compressed(HERE / "fresnel.npz", **make_fresnel())
     np.savez_compressed(HERE / "psf.npz", **make_psf())
+    np.savez_compressed(HERE / "refract.npz", **make_refract())
     for name, case in MKWFS_CASES.items():
         np.savez_compressed(HERE / f"{name}.npz", **make_mkwfs(case))
     print("wrote", ", ".join(["conf.json", "hv.json", "fresnel.npz"] + [f"{n}.npz" for n in MKWFS_CASES]))
