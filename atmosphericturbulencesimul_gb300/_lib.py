@@ -176,6 +176,8 @@ SIGNATURES = [
                                          C.c_void_p, C.c_char_p, _dp, _dp]),
     ("atmwfs_refraction_table", C.c_int, [_dp, C.c_long, _dp, C.c_long, C.c_double, _fp, _dp, C.c_long, C.c_double,
                                           _dp, _dp]),
+    ("atmwfs_refraction_table_host", C.c_int, [_dp, C.c_long, _dp, C.c_long, C.c_double, _fp, _dp, C.c_long,
+                                               C.c_double, C.c_int, _dp, _dp]),
     ("atmwfs_windows_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_void_p]),
     ("atmwfs_advance", C.c_int, [_ctx, C.c_long]),
     # include/atmwfs_fno.h

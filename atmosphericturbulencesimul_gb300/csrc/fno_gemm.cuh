@@ -104,7 +104,7 @@ __device__ __forceinline__ uint2 pack4(float4 v)
 }
 
 template <int BM, int BN>
-__global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
+__global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
 {
     using S = Shape<BM, BN>;
     constexpr int NA = BM * BK / 1024, NB = BN * BK / 1024;  // 4-element groups per thread
@@ -228,34 +228,50 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
     }
     // epilogue.  Each thread owns pairs of adjacent columns (n, n + 1) in
     // rows m and m + 8 of its m16 x n8 tiles.  With a private C, the old
-    // values the beta term needs are all loaded before the first store, and
-    // pairs move as float2 when the row stride and base allow.
+    // values the beta term needs are loaded for a whole row group of tiles
+    // before its first store (so the loads overlap), and pairs move as float2
+    // when the row stride and base allow.
     const bool shared = g.splitk > 1 || (g.batch > 1 && g.sC == 0);
     const bool v2 = !shared && (g.ldc % 2 == 0) && ((reinterpret_cast<uintptr_t>(Cb) & 7) == 0);
-    float2 old[S::TM][S::TN][2];
-    if (!shared && g.beta != 0.0f) {
+    const bool loadc = !shared && g.beta != 0.0f;
+    if (!shared && !loadc && !g.C2) {
+        // plain store (beta 0, no activation): element by element measured
+        // faster than the paired form for the wide-N, short-K products
 #pragma unroll
         for (int i = 0; i < S::TM; i++)
 #pragma unroll
             for (int j = 0; j < S::TN; j++)
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + 8 * h;
-                    const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq;
-                    float2 o = make_float2(0.0f, 0.0f);
-                    if (m < g.M) {
-                        const float* c = Cb + (size_t)m * g.ldc + n;
-                        if (v2 && n + 1 < g.N) o = *reinterpret_cast<const float2*>(c);
-                        else {
-                            if (n < g.N) o.x = c[0];
-                            if (n + 1 < g.N) o.y = c[1];
-                        }
-                    }
-                    old[i][j][h] = o;
+                for (int q = 0; q < 4; q++) {
+                    const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + (q >= 2 ? 8 : 0);
+                    const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq + (q & 1);
+                    if (m >= g.M || n >= g.N) continue;
+                    float v = g.alpha * acc[i][j][q];
+                    if (g.bias && sk == 0) v += g.bias_rows ? g.bias[m] : g.bias[n];
+                    Cb[(size_t)m * g.ldc + n] = v;
                 }
+        return;
     }
 #pragma unroll
-    for (int i = 0; i < S::TM; i++)
+    for (int i = 0; i < S::TM; i++) {
+        float2 old[S::TN][2];
+#pragma unroll
+        for (int j = 0; j < S::TN; j++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + 8 * h;
+                const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq;
+                float2 o = make_float2(0.0f, 0.0f);
+                if (loadc && m < g.M) {
+                    const float* c = Cb + (size_t)m * g.ldc + n;
+                    if (v2 && n + 1 < g.N) o = *reinterpret_cast<const float2*>(c);
+                    else {
+                        if (n < g.N) o.x = c[0];
+                        if (n + 1 < g.N) o.y = c[1];
+                    }
+                }
+                old[j][h] = o;
+            }
 #pragma unroll
         for (int j = 0; j < S::TN; j++)
 #pragma unroll
@@ -276,9 +292,9 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
                     if (n + 1 < g.N) atomicAdd(c + 1, v1);
                     continue;
                 }
-                if (g.beta != 0.0f) {
-                    v0 = fmaf(g.beta, old[i][j][h].x, v0);
-                    v1 = fmaf(g.beta, old[i][j][h].y, v1);
+                if (loadc) {
+                    v0 = fmaf(g.beta, old[j][h].x, v0);
+                    v1 = fmaf(g.beta, old[j][h].y, v1);
                 }
                 float* c2 = g.C2 ? g.C2 + (size_t)bz * g.sC + (size_t)m * g.ldc + n : nullptr;
                 if (v2 && n + 1 < g.N) {
@@ -293,6 +309,7 @@ __global__ void __launch_bounds__(256) k_gemm(const GemmArgs g)
                     }
                 }
             }
+    }
 }
 
 }  // namespace gemm

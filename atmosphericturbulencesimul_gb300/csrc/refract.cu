@@ -13,8 +13,11 @@
 // thread in FP64 for every (wavelength, zenith angle) pair of a table
 // model.  The path geometry needs FP64: the altitude is the difference of
 // two numbers near the Earth radius.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -227,8 +230,10 @@ atmwfs_status atmwfs_refraction_table(const double* lambdas, long nlambda, const
          (!Ktab || cu(cudaMemcpy(dK, Ktab, sizeof(double) * nlambda * ntab, cudaMemcpyHostToDevice))) &&
          cu(cudaMemset(dbad, 0, sizeof(int)));
     if (ok) {
-        k_refraction<<<(unsigned)((nr + 127) / 128), 128>>>(dl, (int)nlambda, dz, (int)nzangle, site_alt, dN, dK, ntab, dh,
-                                                             dr, dt, dbad);
+        // one warp per block: FP64 throughput per SM is low on this part, so
+        // the rays are spread over as many SMs as there are warps of rays
+        k_refraction<<<(unsigned)((nr + 31) / 32), 32>>>(dl, (int)nlambda, dz, (int)nzangle, site_alt, dN, dK, ntab, dh,
+                                                           dr, dt, dbad);
         ok = cu(cudaGetLastError()) &&
              cu(cudaMemcpy(refraction_arcsec, dr, sizeof(double) * nr, cudaMemcpyDeviceToHost)) &&
              cu(cudaMemcpy(tr.data(), dt, sizeof(double) * nr, cudaMemcpyDeviceToHost)) &&
@@ -239,6 +244,37 @@ atmwfs_status atmwfs_refraction_table(const double* lambdas, long nlambda, const
     if (bad) return fail(ATMWFS_ERR_INVALID, "refraction_table: a ray does not reach 99 km");
     if (transmission)
         for (long i = 0; i < nr; i++) transmission[i] = tr[i];
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_refraction_table_host(const double* lambdas, long nlambda, const double* zangles, long nzangle,
+                                           double site_alt, const float* Ntab, const double* Ktab, long ntab, double dh,
+                                           int threads, double* refraction_arcsec, double* transmission)
+{
+    if (!lambdas || !zangles || !Ntab || !refraction_arcsec || nlambda < 1 || nzangle < 1 || ntab < 3 || !(dh > 0))
+        return fail(ATMWFS_ERR_INVALID, "refraction_table_host: bad arguments");
+    for (long z = 0; z < nzangle; z++)
+        if (!(zangles[z] >= 0.0 && zangles[z] < 0.5 * kPi))
+            return fail(ATMWFS_ERR_INVALID, "refraction_table_host: zenith angle out of [0, pi/2)");
+    const long nr = nlambda * nzangle;
+    const int nt = std::max(1, std::min<int>(threads > 0 ? threads : (int)std::thread::hardware_concurrency(), (int)nr));
+    std::atomic<long> next(0);
+    std::atomic<int> bad(0);
+    auto work = [&]() {
+        for (long t; (t = next.fetch_add(1)) < nr;) {
+            const long li = t / nzangle, zi = t % nzangle;
+            const TableModel m{Ntab + (size_t)li * ntab, Ktab ? Ktab + (size_t)li * ntab : nullptr, ntab, dh};
+            const Ray r = trace(lambdas[li], zangles[zi], site_alt, m, nullptr);
+            refraction_arcsec[t] = r.refraction_arcsec;
+            if (transmission) transmission[t] = r.transmission;
+            if (!r.ok) bad = 1;
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int i = 1; i < nt; i++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    if (bad) return fail(ATMWFS_ERR_INVALID, "refraction_table_host: a ray does not reach 99 km");
     return ATMWFS_OK;
 }
 

@@ -280,6 +280,27 @@ def frame_flops(cfg: FnoConfig) -> float:
     return f
 
 
+def frame_bytes(cfg: FnoConfig) -> float:
+    """HBM bytes one inference frame moves in the library's dataflow (FP32
+    activations, each product reading its operands and writing its result
+    once, the residual add and the activation in the pointwise epilogue):
+    the algorithmic figure of the surrogate's HBM roofline."""
+    G, m, w, P = cfg.grid, cfg.modes, cfg.width, cfg.grid * cfg.grid
+    spec_rows = 4.0 * w * G * 2 * m           # one x-DFT image (2m columns per row)
+    modes = 4.0 * w * 2 * m * m               # one mode image (complex m x m per channel)
+    b = 4.0 * cfg.nin * P + 4.0 * w * P       # lift
+    per_layer = (4.0 * w * P + spec_rows      # h -> a
+                 + spec_rows + modes          # a -> z
+                 + 2 * modes                  # z -> y (mode mixing)
+                 + modes + spec_rows          # y -> bb
+                 + spec_rows + 4.0 * w * P    # bb -> u
+                 + 4 * 4.0 * w * P)           # pointwise: read h, u; write u, gelu(u)
+    b += cfg.layers * per_layer
+    b += 4.0 * w * P + 2 * 4.0 * cfg.proj * P  # projection 1 (+ gelu)
+    b += 4.0 * cfg.proj * P + 4.0 * cfg.nout * P
+    return b
+
+
 def main(argv=None) -> int:
     """Train the surrogate on plain-path pairs and report its error on held-out seeds.
 

@@ -205,10 +205,12 @@ def refraction_path(lam: float, zangle: float, site_alt: float, refractivity, ab
     return r.value, t.value
 
 
-def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: np.ndarray | None, dh: float):
+def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: np.ndarray | None, dh: float,
+                     host_threads: int | None = None):
     """Refraction [arcsec] and transmission of every (wavelength, zenith
-    angle) pair, one GPU thread per ray; Ntab[i] / Ktab[i] tabulate the model
-    of wavelength i at altitudes k * dh.  Returns two [nlambda, nzangle] arrays."""
+    angle) pair, one GPU thread per ray (or host_threads CPU threads, 0 =
+    all); Ntab[i] / Ktab[i] tabulate the model of wavelength i at altitudes
+    k * dh.  Returns two [nlambda, nzangle] arrays."""
     lib = _lib.load()
     lam = np.ascontiguousarray(lambdas, np.float64)
     za = np.ascontiguousarray(zangles, np.float64)
@@ -217,8 +219,10 @@ def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: 
     r = np.empty((len(lam), len(za)))
     t = np.empty_like(r)
     dp = C.POINTER(C.c_double)
-    _lib.check(lib.atmwfs_refraction_table(lam.ctypes.data_as(dp), len(lam), za.ctypes.data_as(dp), len(za), site_alt,
-                                           N.ctypes.data_as(C.POINTER(C.c_float)),
-                                           None if K is None else K.ctypes.data_as(dp), N.shape[1], dh,
-                                           r.ctypes.data_as(dp), t.ctypes.data_as(dp)))
+    args = (lam.ctypes.data_as(dp), len(lam), za.ctypes.data_as(dp), len(za), site_alt,
+            N.ctypes.data_as(C.POINTER(C.c_float)), None if K is None else K.ctypes.data_as(dp), N.shape[1], dh)
+    if host_threads is None:
+        _lib.check(lib.atmwfs_refraction_table(*args, r.ctypes.data_as(dp), t.ctypes.data_as(dp)))
+    else:
+        _lib.check(lib.atmwfs_refraction_table_host(*args, int(host_threads), r.ctypes.data_as(dp), t.ctypes.data_as(dp)))
     return r, t

@@ -192,9 +192,16 @@ def surrogate_section(pairs: int = 4096) -> dict:
     plain_fps = 20 * test.count / (e0.elapsed_time(e1) * 1e-3)
     pk = peaks()
     tflops = F.frame_flops(model.cfg) * fps / 1e12
-    roof = {"bound": "tensor", "achieved": round(tflops, 2), "peak": pk.get("bf16_tflops"), "unit": "TFLOP/s",
-            "frac": round(tflops / pk["bf16_tflops"], 4) if pk.get("bf16_tflops") else None,
-            "flops_per_frame": F.frame_flops(model.cfg), "peak_source": pk["source"]}
+    gbs = F.frame_bytes(model.cfg) * fps / 1e9
+    # the products are thin (K or N of 64..256 against 65536 pixels): their
+    # arithmetic intensity is far below the BF16 ridge, so HBM bounds them
+    roof = {"bound": "hbm", "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": round(gbs / pk["hbm_gbs"], 4), "bytes_per_frame": F.frame_bytes(model.cfg),
+            "tensor": {"achieved": round(tflops, 2), "peak": pk.get("bf16_tflops"), "unit": "TFLOP/s",
+                       "frac": round(tflops / pk["bf16_tflops"], 4) if pk.get("bf16_tflops") else None,
+                       "flops_per_frame": F.frame_flops(model.cfg)},
+            "intensity_flop_per_byte": round(F.frame_flops(model.cfg) / F.frame_bytes(model.cfg), 1),
+            "peak_source": pk["source"]}
     res = {"value": round(fps, 1), "unit": "frames/s", "grid": 256, "batch": 16, "ms_per_batch": round(ms, 3),
            "model": {k: v for k, v in model.cfg.__dict__.items()}, "params": model.num_params, "weights": "bf16 (fp32 master)",
            "how": how, "setup_s": round(t_train, 1), "roofline": roof, "plain_same_grid_fps": round(plain_fps, 1),
@@ -206,6 +213,87 @@ def surrogate_section(pairs: int = 4096) -> dict:
         src.close()
     model.close()
     return res
+
+
+def rows_section() -> dict:
+    """The rows around the series, each timed on resident data with CUDA
+    events after warm-up: exposure PSFs (W = 512 frames into 1024^2 PSFs),
+    the 8192^2 2-D transform behind large master screens, and refraction ray
+    traces (GPU table form against the host trace)."""
+    import torch
+    from atmosphericturbulencesimul_gb300 import _lib, psf as P
+    from atmosphericturbulencesimul_gb300.mkwfs import refraction_table
+    lib = _lib.load()
+    pk = peaks()
+    out = {}
+    ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    # exposure PSFs: 64 frames per call, amplitude = one pupil
+    W, nf = 512, 64
+    g = torch.Generator(device="cuda").manual_seed(3)
+    pha = torch.randn((nf, W, W), device="cuda", generator=g)
+    amp = torch.ones((W, W), device="cuda")
+    acc = torch.zeros((2 * W, 2 * W), device="cuda")
+    for _ in range(3):
+        P.expo_accumulate_dev(pha, amp, acc)
+    e0, e1 = ev()
+    torch.cuda.synchronize()
+    e0.record()
+    reps = 10
+    for _ in range(reps):
+        P.expo_accumulate_dev(pha, amp, acc)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    N = 2 * W
+    batch = max(1, min(64, (256 << 20) // (N * N * 8)))
+    bpf = 4.0 * W * W + 2 * 16.0 * W * W + 2 * 4.0 * N * N / batch    # phase in, intermediate out + in, accumulator
+    gbs = bpf * nf / (ms * 1e-3) / 1e9
+    out["psf_expo"] = {"value": round(nf / (ms * 1e-3), 1), "unit": "frames/s", "frame": f"{W}^2 -> {N}^2 PSF",
+                       "ms_per_call": round(ms, 4), "frames_per_call": nf,
+                       "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                    "frac": round(gbs / pk["hbm_gbs"], 4), "bytes_per_frame": bpf}}
+    del pha, acc
+    # 8192^2 complex transform (master screens of that size)
+    M = 8192
+    a = torch.randn((M, M, 2), device="cuda")
+    b = torch.empty_like(a)
+    for _ in range(2):
+        _lib.check(lib.atmwfs_fft2d_dev(a.data_ptr(), b.data_ptr(), M, -1, None))
+    e0, e1 = ev()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(5):
+        _lib.check(lib.atmwfs_fft2d_dev(a.data_ptr(), b.data_ptr(), M, -1, None))
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 5
+    byt = 4 * 2 * 8.0 * M * M
+    out["fft2d_8192"] = {"value": round(ms, 3), "unit": "ms", "higher_is_better": False,
+                         "roofline": {"bound": "hbm", "achieved": round(byt / (ms * 1e-3) / 1e9, 1),
+                                      "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                      "frac": round(byt / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 4), "bytes": byt,
+                                      "note": "rows, transpose, rows, transpose: four read+write passes"}}
+    del a, b
+    # refraction: 16 wavelengths x 64 zenith angles on the GPU, one ray on the host
+    alt = np.arange(10001) * 10.0
+    lams = 0.4e-6 * (2.4 / 0.4) ** (np.arange(16) / 15.0)
+    Ntab = np.stack([(2.7e-4 * (1 + 0.0056 / (l * 1e6) ** 2) * np.exp(-alt / 8000.0)).astype(np.float32) for l in lams])
+    za = np.linspace(0.0, np.deg2rad(75.0), 64)
+    refraction_table(lams[:1], za[:1], 0.0, Ntab[:1], None, 10.0)
+    t0 = time.perf_counter()
+    refraction_table(lams, za, 0.0, Ntab, None, 10.0)
+    t_gpu = time.perf_counter() - t0
+    threads = os.cpu_count() or 1
+    sub = slice(0, 16, 4)                    # a 4 x 64 sample on the host
+    t0 = time.perf_counter()
+    refraction_table(lams[sub], za, 0.0, Ntab[sub], None, 10.0, host_threads=threads)
+    t_host = time.perf_counter() - t0
+    out["refraction"] = {"value": round(len(lams) * len(za) / t_gpu, 1), "unit": "rays/s",
+                         "rays": len(lams) * len(za),
+                         "cpu": {"value": round(4 * len(za) / t_host, 1), "unit": "rays/s", "cores": threads,
+                                 "sample": "4 wavelengths x 64 zenith angles, the same table model"},
+                         "note": "FP64 traces, wall time of the call; one ray per GPU thread (one warp per block)"}
+    return out
 
 
 def cpu_screens(wl: dict, threads: int):
@@ -272,9 +360,14 @@ def main():
     ap.add_argument("--surrogate-only", action="store_true",
                     help="time only the surrogate section (profiling); prints its JSON object")
     ap.add_argument("--surrogate-pairs", type=int, default=4096, help="training pairs of the surrogate section")
+    ap.add_argument("--no-rows", action="store_true", help="skip the PSF / large-transform / refraction section")
+    ap.add_argument("--rows-only", action="store_true", help="time only that section (profiling)")
     args = ap.parse_args()
     if args.surrogate_only:
         print(json.dumps(surrogate_section(args.surrogate_pairs)))
+        return
+    if args.rows_only:
+        print(json.dumps(rows_section()))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -408,6 +501,8 @@ def main():
     s.close()
     if rank == 0 and not args.no_surrogate:
         line["surrogate"] = surrogate_section(args.surrogate_pairs)
+    if rank == 0 and world == 1 and not args.no_rows:
+        line["rows"] = rows_section()
     if rank == 0:
         print(json.dumps(line))
     if dist:

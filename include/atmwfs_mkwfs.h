@@ -226,6 +226,13 @@ atmwfs_status atmwfs_refraction_table(const double* lambdas, long nlambda, const
                                       double site_alt, const float* Ntab, const double* Ktab, long ntab, double dh,
                                       double* refraction_arcsec, double* transmission);
 
+/* The same table model traced on the host, `threads` threads (<= 0: all
+ * hardware threads): for hosts that keep the trace on the CPU, and the CPU
+ * side of a comparison with the GPU form. */
+atmwfs_status atmwfs_refraction_table_host(const double* lambdas, long nlambda, const double* zangles, long nzangle,
+                                           double site_alt, const float* Ntab, const double* Ktab, long ntab, double dh,
+                                           int threads, double* refraction_arcsec, double* transmission);
+
 #ifdef __cplusplus
 }
 #endif

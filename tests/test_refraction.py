@@ -74,3 +74,13 @@ def test_absorption_and_errors(lib):
     assert 0.9 < t < 1.0
     with pytest.raises(_lib.AtmwfsError):
         refraction_path(0.7e-6, np.pi / 2, 0.0, N)
+
+
+def test_host_table_form_matches_reference(lib):
+    """atmwfs_refraction_table_host: the table model traced on host threads."""
+    from atmosphericturbulencesimul_gb300.mkwfs import refraction_table
+    for k in range(3):
+        lam, za, site, ref, tr = G[f"case{k}"]
+        r, t = refraction_table([lam], [za, 0.2], site, G[f"N{k}"][None], G[f"K{k}"][None], DH, host_threads=2)
+        assert abs(r[0, 0] - ref) < 1e-4 and abs(t[0, 0] - tr) < 1e-12
+        assert 0 < r[0, 1] < r[0, 0]
