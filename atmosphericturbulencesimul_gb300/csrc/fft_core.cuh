@@ -66,20 +66,6 @@ AW_HD float2 tw_const(float2 d, int k, int n)
     return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
 }
 
-// d * exp(ds 2 pi i k / n) with the direction ds = -1 (forward) or +1
-// (inverse) known only at run time: one code copy serves both directions.
-AW_HD float2 tw_rt(float2 d, int k, int n, float ds)
-{
-    if (k == 0) return d;
-    const int j = k * (32 / n);
-    if (j == 16) return make_float2(-d.x, -d.y);
-    if (j == 8) return make_float2(-ds * d.y, ds * d.x);
-    if (j == 24) return make_float2(ds * d.y, -ds * d.x);
-    const float c = cos32(j);
-    const float s = ds * sin32(j);
-    return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
-}
-
 template <int R>
 AW_HD constexpr int brev(int i)
 {
@@ -103,28 +89,6 @@ AW_HD void dft(float2* v)
                 const float2 a = v[base + k], b = v[base + k + span];
                 v[base + k] = cadd(a, b);
                 v[base + k + span] = tw_const<D>(csub(a, b), k, 2 * span);
-            }
-        }
-    }
-    float2 t[R];
-    AW_UNROLL
-    for (int i = 0; i < R; i++) t[i] = v[i];
-    AW_UNROLL
-    for (int i = 0; i < R; i++) v[i] = t[brev<R>(i)];
-}
-
-template <int R>
-AW_HD void dft_rt(float2* v, float ds)
-{
-    AW_UNROLL
-    for (int span = R / 2; span >= 1; span >>= 1) {
-        AW_UNROLL
-        for (int base = 0; base < R; base += 2 * span) {
-            AW_UNROLL
-            for (int k = 0; k < span; k++) {
-                const float2 a = v[base + k], b = v[base + k + span];
-                v[base + k] = cadd(a, b);
-                v[base + k + span] = tw_rt(csub(a, b), k, 2 * span, ds);
             }
         }
     }
@@ -199,31 +163,37 @@ AW_HD void stage_store(const float2* v, float2* buf, int t)
     }
 }
 
-// The same with the stride NS and the direction known at run time (ns is a
-// power of two): the stage loop below runs every stage of every transform
-// through one copy of the code of each radix.
+// The same with the stride NS known at run time (ns is a power of two): the
+// stage loop below runs every stage of every transform through one copy of
+// the code of each radix.  The stages are always forward (compile-time
+// butterfly constants, the +-i rotations free); an inverse transform is the
+// conjugate of the forward transform of the conjugate.
 // tws: the stage's twiddle table tws[r * ns + k] = exp(-2 pi i k r / (ns R))
 // (see tw_offset), read with consecutive k across a warp.
 template <int N, int T, int E, int R>
-AW_HD void stage_twiddle_rt(float2* v, int t, const float2* tws, int ns, float ds)
+AW_HD void stage_twiddle_rt(float2* v, int t, const float2* tws, int ns)
 {
     if (ns == 1) return;
     AW_UNROLL
     for (int w = 0; w < E / R; w++) {
         const int k = (t + T * w) & (ns - 1);
         AW_UNROLL
-        for (int r = 1; r < R; r++) {
-            const float2 w0 = tws[r * ns + k];
-            v[w * R + r] = cmul(v[w * R + r], make_float2(w0.x, -ds * w0.y));
-        }
+        for (int r = 1; r < R; r++) v[w * R + r] = cmul(v[w * R + r], tws[r * ns + k]);
     }
 }
 
 template <int E, int R>
-AW_HD void stage_dft_rt(float2* v, float ds)
+AW_HD void stage_dft_rt(float2* v)
 {
     AW_UNROLL
-    for (int w = 0; w < E / R; w++) dft_rt<R>(v + w * R, ds);
+    for (int w = 0; w < E / R; w++) dft<R, -1>(v + w * R);
+}
+
+template <int E>
+AW_HD void conj_all(float2* v)
+{
+    AW_UNROLL
+    for (int e = 0; e < E; e++) v[e].y = -v[e].y;
 }
 
 template <int N, int T, int E, int R>
@@ -346,11 +316,11 @@ inline void build_twiddles(float2* out)
 // Stage body (twiddles + butterflies) of radix r and stride ns for one
 // thread; a uniform branch selects the code of the radix.
 template <int N, int T, int E>
-AW_HD void stage_compute(float2* v, int t, const float2* tw, int r, int ns, float ds)
+AW_HD void stage_compute(float2* v, int t, const float2* tw, int r, int ns)
 {
-    if constexpr (has_radix<N>(32)) if (r == 32) { stage_twiddle_rt<N, T, E, 32>(v, t, tw, ns, ds); stage_dft_rt<E, 32>(v, ds); return; }
-    if constexpr (has_radix<N>(16)) if (r == 16) { stage_twiddle_rt<N, T, E, 16>(v, t, tw, ns, ds); stage_dft_rt<E, 16>(v, ds); return; }
-    if constexpr (has_radix<N>(8)) if (r == 8) { stage_twiddle_rt<N, T, E, 8>(v, t, tw, ns, ds); stage_dft_rt<E, 8>(v, ds); return; }
+    if constexpr (has_radix<N>(32)) if (r == 32) { stage_twiddle_rt<N, T, E, 32>(v, t, tw, ns); stage_dft_rt<E, 32>(v); return; }
+    if constexpr (has_radix<N>(16)) if (r == 16) { stage_twiddle_rt<N, T, E, 16>(v, t, tw, ns); stage_dft_rt<E, 16>(v); return; }
+    if constexpr (has_radix<N>(8)) if (r == 8) { stage_twiddle_rt<N, T, E, 8>(v, t, tw, ns); stage_dft_rt<E, 8>(v); return; }
 }
 
 template <int N, int T, int E>

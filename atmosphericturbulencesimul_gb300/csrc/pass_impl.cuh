@@ -185,6 +185,7 @@ __device__ __forceinline__ void prop_row(float2* v, float2* xrow, int t, const f
 template <int N, int T, int E>
 __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev)
 {
+    if (ds > 0.0f) conj_all<E>(v);     // inverse = conj(forward(conj))
     int ns = 1, rp = 0, nsp = 1;
 #pragma unroll 1
     for (int st = 0; st < Stages<N>::S; st++) {
@@ -195,11 +196,12 @@ __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const flo
             row_sync<T>();
             stage_exchange_load<N, T, E>(v, xrow, t, r);
         }
-        stage_compute<N, T, E>(v, t, tw + tw_offset<N>(rev, st), r, ns, ds);
+        stage_compute<N, T, E>(v, t, tw + tw_offset<N>(rev, st), r, ns);
         rp = r;
         nsp = ns;
         ns *= r;
     }
+    if (ds > 0.0f) conj_all<E>(v);
 }
 
 // 1-D Fresnel propagation (forward FFT, transfer table, inverse FFT) with a
@@ -209,14 +211,20 @@ __device__ __forceinline__ void prop_row_rt(float2* v, float2* xrow, int t, cons
                                             const float2* __restrict__ h)
 {
     constexpr int RL = last_radix<N>();
+    // IFFT(H FFT(x)) = conj(FFT(conj(H FFT(x)))): the first conjugation is
+    // folded into the transfer multiply, both transforms run the forward code
 #pragma unroll 1
     for (int dir = 0; dir < 2; dir++) {
-        fft_rt<N, T, E>(v, xrow, t, tw, dir ? 1.0f : -1.0f, dir);
+        fft_rt<N, T, E>(v, xrow, t, tw, -1.0f, dir);
         if (dir == 0) {
 #pragma unroll
-            for (int s = 0; s < E; s++) v[s] = cmul(v[s], __ldg(h + last_index<N, T, RL>(t, s)));
+            for (int s = 0; s < E; s++) {
+                const float2 a = v[s], b = __ldg(h + last_index<N, T, RL>(t, s));
+                v[s] = make_float2(a.x * b.x - a.y * b.y, -(a.x * b.y + a.y * b.x));
+            }
         }
     }
+    conj_all<E>(v);
 }
 
 // Nearest integer to (hi + lo) / 2 pi, halves rounded up, with the

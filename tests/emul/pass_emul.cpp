@@ -32,6 +32,8 @@ static double urand()
 template <int N, int T, int E>
 void emu_fft_rt(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw, float ds, int rev)
 {
+    if (ds > 0.0f)
+        for (int t = 0; t < T; t++) conj_all<E>(V[t].data());
     int ns = 1, rp = 0, nsp = 1;
     for (int st = 0; st < Stages<N>::S; st++) {
         const int r = stage_radix<N>(st, rev);
@@ -39,11 +41,13 @@ void emu_fft_rt(std::vector<std::array<float2, E>>& V, float2* buf, const float2
             for (int t = 0; t < T; t++) stage_exchange_store<N, T, E>(V[t].data(), buf, t, rp, nsp);
             for (int t = 0; t < T; t++) stage_exchange_load<N, T, E>(V[t].data(), buf, t, r);
         }
-        for (int t = 0; t < T; t++) stage_compute<N, T, E>(V[t].data(), t, tw + tw_offset<N>(rev, st), r, ns, ds);
+        for (int t = 0; t < T; t++) stage_compute<N, T, E>(V[t].data(), t, tw + tw_offset<N>(rev, st), r, ns);
         rp = r;
         nsp = ns;
         ns *= r;
     }
+    if (ds > 0.0f)
+        for (int t = 0; t < T; t++) conj_all<E>(V[t].data());
 }
 
 static std::vector<cd> dft(const std::vector<cd>& x, int sign)
