@@ -182,10 +182,36 @@ __device__ __forceinline__ void prop_row(float2* v, float2* xrow, int t, const f
 // forward, +1 inverse; rev walks the radix sequence backwards (the inverse of
 // a propagation, which starts from the forward's register layout and ends in
 // the natural layout x[t + e T]).
+// Two-stage plans (N <= 1024) with the radices, strides and exchange
+// indices known at compile time: stage A (stride 1, no twiddles), the
+// exchange, stage B (stride RA).
+template <int N, int T, int E, int RA, int RB>
+__device__ __forceinline__ void fft2_ct(float2* v, float2* xrow, int t, const float2* __restrict__ tws1)
+{
+    stage_dft<E, RA, -1>(v);
+    row_sync<T>();
+    stage_store<N, T, E, RA, 1>(v, xrow, t);
+    row_sync<T>();
+    stage_load<N, T, E, RB>(v, xrow, t);
+    stage_twiddle_rt<N, T, E, RB>(v, t, tws1, RA);
+    stage_dft<E, RB, -1>(v);
+}
+
 template <int N, int T, int E>
 __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev)
 {
     if (ds > 0.0f) conj_all<E>(v);     // inverse = conj(forward(conj))
+    if constexpr (Stages<N>::S == 2) {
+        constexpr int R0 = Stages<N>::R0, R1 = Stages<N>::R1;
+        if constexpr (R0 == R1) {
+            fft2_ct<N, T, E, R0, R1>(v, xrow, t, tw + tw_offset<N>(rev, 1));
+        } else {
+            if (rev) fft2_ct<N, T, E, R1, R0>(v, xrow, t, tw + tw_offset<N>(1, 1));
+            else fft2_ct<N, T, E, R0, R1>(v, xrow, t, tw + tw_offset<N>(0, 1));
+        }
+        if (ds > 0.0f) conj_all<E>(v);
+        return;
+    }
     int ns = 1, rp = 0, nsp = 1;
 #pragma unroll 1
     for (int st = 0; st < Stages<N>::S; st++) {

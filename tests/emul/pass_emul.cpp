@@ -29,11 +29,32 @@ static double urand()
 
 // The kernel's runtime stage loop, one thread after the other (the
 // __syncthreads of the device loop separate the per-thread sweeps).
+// The two-stage compile-time plan (fft2_ct), one thread after the other.
+template <int N, int T, int E, int RA, int RB>
+void emu_fft2_ct(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tws1)
+{
+    for (int t = 0; t < T; t++) stage_dft<E, RA, -1>(V[t].data());
+    for (int t = 0; t < T; t++) stage_store<N, T, E, RA, 1>(V[t].data(), buf, t);
+    for (int t = 0; t < T; t++) {
+        stage_load<N, T, E, RB>(V[t].data(), buf, t);
+        stage_twiddle_rt<N, T, E, RB>(V[t].data(), t, tws1, RA);
+        stage_dft<E, RB, -1>(V[t].data());
+    }
+}
+
 template <int N, int T, int E>
 void emu_fft_rt(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw, float ds, int rev)
 {
     if (ds > 0.0f)
         for (int t = 0; t < T; t++) conj_all<E>(V[t].data());
+    if constexpr (Stages<N>::S == 2) {
+        constexpr int R0 = Stages<N>::R0, R1 = Stages<N>::R1;
+        if (rev) emu_fft2_ct<N, T, E, R1, R0>(V, buf, tw + tw_offset<N>(1, 1));
+        else emu_fft2_ct<N, T, E, R0, R1>(V, buf, tw + tw_offset<N>(0, 1));
+        if (ds > 0.0f)
+            for (int t = 0; t < T; t++) conj_all<E>(V[t].data());
+        return;
+    }
     int ns = 1, rp = 0, nsp = 1;
     for (int st = 0; st < Stages<N>::S; st++) {
         const int r = stage_radix<N>(st, rev);
