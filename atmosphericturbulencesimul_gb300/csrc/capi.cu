@@ -107,6 +107,8 @@ static std::vector<float2> host_twiddles(int N)
         case 512: h.resize(tw_total<512>()); build_twiddles<512>(h.data()); break;
         case 1024: h.resize(tw_total<1024>()); build_twiddles<1024>(h.data()); break;
         case 2048: h.resize(tw_total<2048>()); build_twiddles<2048>(h.data()); break;
+        case 4096: h.resize(tw_total<4096>()); build_twiddles<4096>(h.data()); break;
+        case 8192: h.resize(tw_total<8192>()); build_twiddles<8192>(h.data()); break;
         default: break;
     }
     return h;

@@ -224,6 +224,8 @@ template <> struct Plan<256>  { static constexpr int E = 16, T = 16; };
 template <> struct Plan<512>  { static constexpr int E = 32, T = 16; };
 template <> struct Plan<1024> { static constexpr int E = 32, T = 32; };
 template <> struct Plan<2048> { static constexpr int E = 32, T = 64; };
+template <> struct Plan<4096> { static constexpr int E = 16, T = 256; };
+template <> struct Plan<8192> { static constexpr int E = 32, T = 256; };
 
 template <int... Rs> struct Radices {};
 
@@ -252,6 +254,9 @@ template <> struct Stages<256>  { static constexpr int S = 2, R0 = 16, R1 = 16, 
 template <> struct Stages<512>  { static constexpr int S = 2, R0 = 32, R1 = 16, R2 = 0; };
 template <> struct Stages<1024> { static constexpr int S = 2, R0 = 32, R1 = 32, R2 = 0; };
 template <> struct Stages<2048> { static constexpr int S = 3, R0 = 32, R1 = 8, R2 = 8; };
+// whole-row plans of the large 2-D transforms (one CTA of 256 threads per row)
+template <> struct Stages<4096> { static constexpr int S = 3, R0 = 16, R1 = 16, R2 = 16; };
+template <> struct Stages<8192> { static constexpr int S = 3, R0 = 32, R1 = 16, R2 = 16; };
 
 template <int N>
 AW_HD constexpr bool has_radix(int r)

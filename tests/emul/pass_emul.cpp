@@ -216,6 +216,8 @@ int main()
     check_fft<512>();
     check_fft<1024>();
     check_fft<2048>();
+    check_fft<4096>();   // whole-row plans of the large 2-D transforms
+    check_fft<8192>();
     const int M = 512;
     for (int orient = 0; orient < 2; orient++) {
         check_gather<64>(M, 0, 0, 0.25f, 0.75f, orient, 32);

@@ -22,7 +22,7 @@ def emul_output(tmp_path_factory):
     return dict((l.split()[0], float(l.split()[1])) for l in out.strip().splitlines())
 
 
-@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048])
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048, 4096, 8192])
 def test_fft_stages(emul_output, n):
     assert emul_output[f"fftfwd_{n}"] < 5e-7
     assert emul_output[f"fftinv_{n}"] < 5e-7
