@@ -109,11 +109,14 @@ __constant__ Sweep c_sweeps[12] = {
 
 __device__ __forceinline__ float vote_acc(float ch, double c) { return __double2float_rn((double)ch + c); }
 
-__device__ float bin_votes(const float* pb, int nb, int bx, int by)
+// ppf[i] = (double)pb[i] + pi rounded toward -inf to float: for a float x,
+// x > (double)pb[i] + pi  <=>  x > ppf[i], so the reference's double
+// comparisons run as float comparisons with identical outcomes.
+__device__ float bin_votes(const float* pb, const float* ppf, int nb, int bx, int by)
 {
-    const double kPi = 3.14159265358979323846;
     float ch = 0.0f;
-    const double pv = (double)pb[by * nb + bx];
+    const float pv = pb[by * nb + bx];
+    const float pvp = ppf[by * nb + bx];
     for (int s = 0; s < 12; s++) {
         const Sweep w = c_sweeps[s];
         // role A: this bin is index1, partner index2 = (bx + dx, by + dy)
@@ -126,14 +129,14 @@ __device__ float bin_votes(const float* pb, int nb, int bx, int by)
         for (int k = 0; k < 2; k++) {
             const bool doA = (k == 0) == a_first;
             if (doA && va) {
-                const double pv2 = (double)pb[ay * nb + ax];
-                if (pv2 > pv + kPi) ch = vote_acc(ch, w.c);
-                if (pv > pv2 + kPi) ch = vote_acc(ch, -w.c);
+                const int j = ay * nb + ax;
+                if (pb[j] > pvp) ch = vote_acc(ch, w.c);          // pv2 > pv + pi
+                if (pv > ppf[j]) ch = vote_acc(ch, -w.c);         // pv > pv2 + pi
             }
             if (!doA && vb) {
-                const double pv1 = (double)pb[byp * nb + bxp];
-                if (pv > pv1 + kPi) ch = vote_acc(ch, -w.c);
-                if (pv1 > pv + kPi) ch = vote_acc(ch, w.c);
+                const int j = byp * nb + bxp;
+                if (pv > ppf[j]) ch = vote_acc(ch, -w.c);         // pv > pv1 + pi
+                if (pb[j] > pvp) ch = vote_acc(ch, w.c);          // pv1 > pv + pi
             }
         }
     }
@@ -150,6 +153,7 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
     extern __shared__ float sh[];
     float* pb = sh;
     float* ch = sh + n;
+    float* ppf = sh + 2 * n;
     __shared__ unsigned s_max;
     __shared__ int s_cnt;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -164,27 +168,38 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
     const double kTwoPi = 2.0 * 3.14159265358979323846;
     while (plim > 0.51 && chiter < 1000 && chcnt0cnt < 5) {
         chiter++;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) ppf[i] = __double2float_rd((double)pb[i] + kTwoPi * 0.5);
+        __syncthreads();
+        unsigned umax = 0u;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const float c = bin_votes(pb, nb, i % nb, i / nb);
+            const float c = bin_votes(pb, ppf, nb, i % nb, i / nb);
             ch[i] = c;
-            atomicMax(&s_max, __float_as_uint(fabsf(c)));
+            umax = max(umax, __float_as_uint(fabsf(c)));
         }
+        // one shared atomic per warp (max is order-free)
+        umax = __reduce_max_sync(0xffffffffu, umax);
+        if ((threadIdx.x & 31) == 0) atomicMax(&s_max, umax);
         __syncthreads();
         plim = (double)__uint_as_float(s_max) - 0.001;
         if (plim < 0.5) plim = 0.5;
+        // for a float c: c > plim <=> c > rd(plim) (rd: round toward -inf to float)
+        const float plimf = __double2float_rd(plim);
+        int cnt = 0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int bx = i % nb, by = i / nb;
             const bool interior = bx > 1 && by > 1 && bx < nb - 2 && by < nb - 2;
-            const double c = (double)ch[i];
-            if (c > plim) {
-                if (interior) atomicAdd(&s_cnt, 1);
+            const float c = ch[i];
+            if (c > plimf) {
+                if (interior) cnt++;
                 pb[i] = (float)((double)pb[i] + kTwoPi);
             }
-            if (c < -plim) {
-                if (interior) atomicAdd(&s_cnt, 1);
+            if (c < -plimf) {
+                if (interior) cnt++;
                 pb[i] = (float)((double)pb[i] - kTwoPi);
             }
         }
+        cnt = __reduce_add_sync(0xffffffffu, cnt);
+        if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_cnt, cnt);
         __syncthreads();
         const int chcnt = s_cnt;
         __syncthreads();
@@ -201,7 +216,7 @@ cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int max
                         cudaStream_t st)
 {
     if (nsci <= 0) return cudaSuccess;
-    const size_t sm = (size_t)2 * maxnb * maxnb * sizeof(float);
+    const size_t sm = (size_t)3 * maxnb * maxnb * sizeof(float);
     if (sm > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_unwrap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
