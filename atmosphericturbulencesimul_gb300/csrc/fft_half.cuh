@@ -30,19 +30,23 @@ __device__ __forceinline__ void row_sync()
 
 __device__ __forceinline__ __half2 hcmul(__half2 a, __half2 b) { return __hcmadd(a, b, __float2half2_rn(0.0f)); }
 
-// d * exp(ds 2 pi i k / n) for k < n <= 32
-__device__ __forceinline__ __half2 tw_rt_h(__half2 d, int k, int n, float ds)
+// d * exp(-2 pi i k / n) for a compile-time (after unrolling) k < n <= 32:
+// every stage runs forward; an inverse transform is the conjugate of the
+// forward transform of the conjugate.
+__device__ __forceinline__ __half2 tw_fwd_h(__half2 d, int k, int n)
 {
     if (k == 0) return d;
     const int j = k * (32 / n);
     if (j == 16) return __hneg2(d);
-    if (j == 8) return __hmul2(__lowhigh2highlow(d), __floats2half2_rn(-ds, ds));  // (x, y) -> (-ds y, ds x)
-    if (j == 24) return __hmul2(__lowhigh2highlow(d), __floats2half2_rn(ds, -ds));
-    return hcmul(d, __floats2half2_rn(cos32(j), ds * sin32(j)));
+    if (j == 8) return __hmul2(__lowhigh2highlow(d), __floats2half2_rn(1.0f, -1.0f));   // (x, y) -> (y, -x)
+    if (j == 24) return __hmul2(__lowhigh2highlow(d), __floats2half2_rn(-1.0f, 1.0f));  // (x, y) -> (-y, x)
+    return hcmul(d, __floats2half2_rn(cos32(j), -sin32(j)));
 }
 
+__device__ __forceinline__ __half2 hconj(__half2 v) { return __hmul2(v, __floats2half2_rn(1.0f, -1.0f)); }
+
 template <int R>
-__device__ __forceinline__ void dft_rt_h(__half2* v, float ds)
+__device__ __forceinline__ void dft_fwd_h(__half2* v)
 {
 #pragma unroll
     for (int span = R / 2; span >= 1; span >>= 1) {
@@ -52,7 +56,7 @@ __device__ __forceinline__ void dft_rt_h(__half2* v, float ds)
             for (int k = 0; k < span; k++) {
                 const __half2 a = v[base + k], b = v[base + k + span];
                 v[base + k] = __hadd2(a, b);
-                v[base + k + span] = tw_rt_h(__hsub2(a, b), k, 2 * span, ds);
+                v[base + k + span] = tw_fwd_h(__hsub2(a, b), k, 2 * span);
             }
         }
     }
@@ -63,21 +67,21 @@ __device__ __forceinline__ void dft_rt_h(__half2* v, float ds)
     for (int i = 0; i < R; i++) v[i] = t[brev<R>(i)];
 }
 
+// One forward stage: stage twiddles, butterflies, and the 1 / R scaling of
+// the forward transforms of a propagation.
 template <int N, int T, int E, int R>
-__device__ __forceinline__ void stage_h(__half2* v, int t, const __half2* __restrict__ tws, int ns, float ds,
-                                        bool scale)
+__device__ __forceinline__ void stage_h(__half2* v, int t, const __half2* __restrict__ tws, int ns, bool scale)
 {
     if (ns > 1) {
-        const __half2 cj = __floats2half2_rn(1.0f, -ds);  // conjugate the table for the inverse
 #pragma unroll
         for (int w = 0; w < E / R; w++) {
             const int k = (t + T * w) & (ns - 1);
 #pragma unroll
-            for (int r = 1; r < R; r++) v[w * R + r] = hcmul(v[w * R + r], __hmul2(tws[r * ns + k], cj));
+            for (int r = 1; r < R; r++) v[w * R + r] = hcmul(v[w * R + r], tws[r * ns + k]);
         }
     }
 #pragma unroll
-    for (int w = 0; w < E / R; w++) dft_rt_h<R>(v + w * R, ds);
+    for (int w = 0; w < E / R; w++) dft_fwd_h<R>(v + w * R);
     if (scale) {
         const __half2 s = __float2half2_rn(1.0f / R);
 #pragma unroll
@@ -86,11 +90,11 @@ __device__ __forceinline__ void stage_h(__half2* v, int t, const __half2* __rest
 }
 
 template <int N, int T, int E>
-__device__ __forceinline__ void stage_compute_h(__half2* v, int t, const __half2* tw, int r, int ns, float ds, bool scale)
+__device__ __forceinline__ void stage_compute_h(__half2* v, int t, const __half2* tw, int r, int ns, bool scale)
 {
-    if constexpr (has_radix<N>(32)) if (r == 32) { stage_h<N, T, E, 32>(v, t, tw, ns, ds, scale); return; }
-    if constexpr (has_radix<N>(16)) if (r == 16) { stage_h<N, T, E, 16>(v, t, tw, ns, ds, scale); return; }
-    if constexpr (has_radix<N>(8)) if (r == 8) { stage_h<N, T, E, 8>(v, t, tw, ns, ds, scale); return; }
+    if constexpr (has_radix<N>(32)) if (r == 32) { stage_h<N, T, E, 32>(v, t, tw, ns, scale); return; }
+    if constexpr (has_radix<N>(16)) if (r == 16) { stage_h<N, T, E, 16>(v, t, tw, ns, scale); return; }
+    if constexpr (has_radix<N>(8)) if (r == 8) { stage_h<N, T, E, 8>(v, t, tw, ns, scale); return; }
 }
 
 template <int N, int T, int E, int R>
@@ -128,13 +132,36 @@ __device__ __forceinline__ void exchange_h(__half2* v, __half2* buf, int t, int 
     if constexpr (has_radix<N>(8)) if (r == 8) load_h<N, T, E, 8>(v, buf, t);
 }
 
-// One transform of the row in FP16; forward stages scaled by 1 / radix.
-template <int N, int T, int E>
-__device__ __forceinline__ void fft_rt_h(__half2* v, __half2* xrow, int t, const __half2* __restrict__ tw, float ds,
-                                         int rev)
+// Two-stage plans with compile-time radices, strides and exchange indices.
+template <int N, int T, int E, int RA, int RB>
+__device__ __forceinline__ void fft2_ct_h(__half2* v, __half2* xrow, int t, const __half2* __restrict__ tws1,
+                                          bool scale)
 {
+    stage_h<N, T, E, RA>(v, t, nullptr, 1, scale);
+    row_sync<T>();
+    store_h<N, T, E, RA>(v, xrow, t, 1);
+    row_sync<T>();
+    load_h<N, T, E, RB>(v, xrow, t);
+    stage_h<N, T, E, RB>(v, t, tws1, RA, scale);
+}
+
+// One transform of the row in FP16, all stages forward; `scale` applies
+// 1 / radix per stage (the forward transform of a propagation).
+template <int N, int T, int E>
+__device__ __forceinline__ void fft_fwd_h(__half2* v, __half2* xrow, int t, const __half2* __restrict__ tw, int rev,
+                                          bool scale)
+{
+    if constexpr (Stages<N>::S == 2) {
+        constexpr int R0 = Stages<N>::R0, R1 = Stages<N>::R1;
+        if constexpr (R0 == R1) {
+            fft2_ct_h<N, T, E, R0, R1>(v, xrow, t, tw + tw_offset<N>(rev, 1), scale);
+        } else {
+            if (rev) fft2_ct_h<N, T, E, R1, R0>(v, xrow, t, tw + tw_offset<N>(1, 1), scale);
+            else fft2_ct_h<N, T, E, R0, R1>(v, xrow, t, tw + tw_offset<N>(0, 1), scale);
+        }
+        return;
+    }
     int ns = 1, rp = 0, nsp = 1;
-    const bool scale = ds < 0.0f;
 #pragma unroll 1
     for (int st = 0; st < Stages<N>::S; st++) {
         const int r = stage_radix<N>(st, rev);
@@ -142,7 +169,7 @@ __device__ __forceinline__ void fft_rt_h(__half2* v, __half2* xrow, int t, const
             row_sync<T>();
             exchange_h<N, T, E>(v, xrow, t, rp, nsp, r);
         }
-        stage_compute_h<N, T, E>(v, t, tw + tw_offset<N>(rev, st), r, ns, ds, scale);
+        stage_compute_h<N, T, E>(v, t, tw + tw_offset<N>(rev, st), r, ns, scale);
         rp = r;
         nsp = ns;
         ns *= r;
@@ -151,6 +178,8 @@ __device__ __forceinline__ void fft_rt_h(__half2* v, __half2* xrow, int t, const
 
 // 1-D Fresnel propagation of the row with FP16 transforms: the FP32 values
 // are rounded once on entry and widened once on exit; h is N H in FP16.
+// IFFT(H FFT(x)) = conj(FFT(conj(H FFT(x)))), the inner conjugation folded
+// into the transfer multiply, the outer one into the widening.
 template <int N, int T, int E>
 __device__ __forceinline__ void prop_row_h(float2* v, float2* xrow, int t, const __half2* __restrict__ tw,
                                            const __half2* __restrict__ h)
@@ -160,12 +189,15 @@ __device__ __forceinline__ void prop_row_h(float2* v, float2* xrow, int t, const
 #pragma unroll
     for (int e = 0; e < E; e++) u[e] = __floats2half2_rn(v[e].x, v[e].y);
     __half2* xr = reinterpret_cast<__half2*>(xrow);
-    fft_rt_h<N, T, E>(u, xr, t, tw, -1.0f, 0);
+    fft_fwd_h<N, T, E>(u, xr, t, tw, 0, true);
 #pragma unroll
-    for (int s = 0; s < E; s++) u[s] = hcmul(u[s], h[last_index<N, T, RL>(t, s)]);
-    fft_rt_h<N, T, E>(u, xr, t, tw, 1.0f, 1);
+    for (int s = 0; s < E; s++) u[s] = hconj(hcmul(u[s], h[last_index<N, T, RL>(t, s)]));
+    fft_fwd_h<N, T, E>(u, xr, t, tw, 1, false);
 #pragma unroll
-    for (int e = 0; e < E; e++) v[e] = __half22float2(u[e]);
+    for (int e = 0; e < E; e++) {
+        const float2 f = __half22float2(u[e]);
+        v[e] = make_float2(f.x, -f.y);
+    }
 }
 
 }  // namespace atmwfs
