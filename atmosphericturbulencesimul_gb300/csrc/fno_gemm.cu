@@ -24,6 +24,20 @@ __global__ void k_scale_rows(float* C, long ldc, long sC, int M, int N, float be
 
 }  // namespace
 
+template <int BM, int BN>
+cudaError_t launch_tile(dim3 grid, const GemmArgs& g, cudaStream_t st)
+{
+    constexpr size_t sm = gemm::stage_bytes(BM, BN);
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(gemm::k_gemm<BM, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    gemm::k_gemm<BM, BN><<<grid, 256, sm, st>>>(g);
+    return cudaGetLastError();
+}
+
 cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
 {
     GemmArgs g = g0;
@@ -49,11 +63,10 @@ cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
     }
     if (g.K <= 0) return cudaSuccess;
     const dim3 grid((unsigned)((g.M + BM - 1) / BM), (unsigned)((g.N + BN - 1) / BN), (unsigned)(g.batch * g.splitk));
-    if (bm128 && bn128) gemm::k_gemm<128, 128><<<grid, 256, 0, st>>>(g);
-    else if (!bm128 && bn128) gemm::k_gemm<64, 128><<<grid, 256, 0, st>>>(g);
-    else if (bm128 && !bn128) gemm::k_gemm<128, 64><<<grid, 256, 0, st>>>(g);
-    else gemm::k_gemm<64, 64><<<grid, 256, 0, st>>>(g);
-    return cudaGetLastError();
+    if (bm128 && bn128) return launch_tile<128, 128>(grid, g, st);
+    if (!bm128 && bn128) return launch_tile<64, 128>(grid, g, st);
+    if (bm128 && !bn128) return launch_tile<128, 64>(grid, g, st);
+    return launch_tile<64, 64>(grid, g, st);
 }
 
 }  // namespace atmwfs

@@ -226,17 +226,13 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
                     mma_bf16(acc[i][j], af[i][0], af[i][1], af[i][2], af[i][3], bfr[j][0], bfr[j][1]);
         }
     }
-    // epilogue.  Each thread owns pairs of adjacent columns (n, n + 1) in
-    // rows m and m + 8 of its m16 x n8 tiles.  With a private C, the old
-    // values the beta term needs are loaded for a whole row group of tiles
-    // before its first store (so the loads overlap), and pairs move as float2
-    // when the row stride and base allow.
+    // epilogue.  A private C (no split K, no batch summed into one C) goes
+    // through a shared-memory stage so that C, its beta term and the
+    // activation move as whole 16-byte vectors along rows; a shared C takes
+    // atomics from the fragments (gemm_launch scaled it by beta beforehand).
     const bool shared = g.splitk > 1 || (g.batch > 1 && g.sC == 0);
-    const bool v2 = !shared && (g.ldc % 2 == 0) && ((reinterpret_cast<uintptr_t>(Cb) & 7) == 0);
-    const bool loadc = !shared && g.beta != 0.0f;
-    if (!shared && !loadc && !g.C2) {
-        // plain store (beta 0, no activation): element by element measured
-        // faster than the paired form for the wide-N, short-K products
+    const bool add_bias = g.bias && sk == 0 && (bz == 0 || g.sC != 0);
+    if (shared) {
 #pragma unroll
         for (int i = 0; i < S::TM; i++)
 #pragma unroll
@@ -247,70 +243,66 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
                     const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq + (q & 1);
                     if (m >= g.M || n >= g.N) continue;
                     float v = g.alpha * acc[i][j][q];
-                    if (g.bias && sk == 0) v += g.bias_rows ? g.bias[m] : g.bias[n];
-                    Cb[(size_t)m * g.ldc + n] = v;
+                    if (add_bias) v += g.bias_rows ? g.bias[m] : g.bias[n];
+                    atomicAdd(Cb + (size_t)m * g.ldc + n, v);
                 }
         return;
     }
+    extern __shared__ float4 gemm_stage[];
+    constexpr int LDS = BN + 4;                 // padded row of the stage (floats)
+    float* Cs = reinterpret_cast<float*>(gemm_stage);
 #pragma unroll
-    for (int i = 0; i < S::TM; i++) {
-        float2 old[S::TN][2];
+    for (int i = 0; i < S::TM; i++)
 #pragma unroll
         for (int j = 0; j < S::TN; j++)
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + 8 * h;
-                const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq;
-                float2 o = make_float2(0.0f, 0.0f);
-                if (loadc && m < g.M) {
-                    const float* c = Cb + (size_t)m * g.ldc + n;
-                    if (v2 && n + 1 < g.N) o = *reinterpret_cast<const float2*>(c);
-                    else {
-                        if (n < g.N) o.x = c[0];
-                        if (n + 1 < g.N) o.y = c[1];
-                    }
-                }
-                old[j][h] = o;
+            for (int q = 0; q < 4; q++) {
+                const int ml = wm * (BM / S::WM) + i * 16 + gq + (q >= 2 ? 8 : 0);
+                const int nl = wn * (BN / S::WN) + j * 8 + 2 * tq + (q & 1);
+                Cs[ml * LDS + nl] = g.alpha * acc[i][j][q];
             }
-#pragma unroll
-        for (int j = 0; j < S::TN; j++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int m = m0 + wm * (BM / S::WM) + i * 16 + gq + 8 * h;
-                const int n = n0 + wn * (BN / S::WN) + j * 8 + 2 * tq;
-                if (m >= g.M || n >= g.N) continue;
-                float v0 = g.alpha * acc[i][j][2 * h], v1 = g.alpha * acc[i][j][2 * h + 1];
-                if (g.bias && sk == 0 && (bz == 0 || g.sC != 0)) {
-                    v0 += g.bias_rows ? g.bias[m] : g.bias[n];
-                    if (n + 1 < g.N) v1 += g.bias_rows ? g.bias[m] : g.bias[n + 1];
-                }
-                float* c = Cb + (size_t)m * g.ldc + n;
-                if (shared) {
-                    // split K, or a batch summed into one C: several CTAs add
-                    // here (gemm_launch scaled C by beta beforehand)
-                    atomicAdd(c, v0);
-                    if (n + 1 < g.N) atomicAdd(c + 1, v1);
-                    continue;
-                }
-                if (loadc) {
-                    v0 = fmaf(g.beta, old[j][h].x, v0);
-                    v1 = fmaf(g.beta, old[j][h].y, v1);
-                }
-                float* c2 = g.C2 ? g.C2 + (size_t)bz * g.sC + (size_t)m * g.ldc + n : nullptr;
-                if (v2 && n + 1 < g.N) {
-                    *reinterpret_cast<float2*>(c) = make_float2(v0, v1);
-                    if (c2) *reinterpret_cast<float2*>(c2) = make_float2(gelu_f(v0), gelu_f(v1));
+    __syncthreads();
+    const bool v4 = (g.ldc % 4 == 0) && ((reinterpret_cast<uintptr_t>(Cb) & 15) == 0) &&
+                    (!g.C2 || ((reinterpret_cast<uintptr_t>(g.C2 + (size_t)bz * g.sC) & 15) == 0));
+    float* C2b = g.C2 ? g.C2 + (size_t)bz * g.sC : nullptr;
+    for (int idx = tid; idx < BM * BN / 4; idx += 256) {
+        const int ml = idx / (BN / 4), nl = (idx % (BN / 4)) * 4;
+        const int m = m0 + ml, n = n0 + nl;
+        if (m >= g.M || n >= g.N) continue;
+        float4 v = *reinterpret_cast<const float4*>(&Cs[ml * LDS + nl]);
+        float* c = Cb + (size_t)m * g.ldc + n;
+        float* c2 = C2b ? C2b + (size_t)m * g.ldc + n : nullptr;
+        if (v4 && n + 3 < g.N) {
+            if (add_bias) {
+                if (g.bias_rows) {
+                    const float b = g.bias[m];
+                    v.x += b; v.y += b; v.z += b; v.w += b;
                 } else {
-                    c[0] = v0;
-                    if (c2) c2[0] = gelu_f(v0);
-                    if (n + 1 < g.N) {
-                        c[1] = v1;
-                        if (c2) c2[1] = gelu_f(v1);
-                    }
+                    v.x += g.bias[n]; v.y += g.bias[n + 1]; v.z += g.bias[n + 2]; v.w += g.bias[n + 3];
                 }
             }
+            if (g.beta != 0.0f) {
+                const float4 o = *reinterpret_cast<const float4*>(c);
+                v.x = fmaf(g.beta, o.x, v.x); v.y = fmaf(g.beta, o.y, v.y);
+                v.z = fmaf(g.beta, o.z, v.z); v.w = fmaf(g.beta, o.w, v.w);
+            }
+            *reinterpret_cast<float4*>(c) = v;
+            if (c2) *reinterpret_cast<float4*>(c2) = make_float4(gelu_f(v.x), gelu_f(v.y), gelu_f(v.z), gelu_f(v.w));
+        } else {
+            const float vv[4] = {v.x, v.y, v.z, v.w};
+            for (int e = 0; e < 4 && n + e < g.N; e++) {
+                float x = vv[e];
+                if (add_bias) x += g.bias_rows ? g.bias[m] : g.bias[n + e];
+                if (g.beta != 0.0f) x = fmaf(g.beta, c[e], x);
+                c[e] = x;
+                if (c2) c2[e] = gelu_f(x);
+            }
+        }
     }
 }
+
+// dynamic shared memory of the epilogue stage of a BM x BN tile
+constexpr size_t stage_bytes(int BM, int BN) { return (size_t)BM * (BN + 4) * sizeof(float); }
 
 }  // namespace gemm
 
