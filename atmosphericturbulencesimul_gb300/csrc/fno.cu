@@ -63,7 +63,7 @@ struct atmwfs_fno {
     float* adam_v = nullptr;
     long step = 0;
     // DFT matrices (FP32, rounded to BF16 by the products)
-    float *Fx = nullptr, *FyA = nullptr, *FyB = nullptr, *Gyr = nullptr, *Gyi = nullptr, *Gyin = nullptr, *Gx = nullptr;
+    float *Fx = nullptr, *FyAB = nullptr, *GyBig = nullptr, *Gx = nullptr;
     // activations for one batch size
     int cap = 0;
     std::vector<float*> h, u, a, z;     // h[0..nl], u[0..nl-1], a/z per layer
@@ -167,14 +167,15 @@ __global__ void k_mse(const float* __restrict__ out, const float* __restrict__ t
 }
 
 // Mode mixing y[b][o][k] = sum_c R[k][o][c] z[b][c][k] (complex), one block
-// per mode k = (ky, kx).  z / y layout per (b, channel): [2m][m] with the
-// real parts in rows 0..m-1 and the imaginary parts in rows m..2m-1.
+// per mode k = (ky, kx).  z / y layout [2m][B w][m]: row ky holds the real
+// parts, row m + ky the imaginary parts, then (sample, channel), then kx.
 __global__ void k_modemix(const __nv_bfloat16* __restrict__ R, const float* __restrict__ z, float* __restrict__ y,
                           int B, int w, int m)
 {
     const int k = blockIdx.x, ky = k / m, kx = k % m;
-    const long plane = 2L * m * m;
-    const long ore = (long)ky * m + kx, oim = (long)(m + ky) * m + kx;
+    const long plane = m;                                     // (sample, channel) stride
+    const long Nc = (long)B * w * m;
+    const long ore = (long)ky * Nc + kx, oim = (long)(m + ky) * Nc + kx;
     extern __shared__ float sh[];
     float* zs = sh;                  // [B][w][2]
     float2* rs = reinterpret_cast<float2*>(sh + 2 * B * w);  // [w][w + 1]: R[o][c], padded rows
@@ -210,8 +211,9 @@ __global__ void k_modemix_bwd(const __nv_bfloat16* __restrict__ R, const float* 
                               int m)
 {
     const int k = blockIdx.x, ky = k / m, kx = k % m;
-    const long plane = 2L * m * m;
-    const long ore = (long)ky * m + kx, oim = (long)(m + ky) * m + kx;
+    const long plane = m;                                     // (sample, channel) stride
+    const long Nc = (long)B * w * m;
+    const long ore = (long)ky * Nc + kx, oim = (long)(m + ky) * Nc + kx;
     extern __shared__ float sh[];
     float* zs = sh;                  // [B][w][2]
     float* ds = sh + 2 * B * w;      // [B][w][2]
@@ -406,8 +408,24 @@ atmwfs_status build_dft(atmwfs_fno* f)
             Gx[(size_t)(m + kx) * G + x] = (float)(-ck * norm * sin(ang(kx, x)));
         }
     }
-    struct M { float** d; std::vector<float>* h; } mats[] = {{&f->Fx, &Fx}, {&f->FyA, &FyA}, {&f->FyB, &FyB}, {&f->Gyr, &Gyr},
-                                                            {&f->Gyi, &Gyi}, {&f->Gyin, &Gyin}, {&f->Gx, &Gx}};
+    // the y transforms as single products over the planar spectra:
+    // FyAB = [FyA | FyB] (2m x 2G) maps [a_re; a_im] to z;
+    // GyBig = [[Gyr | Gyin]; [Gyi | Gyr]] (2G x 2m) maps [y_re; y_im] to [bb_re; bb_im]
+    std::vector<float> FyAB((size_t)2 * m * 2 * G), GyBig((size_t)2 * G * 2 * m);
+    for (int r = 0; r < 2 * m; r++)
+        for (int yy = 0; yy < G; yy++) {
+            FyAB[(size_t)r * 2 * G + yy] = FyA[(size_t)r * G + yy];
+            FyAB[(size_t)r * 2 * G + G + yy] = FyB[(size_t)r * G + yy];
+        }
+    for (int yy = 0; yy < G; yy++)
+        for (int j = 0; j < m; j++) {
+            GyBig[(size_t)yy * 2 * m + j] = Gyr[(size_t)yy * m + j];
+            GyBig[(size_t)yy * 2 * m + m + j] = Gyin[(size_t)yy * m + j];
+            GyBig[(size_t)(G + yy) * 2 * m + j] = Gyi[(size_t)yy * m + j];
+            GyBig[(size_t)(G + yy) * 2 * m + m + j] = Gyr[(size_t)yy * m + j];
+        }
+    struct M { float** d; std::vector<float>* h; } mats[] = {{&f->Fx, &Fx}, {&f->FyAB, &FyAB}, {&f->GyBig, &GyBig},
+                                                            {&f->Gx, &Gx}};
     for (auto& mm : mats) {
         FN_TRY(dalloc(f, (void**)mm.d, mm.h->size() * sizeof(float)));
         FN_CUDA(cudaMemcpy(*mm.d, mm.h->data(), mm.h->size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -462,37 +480,52 @@ atmwfs_status ensure_batch(atmwfs_fno* f, int B)
     return ATMWFS_OK;
 }
 
+// Spectral images are planar and channel-interleaved so that the DFTs along
+// y are single wide products over every (sample, channel): with Nc = B w m,
+//   a, bb : [2][G][B w][m]   (real plane, imaginary plane; row y, channel, kx)
+//   z, y  : [2m][B w][m]     (rows: real parts of the m kept ky, then imaginary)
+// The x-DFT writes a through the product's row / column maps, and the x
+// inverse reads bb through its column map.
+static cudaError_t gemm_args(GemmArgs& g, float beta, cudaStream_t st)
+{
+    g.alpha = 1.0f;
+    g.batch = 1;
+    return gemm_launch(g, beta, st);
+}
+
 // spectral convolution of layer l: spec = S_l(h)
 atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, float* spec, int B, cudaStream_t st)
 {
     const atmwfs_fno_cfg& c = f->cfg;
     const int G = c.grid, m = c.modes, w = c.width;
-    const long rows = (long)B * w * G, bc = (long)B * w;
+    const long BW = (long)B * w, Nc = BW * m;
     float* a = f->a[l];
     float* z = f->z[l];
-    // a = h Fx: [B w G, G] x [G, 2m]
-    FN_CUDA(gemm((int)rows, 2 * m, G, h, G, 0, 0, f->Fx, 2 * m, 0, 0, a, 2 * m, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
-    // z = FyA a_re + FyB a_im per (b, c): [2m, G] x [G, m]
-    FN_CUDA(gemm(2 * m, m, G, f->FyA, G, 0, 0, a, 2 * m, 0, 0, z, m, 0.0f, (int)bc, 0, (long)G * 2 * m, 2L * m * m,
-                 nullptr, 0, st));
-    FN_CUDA(gemm(2 * m, m, G, f->FyB, G, 0, 0, a + m, 2 * m, 0, 0, z, m, 1.0f, (int)bc, 0, (long)G * 2 * m, 2L * m * m,
-                 nullptr, 0, st));
+    {   // a[p][y][bc][kx] = sum_x h[bc][y][x] Fx[x][p m + kx]
+        GemmArgs g{};
+        g.M = (int)(BW * G); g.N = 2 * m; g.K = G;
+        g.A = h; g.lda = G; g.B = f->Fx; g.ldb = 2 * m; g.C = a; g.ldc = 2 * m;
+        g.rdiv = G; g.c_lo = Nc; g.c_hi = m; g.cdiv = m; g.cc_hi = (long)G * Nc;
+        FN_CUDA(gemm_args(g, 0.0f, st));
+    }
+    // z = FyAB a: [2m, 2G] x [2G, Nc]
+    FN_CUDA(gemm(2 * m, (int)Nc, 2 * G, f->FyAB, 2 * G, 0, 0, a, Nc, 0, 0, z, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
     // y = R z per mode
     const size_t smf = sizeof(float) * (2 * B * w + 2 * w * (w + 1));
     if (smf > 227 * 1024) return err(ATMWFS_ERR_INVALID, "batch %d x width %d exceeds the mode-mixing shared memory", B, w);
     if (smf > 48 * 1024) FN_CUDA(cudaFuncSetAttribute(k_modemix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
     k_modemix<<<m * m, 256, smf, st>>>(f->pbf + f->L.R[l], z, f->y, B, w, m);
     FN_CUDA(cudaGetLastError());
-    // bb = Gy y per (b, o): bb_re = Gyr y_re + Gyin y_im; bb_im = Gyi y_re + Gyr y_im  ([G, m] x [m, m])
-    const long ys = 2L * m * m, bs = (long)G * 2 * m;
-    FN_CUDA(gemm(G, m, m, f->Gyr, m, 0, 0, f->y, m, 0, 0, f->bb, 2 * m, 0.0f, (int)bc, 0, ys, bs, nullptr, 0, st));
-    FN_CUDA(gemm(G, m, m, f->Gyin, m, 0, 0, f->y + (long)m * m, m, 0, 0, f->bb, 2 * m, 1.0f, (int)bc, 0, ys, bs, nullptr,
-                 0, st));
-    FN_CUDA(gemm(G, m, m, f->Gyi, m, 0, 0, f->y, m, 0, 0, f->bb + m, 2 * m, 0.0f, (int)bc, 0, ys, bs, nullptr, 0, st));
-    FN_CUDA(gemm(G, m, m, f->Gyr, m, 0, 0, f->y + (long)m * m, m, 0, 0, f->bb + m, 2 * m, 1.0f, (int)bc, 0, ys, bs,
-                 nullptr, 0, st));
-    // spec = bb Gx: [B w G, 2m] x [2m, G]
-    FN_CUDA(gemm((int)rows, G, 2 * m, f->bb, 2 * m, 0, 0, f->Gx, G, 0, 0, spec, G, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
+    // bb = GyBig y: [2G, 2m] x [2m, Nc]
+    FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->GyBig, 2 * m, 0, 0, f->y, Nc, 0, 0, f->bb, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
+    {   // spec[bo][y][x] = sum_{p,kx} bb[p][y][bo][kx] Gx[p m + kx][x]: rows (y, bo)
+        GemmArgs g{};
+        g.M = (int)(G * BW); g.N = G; g.K = 2 * m;
+        g.A = f->bb; g.lda = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
+        g.B = f->Gx; g.ldb = G; g.C = spec; g.ldc = G;
+        g.rdiv = (int)BW; g.c_lo = (long)G * G; g.c_hi = G;
+        FN_CUDA(gemm_args(g, 0.0f, st));
+    }
     return ATMWFS_OK;
 }
 
@@ -501,30 +534,34 @@ atmwfs_status spectral_bwd(atmwfs_fno* f, int l, const float* ds, float* dh, int
 {
     const atmwfs_fno_cfg& c = f->cfg;
     const int G = c.grid, m = c.modes, w = c.width;
-    const long rows = (long)B * w * G, bc = (long)B * w;
-    const long ys = 2L * m * m, bs = (long)G * 2 * m;
-    // dbb = ds Gx^T: [B w G, G] x [G, 2m]
-    FN_CUDA(gemm((int)rows, 2 * m, G, ds, G, 0, 0, f->Gx, G, 1, 0, f->dbb, 2 * m, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
-    // dy_re = Gyr^T dbb_re + Gyi^T dbb_im; dy_im = Gyin^T dbb_re + Gyr^T dbb_im  ([m, G] x [G, m])
-    FN_CUDA(gemm(m, m, G, f->Gyr, m, 1, 0, f->dbb, 2 * m, 0, 0, f->dy, m, 0.0f, (int)bc, 0, bs, ys, nullptr, 0, st));
-    FN_CUDA(gemm(m, m, G, f->Gyi, m, 1, 0, f->dbb + m, 2 * m, 0, 0, f->dy, m, 1.0f, (int)bc, 0, bs, ys, nullptr, 0, st));
-    FN_CUDA(gemm(m, m, G, f->Gyin, m, 1, 0, f->dbb, 2 * m, 0, 0, f->dy + (long)m * m, m, 0.0f, (int)bc, 0, bs, ys, nullptr,
-                 0, st));
-    FN_CUDA(gemm(m, m, G, f->Gyr, m, 1, 0, f->dbb + m, 2 * m, 0, 0, f->dy + (long)m * m, m, 1.0f, (int)bc, 0, bs, ys,
-                 nullptr, 0, st));
+    const long BW = (long)B * w, Nc = BW * m;
+    {   // dbb[p][y][bo][kx] = sum_x ds[bo][y][x] Gx[p m + kx][x]
+        GemmArgs g{};
+        g.M = (int)(BW * G); g.N = 2 * m; g.K = G;
+        g.A = ds; g.lda = G; g.B = f->Gx; g.ldb = G; g.tb = 1; g.C = f->dbb; g.ldc = 2 * m;
+        g.rdiv = G; g.c_lo = Nc; g.c_hi = m; g.cdiv = m; g.cc_hi = (long)G * Nc;
+        FN_CUDA(gemm_args(g, 0.0f, st));
+    }
+    // dy = GyBig^T dbb: [2m, 2G] x [2G, Nc]
+    FN_CUDA(gemm(2 * m, (int)Nc, 2 * G, f->GyBig, 2 * m, 1, 0, f->dbb, Nc, 0, 0, f->dy, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0,
+                 st));
     // dz, dR
     const size_t smb = sizeof(float) * (4 * B * w + 2 * w * (w + 1));
     if (smb > 227 * 1024) return err(ATMWFS_ERR_INVALID, "batch %d x width %d exceeds the mode-mixing shared memory", B, w);
     if (smb > 48 * 1024) FN_CUDA(cudaFuncSetAttribute(k_modemix_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
-    k_modemix_bwd<<<m * m, 256, smb, st>>>(f->pbf + f->L.R[l], f->z[l], f->dy, f->dz,
-                                                                 f->grads + f->L.R[l], B, w, m);
+    k_modemix_bwd<<<m * m, 256, smb, st>>>(f->pbf + f->L.R[l], f->z[l], f->dy, f->dz, f->grads + f->L.R[l], B, w, m);
     FN_CUDA(cudaGetLastError());
-    // da_re = FyA^T dz; da_im = FyB^T dz  ([G, 2m] x [2m, m])
-    FN_CUDA(gemm(G, m, 2 * m, f->FyA, G, 1, 0, f->dz, m, 0, 0, f->da, 2 * m, 0.0f, (int)bc, 0, ys, bs, nullptr, 0, st));
-    FN_CUDA(gemm(G, m, 2 * m, f->FyB, G, 1, 0, f->dz, m, 0, 0, f->da + m, 2 * m, 0.0f, (int)bc, 0, ys, bs, nullptr, 0,
+    // da = FyAB^T dz: [2G, 2m] x [2m, Nc]
+    FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->FyAB, 2 * G, 1, 0, f->dz, Nc, 0, 0, f->da, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0,
                  st));
-    // dh += da Fx^T: [B w G, 2m] x [2m, G]
-    FN_CUDA(gemm((int)rows, G, 2 * m, f->da, 2 * m, 0, 0, f->Fx, 2 * m, 1, 0, dh, G, 1.0f, 1, 0, 0, 0, nullptr, 0, st));
+    {   // dh[bc][y][x] += sum_{p,kx} da[p][y][bc][kx] Fx[x][p m + kx]: rows (y, bc)
+        GemmArgs g{};
+        g.M = (int)(G * BW); g.N = G; g.K = 2 * m;
+        g.A = f->da; g.lda = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
+        g.B = f->Fx; g.ldb = 2 * m; g.tb = 1; g.C = dh; g.ldc = G;
+        g.rdiv = (int)BW; g.c_lo = (long)G * G; g.c_hi = G;
+        FN_CUDA(gemm_args(g, 1.0f, st));
+    }
     return ATMWFS_OK;
 }
 

@@ -42,6 +42,9 @@ cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
 {
     GemmArgs g = g0;
     if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
+    // a split block must hold whole 4-element vectors; A maps need A stored M x K
+    if ((g.cdiv && (g.cdiv % 4 || g.cc_hi % 4)) || (g.kdiv && (g.kdiv % 4 || g.ka_hi % 4 || g.ta)))
+        return cudaErrorInvalidValue;
     const bool bm128 = g.M > 64, bn128 = g.N > 64;
     const int BM = bm128 ? 128 : 64, BN = bn128 ? 128 : 64;
     const long tiles = (long)((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN) * g.batch;
@@ -50,6 +53,7 @@ cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
     int split = 1;
     while (split < 64 && tiles * split < 4 * 152 && kchunks / (split * 2) >= 4) split *= 2;
     if (g.splitk < 1) g.splitk = split;
+    if (g.rdiv || g.cdiv) g.splitk = 1;   // index maps: private C only
     if ((long)g.batch * g.splitk > 65535) g.splitk = std::max(1, 65535 / g.batch);
     const bool atomic = g.splitk > 1 || (g.batch > 1 && g.sC == 0);
     g.beta = beta;

@@ -31,6 +31,17 @@ struct GemmArgs {
     int splitk;           // K ranges over grid.z % splitk
     int batch;
     float* C2;            // optional: gelu of the final C value, same layout (not with shared accumulation)
+    // Optional index maps (0 = off; private C only).  Row m of C at
+    // (m % rdiv) c_lo + (m / rdiv) c_hi instead of m ldc; column n of C at
+    // (n / cdiv) cc_hi + n % cdiv; column k of A (stored M x K) at
+    // (k / kdiv) ka_hi + k % kdiv.  They let a product read or write planar
+    // and transposed layouts directly (multiples of 4 keep 16-byte vectors).
+    int rdiv;
+    long c_lo, c_hi;
+    int cdiv;
+    long cc_hi;
+    int kdiv;
+    long ka_hi;
 };
 
 // GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 x (1 + tanh(c (x + 0.044715 x^3))), c = sqrt(2 / pi)
@@ -137,9 +148,10 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
                 const int kk = e / BM, mm = e % BM, k = k0 + kk;
                 ra[j] = (k < g.K) ? ld4(Ab + (size_t)k * g.lda * esa, m0 + mm, g.M, g.a_bf16, va)
                                   : make_float4(0.f, 0.f, 0.f, 0.f);
-            } else {     // stored M x K: 4 consecutive k
-                const int mm = e / BK, kk = e % BK, m = m0 + mm;
-                ra[j] = (m < g.M) ? ld4(Ab + (size_t)m * g.lda * esa, k0 + kk, g.K, g.a_bf16, va)
+            } else {     // stored M x K: 4 consecutive k (one block of a split never straddles 4)
+                const int mm = e / BK, kk = e % BK, m = m0 + mm, k = k0 + kk;
+                const long ksh = g.kdiv ? (long)(k / g.kdiv) * (g.ka_hi - g.kdiv) : 0;   // split offset of column k
+                ra[j] = (m < g.M) ? ld4(Ab + ((size_t)m * g.lda + ksh) * esa, k, g.K, g.a_bf16, va)
                                   : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
@@ -263,15 +275,19 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
             }
     __syncthreads();
     const bool v4 = (g.ldc % 4 == 0) && ((reinterpret_cast<uintptr_t>(Cb) & 15) == 0) &&
-                    (!g.C2 || ((reinterpret_cast<uintptr_t>(g.C2 + (size_t)bz * g.sC) & 15) == 0));
+                    (!g.C2 || ((reinterpret_cast<uintptr_t>(g.C2 + (size_t)bz * g.sC) & 15) == 0)) &&
+                    (!g.rdiv || (g.c_lo % 4 == 0 && g.c_hi % 4 == 0)) &&
+                    (!g.cdiv || (g.cdiv % 4 == 0 && g.cc_hi % 4 == 0));
     float* C2b = g.C2 ? g.C2 + (size_t)bz * g.sC : nullptr;
     for (int idx = tid; idx < BM * BN / 4; idx += 256) {
         const int ml = idx / (BN / 4), nl = (idx % (BN / 4)) * 4;
         const int m = m0 + ml, n = n0 + nl;
         if (m >= g.M || n >= g.N) continue;
         float4 v = *reinterpret_cast<const float4*>(&Cs[ml * LDS + nl]);
-        float* c = Cb + (size_t)m * g.ldc + n;
-        float* c2 = C2b ? C2b + (size_t)m * g.ldc + n : nullptr;
+        const size_t roff = g.rdiv ? (size_t)(m % g.rdiv) * g.c_lo + (size_t)(m / g.rdiv) * g.c_hi : (size_t)m * g.ldc;
+        const long csh = g.cdiv ? (long)(n / g.cdiv) * (g.cc_hi - g.cdiv) : 0;   // split offset of column n
+        float* c = Cb + roff + csh + n;
+        float* c2 = C2b ? C2b + roff + csh + n : nullptr;
         if (v4 && n + 3 < g.N) {
             if (add_bias) {
                 if (g.bias_rows) {
