@@ -518,12 +518,11 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, float* spec, in
     FN_CUDA(cudaGetLastError());
     // bb = GyBig y: [2G, 2m] x [2m, Nc]
     FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->GyBig, 2 * m, 0, 0, f->y, Nc, 0, 0, f->bb, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
-    {   // spec[bo][y][x] = sum_{p,kx} bb[p][y][bo][kx] Gx[p m + kx][x]: rows (y, bo)
+    {   // spec[bo][y][x] = sum_{p,kx} bb[p][y][bo][kx] Gx[p m + kx][x]: rows (bo, y), A read through its maps
         GemmArgs g{};
-        g.M = (int)(G * BW); g.N = G; g.K = 2 * m;
-        g.A = f->bb; g.lda = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
+        g.M = (int)(BW * G); g.N = G; g.K = 2 * m;
+        g.A = f->bb; g.lda = m; g.ardiv = G; g.a_lo = Nc; g.a_hi = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
         g.B = f->Gx; g.ldb = G; g.C = spec; g.ldc = G;
-        g.rdiv = (int)BW; g.c_lo = (long)G * G; g.c_hi = G;
         FN_CUDA(gemm_args(g, 0.0f, st));
     }
     return ATMWFS_OK;
@@ -554,12 +553,11 @@ atmwfs_status spectral_bwd(atmwfs_fno* f, int l, const float* ds, float* dh, int
     // da = FyAB^T dz: [2G, 2m] x [2m, Nc]
     FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->FyAB, 2 * G, 1, 0, f->dz, Nc, 0, 0, f->da, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0,
                  st));
-    {   // dh[bc][y][x] += sum_{p,kx} da[p][y][bc][kx] Fx[x][p m + kx]: rows (y, bc)
+    {   // dh[bc][y][x] += sum_{p,kx} da[p][y][bc][kx] Fx[x][p m + kx]: rows (bc, y), A read through its maps
         GemmArgs g{};
-        g.M = (int)(G * BW); g.N = G; g.K = 2 * m;
-        g.A = f->da; g.lda = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
+        g.M = (int)(BW * G); g.N = G; g.K = 2 * m;
+        g.A = f->da; g.lda = m; g.ardiv = G; g.a_lo = Nc; g.a_hi = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
         g.B = f->Fx; g.ldb = 2 * m; g.tb = 1; g.C = dh; g.ldc = G;
-        g.rdiv = (int)BW; g.c_lo = (long)G * G; g.c_hi = G;
         FN_CUDA(gemm_args(g, 1.0f, st));
     }
     return ATMWFS_OK;

@@ -43,7 +43,8 @@ cudaError_t gemm_launch(const GemmArgs& g0, float beta, cudaStream_t st)
     GemmArgs g = g0;
     if (g.M <= 0 || g.N <= 0 || g.batch <= 0) return cudaSuccess;
     // a split block must hold whole 4-element vectors; A maps need A stored M x K
-    if ((g.cdiv && (g.cdiv % 4 || g.cc_hi % 4)) || (g.kdiv && (g.kdiv % 4 || g.ka_hi % 4 || g.ta)))
+    if ((g.cdiv && (g.cdiv % 4 || g.cc_hi % 4)) || (g.kdiv && (g.kdiv % 4 || g.ka_hi % 4 || g.ta)) ||
+        (g.ardiv && g.ta))
         return cudaErrorInvalidValue;
     const bool bm128 = g.M > 64, bn128 = g.N > 64;
     const int BM = bm128 ? 128 : 64, BN = bn128 ? 128 : 64;

@@ -42,6 +42,8 @@ struct GemmArgs {
     long cc_hi;
     int kdiv;
     long ka_hi;
+    int ardiv;            // row m of A (stored M x K) at (m % ardiv) a_lo + (m / ardiv) a_hi
+    long a_lo, a_hi;
 };
 
 // GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 x (1 + tanh(c (x + 0.044715 x^3))), c = sqrt(2 / pi)
@@ -131,7 +133,8 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
     const char* Bb = reinterpret_cast<const char*>(g.B) + (size_t)bz * g.sB * esb;
     float* Cb = g.C + (size_t)bz * g.sC;
     // vector loads need the contiguous dimension's stride and the base aligned
-    const bool va = (g.lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(Ab) & (4 * esa - 1)) == 0);
+    const bool va = (g.lda % 4 == 0) && ((reinterpret_cast<uintptr_t>(Ab) & (4 * esa - 1)) == 0) &&
+                    (!g.ardiv || (g.a_lo % 4 == 0 && g.a_hi % 4 == 0));
     const bool vb = (g.ldb % 4 == 0) && ((reinterpret_cast<uintptr_t>(Bb) & (4 * esb - 1)) == 0);
     // K range of this split, a multiple of BK
     const int kchunks = (g.K + BK - 1) / BK;
@@ -151,7 +154,9 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
             } else {     // stored M x K: 4 consecutive k (one block of a split never straddles 4)
                 const int mm = e / BK, kk = e % BK, m = m0 + mm, k = k0 + kk;
                 const long ksh = g.kdiv ? (long)(k / g.kdiv) * (g.ka_hi - g.kdiv) : 0;   // split offset of column k
-                ra[j] = (m < g.M) ? ld4(Ab + ((size_t)m * g.lda + ksh) * esa, k, g.K, g.a_bf16, va)
+                const size_t aro = g.ardiv ? (size_t)(m % g.ardiv) * g.a_lo + (size_t)(m / g.ardiv) * g.a_hi
+                                           : (size_t)m * g.lda;
+                ra[j] = (m < g.M) ? ld4(Ab + (aro + ksh) * esa, k, g.K, g.a_bf16, va)
                                   : make_float4(0.f, 0.f, 0.f, 0.f);
             }
         }
@@ -279,39 +284,96 @@ __global__ void __launch_bounds__(256, 2) k_gemm(const GemmArgs g)
                     (!g.rdiv || (g.c_lo % 4 == 0 && g.c_hi % 4 == 0)) &&
                     (!g.cdiv || (g.cdiv % 4 == 0 && g.cc_hi % 4 == 0));
     float* C2b = g.C2 ? g.C2 + (size_t)bz * g.sC : nullptr;
-    for (int idx = tid; idx < BM * BN / 4; idx += 256) {
-        const int ml = idx / (BN / 4), nl = (idx % (BN / 4)) * 4;
-        const int m = m0 + ml, n = n0 + nl;
-        if (m >= g.M || n >= g.N) continue;
-        float4 v = *reinterpret_cast<const float4*>(&Cs[ml * LDS + nl]);
-        const size_t roff = g.rdiv ? (size_t)(m % g.rdiv) * g.c_lo + (size_t)(m / g.rdiv) * g.c_hi : (size_t)m * g.ldc;
-        const long csh = g.cdiv ? (long)(n / g.cdiv) * (g.cc_hi - g.cdiv) : 0;   // split offset of column n
-        float* c = Cb + roff + csh + n;
-        float* c2 = C2b ? C2b + roff + csh + n : nullptr;
-        if (v4 && n + 3 < g.N) {
-            if (add_bias) {
-                if (g.bias_rows) {
-                    const float b = g.bias[m];
-                    v.x += b; v.y += b; v.z += b; v.w += b;
-                } else {
-                    v.x += g.bias[n]; v.y += g.bias[n + 1]; v.z += g.bias[n + 2]; v.w += g.bias[n + 3];
+    const bool loadc = g.beta != 0.0f;
+    if (!loadc) {
+        // plain stores, one vector at a time
+        for (int idx = tid; idx < BM * BN / 4; idx += 256) {
+            const int ml = idx / (BN / 4), nl = (idx % (BN / 4)) * 4;
+            const int m = m0 + ml, n = n0 + nl;
+            if (m >= g.M || n >= g.N) continue;
+            float4 v = *reinterpret_cast<const float4*>(&Cs[ml * LDS + nl]);
+            const size_t roff = g.rdiv ? (size_t)(m % g.rdiv) * g.c_lo + (size_t)(m / g.rdiv) * g.c_hi : (size_t)m * g.ldc;
+            const long csh = g.cdiv ? (long)(n / g.cdiv) * (g.cc_hi - g.cdiv) : 0;   // split offset of column n
+            float* c = Cb + roff + csh + n;
+            float* c2 = C2b ? C2b + roff + csh + n : nullptr;
+            if (v4 && n + 3 < g.N) {
+                if (add_bias) {
+                    if (g.bias_rows) {
+                        const float b = g.bias[m];
+                        v.x += b; v.y += b; v.z += b; v.w += b;
+                    } else {
+                        v.x += g.bias[n]; v.y += g.bias[n + 1]; v.z += g.bias[n + 2]; v.w += g.bias[n + 3];
+                    }
+                }
+                *reinterpret_cast<float4*>(c) = v;
+                if (c2) *reinterpret_cast<float4*>(c2) = make_float4(gelu_f(v.x), gelu_f(v.y), gelu_f(v.z), gelu_f(v.w));
+            } else {
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+                for (int e = 0; e < 4 && n + e < g.N; e++) {
+                    float x = vv[e];
+                    if (add_bias) x += g.bias_rows ? g.bias[m] : g.bias[n + e];
+                    c[e] = x;
+                    if (c2) c2[e] = gelu_f(x);
                 }
             }
-            if (g.beta != 0.0f) {
-                const float4 o = *reinterpret_cast<const float4*>(c);
-                v.x = fmaf(g.beta, o.x, v.x); v.y = fmaf(g.beta, o.y, v.y);
-                v.z = fmaf(g.beta, o.z, v.z); v.w = fmaf(g.beta, o.w, v.w);
-            }
-            *reinterpret_cast<float4*>(c) = v;
-            if (c2) *reinterpret_cast<float4*>(c2) = make_float4(gelu_f(v.x), gelu_f(v.y), gelu_f(v.z), gelu_f(v.w));
-        } else {
-            const float vv[4] = {v.x, v.y, v.z, v.w};
-            for (int e = 0; e < 4 && n + e < g.N; e++) {
-                float x = vv[e];
-                if (add_bias) x += g.bias_rows ? g.bias[m] : g.bias[n + e];
-                if (g.beta != 0.0f) x = fmaf(g.beta, c[e], x);
-                c[e] = x;
-                if (c2) c2[e] = gelu_f(x);
+        }
+        return;
+    }
+    // with a beta term: groups of four vectors per thread, the old values of
+    // a group all requested before the group's first store (their loads overlap)
+    constexpr int ITER = BM * BN / 4 / 256, GRP = 4;
+    static_assert(ITER % GRP == 0, "whole groups");
+#pragma unroll 1
+    for (int g0 = 0; g0 < ITER; g0 += GRP) {
+        float4 val[GRP], old[GRP];
+        size_t off[GRP];
+        int mq[GRP], nq[GRP];
+#pragma unroll
+        for (int q = 0; q < GRP; q++) {
+            const int idx = tid + 256 * (g0 + q);
+            const int ml = idx / (BN / 4), nl = (idx % (BN / 4)) * 4;
+            const int m = m0 + ml, n = n0 + nl;
+            mq[q] = m;
+            nq[q] = n;
+            val[q] = *reinterpret_cast<const float4*>(&Cs[ml * LDS + nl]);
+            const size_t roff = g.rdiv ? (size_t)(m % g.rdiv) * g.c_lo + (size_t)(m / g.rdiv) * g.c_hi : (size_t)m * g.ldc;
+            const long csh = g.cdiv ? (long)(n / g.cdiv) * (g.cc_hi - g.cdiv) : 0;   // split offset of column n
+            off[q] = roff + csh + n;
+            old[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (loadc && v4 && m < g.M && n + 3 < g.N) old[q] = *reinterpret_cast<const float4*>(Cb + off[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < GRP; q++) {
+            const int m = mq[q], n = nq[q];
+            if (m >= g.M || n >= g.N) continue;
+            float4 v = val[q];
+            float* c = Cb + off[q];
+            float* c2 = C2b ? C2b + off[q] : nullptr;
+            if (v4 && n + 3 < g.N) {
+                if (add_bias) {
+                    if (g.bias_rows) {
+                        const float b = g.bias[m];
+                        v.x += b; v.y += b; v.z += b; v.w += b;
+                    } else {
+                        v.x += g.bias[n]; v.y += g.bias[n + 1]; v.z += g.bias[n + 2]; v.w += g.bias[n + 3];
+                    }
+                }
+                if (loadc) {
+                    const float4 o = old[q];
+                    v.x = fmaf(g.beta, o.x, v.x); v.y = fmaf(g.beta, o.y, v.y);
+                    v.z = fmaf(g.beta, o.z, v.z); v.w = fmaf(g.beta, o.w, v.w);
+                }
+                *reinterpret_cast<float4*>(c) = v;
+                if (c2) *reinterpret_cast<float4*>(c2) = make_float4(gelu_f(v.x), gelu_f(v.y), gelu_f(v.z), gelu_f(v.w));
+            } else {
+                const float vv[4] = {v.x, v.y, v.z, v.w};
+                for (int e = 0; e < 4 && n + e < g.N; e++) {
+                    float x = vv[e];
+                    if (add_bias) x += g.bias_rows ? g.bias[m] : g.bias[n + e];
+                    if (loadc) x = fmaf(g.beta, c[e], x);
+                    c[e] = x;
+                    if (c2) c2[e] = gelu_f(x);
+                }
             }
         }
     }
