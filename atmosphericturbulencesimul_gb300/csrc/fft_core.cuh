@@ -24,8 +24,25 @@
 
 namespace atmwfs {
 
-AW_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-AW_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add / subtract.  On sm_100 and later the (re, im) pair is one
+// packed FP32x2 operation (per component the same IEEE rounding as the
+// scalar form; a - b as the exact b * (-1) + a).
+AW_HD float2 cadd(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+AW_HD float2 csub(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 AW_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 // a * conj(b)
 AW_HD float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
