@@ -236,17 +236,30 @@ __global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __rest
     const short* __restrict__ binx = I.binx;
     const float* __restrict__ peakv = I.peak;
     const float* __restrict__ psum = I.phisum;
-    // one row per block iteration, one column per thread
+    // one row per block iteration; four columns per thread as 16-byte vectors
+    // when the row length allows, else one column per thread
+    const bool v4 = (Nout % 4 == 0) && ((reinterpret_cast<uintptr_t>(pha) & 15) == 0) &&
+                    ((reinterpret_cast<uintptr_t>(psum) & 15) == 0);
     for (int jj = blockIdx.x; jj < Nout; jj += gridDim.x) {
         const int bj = nb > 0 ? binx[jj] * nb : 0;
         const size_t ro = (size_t)jj * Nout;
-        for (int ii = threadIdx.x; ii < Nout; ii += blockDim.x) {
+        auto one = [&](float p, float s, int ii) {
             const float peak = nb > 0 ? peakv[bj + binx[ii]] : 0.0f;
-            const float p = pha[ro + ii];
             float d1, e1, d2, e2;
-            two_sum(psum[ro + ii], -p, d1, e1);
+            two_sum(s, -p, d1, e1);
             two_sum(d1, -peak, d2, e2);
-            pha[ro + ii] = add_2pi_multiple(p, round_2pi(d2, e1 + e2));
+            return add_2pi_multiple(p, round_2pi(d2, e1 + e2));
+        };
+        if (v4) {
+            for (int i4 = threadIdx.x; i4 < Nout / 4; i4 += blockDim.x) {
+                const int ii = 4 * i4;
+                const float4 p = *reinterpret_cast<const float4*>(pha + ro + ii);
+                const float4 s = *reinterpret_cast<const float4*>(psum + ro + ii);
+                *reinterpret_cast<float4*>(pha + ro + ii) =
+                    make_float4(one(p.x, s.x, ii), one(p.y, s.y, ii + 1), one(p.z, s.z, ii + 2), one(p.w, s.w, ii + 3));
+            }
+        } else {
+            for (int ii = threadIdx.x; ii < Nout; ii += blockDim.x) pha[ro + ii] = one(pha[ro + ii], psum[ro + ii], ii);
         }
     }
 }
