@@ -154,22 +154,26 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
     float* pb = sh;
     float* ch = sh + n;
     float* ppf = sh + 2 * n;
-    __shared__ unsigned s_max;
-    __shared__ int s_cnt;
+    // vote maximum and flip count, double-buffered by iteration parity so
+    // that one iteration needs two barriers: the counters of iteration it-1
+    // are cleared in iteration it after its first barrier, when every thread
+    // has read them, and are next written after its second barrier
+    __shared__ unsigned s_max[2];
+    __shared__ int s_cnt[2];
+    const double kTwoPi = 2.0 * 3.14159265358979323846;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        pb[i] = (float)atan2((double)I.bins[n + i], (double)I.bins[i]);
+        const float v = (float)atan2((double)I.bins[n + i], (double)I.bins[i]);
+        pb[i] = v;
+        ppf[i] = __double2float_rd((double)v + kTwoPi * 0.5);
         I.bins[i] = 0.0f;
         I.bins[n + i] = 0.0f;
     }
-    if (threadIdx.x == 0) { s_max = 0u; s_cnt = 0; }
+    if (threadIdx.x < 2) { s_max[threadIdx.x] = 0u; s_cnt[threadIdx.x] = 0; }
     __syncthreads();
-    int chiter = 0, chcnt0cnt = 0;
+    int chiter = 0, chcnt0cnt = 0, par = 0;
     double plim = 1.0;
-    const double kTwoPi = 2.0 * 3.14159265358979323846;
     while (plim > 0.51 && chiter < 1000 && chcnt0cnt < 5) {
         chiter++;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) ppf[i] = __double2float_rd((double)pb[i] + kTwoPi * 0.5);
-        __syncthreads();
         unsigned umax = 0u;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const float c = bin_votes(pb, ppf, nb, i % nb, i / nb);
@@ -178,10 +182,11 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
         }
         // one shared atomic per warp (max is order-free)
         umax = __reduce_max_sync(0xffffffffu, umax);
-        if ((threadIdx.x & 31) == 0) atomicMax(&s_max, umax);
+        if ((threadIdx.x & 31) == 0) atomicMax(&s_max[par], umax);
         __syncthreads();
-        plim = (double)__uint_as_float(s_max) - 0.001;
+        plim = (double)__uint_as_float(s_max[par]) - 0.001;
         if (plim < 0.5) plim = 0.5;
+        if (threadIdx.x == 0) { s_max[par ^ 1] = 0u; s_cnt[par ^ 1] = 0; }
         // for a float c: c > plim <=> c > rd(plim) (rd: round toward -inf to float)
         const float plimf = __double2float_rd(plim);
         int cnt = 0;
@@ -189,24 +194,26 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
             const int bx = i % nb, by = i / nb;
             const bool interior = bx > 1 && by > 1 && bx < nb - 2 && by < nb - 2;
             const float c = ch[i];
+            float v = pb[i];
             if (c > plimf) {
                 if (interior) cnt++;
-                pb[i] = (float)((double)pb[i] + kTwoPi);
+                v = (float)((double)v + kTwoPi);
             }
             if (c < -plimf) {
                 if (interior) cnt++;
-                pb[i] = (float)((double)pb[i] - kTwoPi);
+                v = (float)((double)v - kTwoPi);
+            }
+            if (v != pb[i]) {
+                pb[i] = v;
+                ppf[i] = __double2float_rd((double)v + kTwoPi * 0.5);
             }
         }
         cnt = __reduce_add_sync(0xffffffffu, cnt);
-        if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_cnt, cnt);
+        if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&s_cnt[par], cnt);
         __syncthreads();
-        const int chcnt = s_cnt;
-        __syncthreads();
-        if (threadIdx.x == 0) { s_max = 0u; s_cnt = 0; }
-        if (chcnt == 0) chcnt0cnt++;
+        if (s_cnt[par] == 0) chcnt0cnt++;
         else chcnt0cnt = 0;
-        __syncthreads();
+        par ^= 1;
     }
     for (int i = threadIdx.x; i < n; i += blockDim.x) I.peak[i] = pb[i];
     if (threadIdx.x == 0 && iters_out) iters_out[list[blockIdx.x]] = chiter;

@@ -122,15 +122,24 @@ struct PassGeom {
     static_assert(COLSUM_BYTES <= TILE_BYTES, "column sums must fit in the tile buffer");
 };
 
+// One layer's tile as NBOX box copies, issued by lane 0 of every warp of the
+// CTA (warp w takes boxes w, w + nwarps, ...): a single issuing thread would
+// hold its warp, and with it the whole CTA at the next barrier, for the
+// length of the issue sequence.  Warp 0 posts the tile's byte count with its
+// arrival; boxes of other warps may land before that, which leaves the
+// phase's transaction count negative until the arrival and is allowed.
+// Called by every thread of the CTA (threads other than lane 0 return).
 template <int N, int RR>
 __device__ __forceinline__ void tma_issue_layer(const TmaSet& maps, int orient, int l, const TileGeom& g, float* tile,
-                                                uint64_t* bar)
+                                                uint64_t* bar, int tid, int nthreads)
 {
     using G = PassGeom<N, RR>;
-    mbar_expect_tx(bar, (uint32_t)G::TILE_BYTES);
+    if (tid & 31) return;
+    const int w = tid >> 5, nw = (nthreads + 31) >> 5;
+    if (w == 0) mbar_expect_tx(bar, (uint32_t)G::TILE_BYTES);
     const CUtensorMap* m = &maps.m[orient][l];
 #pragma unroll 1
-    for (int k = 0; k < G::NBOX; k++) tma_load_2d(tile + k * G::TROWS * kBoxW, m, g.xs + k * kBoxW, g.ys, bar);
+    for (int k = w; k < G::NBOX; k += nw) tma_load_2d(tile + k * G::TROWS * kBoxW, m, g.xs + k * kBoxW, g.ys, bar);
 }
 
 // ---------------------------------------------------------------------------
@@ -330,7 +339,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         __syncthreads();
         // separate tile: its first copy overlaps the first propagation
         if constexpr (!ALIAS)
-            if (tid == 0 && ltop >= lbot) tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar);
+            if (ltop >= lbot) tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar, tid, NT);
     }
 
     float2 v[E];
@@ -356,9 +365,9 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                     __syncthreads();
                     if constexpr (ALIAS) {
                         // overlaid tile: the exchange rows are free now
-                        if (tid == 0 && ltop >= lbot) {
+                        if (ltop >= lbot && (tid & 31) == 0) {
                             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                            tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar);
+                            tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar, tid, NT);
                         }
                     }
                     for (int l = ltop; l >= lbot; l--) {
@@ -370,8 +379,8 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                                                    phi[r * N + x] = first ? val : phi[r * N + x] + val;
                                                });
                         __syncthreads();
-                        if (tid == 0 && l > lbot)
-                            tma_issue_layer<N, RR>(maps, a.orient, l - 1, tile_geom(P[l - 1], a.orient, y0), tile, &bar);
+                        if (l > lbot)
+                            tma_issue_layer<N, RR>(maps, a.orient, l - 1, tile_geom(P[l - 1], a.orient, y0), tile, &bar, tid, NT);
                     }
 #pragma unroll
                     for (int e = 0; e < E; e++) v[e] = cmul(v[e], phasor(phi[rr * N + t + e * T]));
@@ -522,13 +531,62 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
 // sarray1, AtmosphericTurbulence.c:2909-2916, 3237-3245): gather only, one
 // TMA tile per layer, compensated (two-sum) accumulation in registers.
 // Independent of the field, so it runs beside the propagation passes.
+//
+// Each thread owns column pairs (x, x + N/2 ... strided by the block): the
+// two columns share the layer's interpolation weights, so the Keys taps,
+// the scaling and the two-sum run as packed FP32x2 operations (sm_100+),
+// which round each component exactly like the scalar forms.
 // ---------------------------------------------------------------------------
 template <int N, int RR>
-__global__ void __launch_bounds__(Plan<N>::T* RR, 2)
+struct PhasumGeom {
+    static constexpr int NT0 = PassGeom<N, RR>::NT;
+    static constexpr int NTP = N >= 2 * NT0 ? NT0 : N / 2;  // threads per CTA
+    static constexpr int NCP = N / NTP;                     // columns per thread
+    static constexpr int NP = NCP / 2;                      // column pairs per thread
+    static_assert(N % NTP == 0 && NCP % 2 == 0, "column pairs must tile the row");
+};
+
+__device__ __forceinline__ float2 f2add(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+// a - b, one rounding per component
+__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fmul2_rn(a, b);
+#else
+    return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c)
+{
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __ffma2_rn(a, b, c);
+#else
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+
+template <int N, int RR>
+__global__ void __launch_bounds__(PhasumGeom<N, RR>::NTP, 2)
     k_phasum(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps)
 {
     using G = PassGeom<N, RR>;
-    constexpr int NT = G::NT, TROWS = G::TROWS, NC = (N + NT - 1) / NT;
+    using H = PhasumGeom<N, RR>;
+    constexpr int NTP = H::NTP, NP = H::NP, TROWS = G::TROWS;
     constexpr int TILE_FLOATS = (int)(G::TILE_BYTES / 4);
     extern __shared__ __align__(1024) unsigned char sm[];
     // two tile buffers: the next layer's copy overlaps this layer's sums
@@ -542,15 +600,14 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 2)
     const int L = a.L;
     if (tid == 0) { mbar_init(&bar[0], 1); mbar_init(&bar[1], 1); }
     __syncthreads();
-    if (tid == 0) {
-        tma_issue_layer<N, RR>(maps, 0, L - 1, tile_geom(P[L - 1], 0, y0), tiles, &bar[0]);
-        if (L > 1) tma_issue_layer<N, RR>(maps, 0, L - 2, tile_geom(P[L - 2], 0, y0), tiles + TILE_FLOATS, &bar[1]);
-    }
-    float hi[NC][RR], lo[NC][RR];
+    tma_issue_layer<N, RR>(maps, 0, L - 1, tile_geom(P[L - 1], 0, y0), tiles, &bar[0], tid, NTP);
+    if (L > 1) tma_issue_layer<N, RR>(maps, 0, L - 2, tile_geom(P[L - 2], 0, y0), tiles + TILE_FLOATS, &bar[1], tid, NTP);
+    // pair p: columns tid + p NTP (.x) and tid + (p + NP) NTP (.y)
+    float2 hi[NP][RR], lo[NP][RR];
 #pragma unroll
-    for (int c = 0; c < NC; c++)
+    for (int p = 0; p < NP; p++)
 #pragma unroll
-        for (int r = 0; r < RR; r++) hi[c][r] = lo[c][r] = 0.0f;
+        for (int r = 0; r < RR; r++) hi[p][r] = lo[p][r] = make_float2(0.0f, 0.0f);
     int parity = 0;  // bit b: phase parity of buffer b
     for (int l = L - 1; l >= 0; l--) {
         const int b = (L - 1 - l) & 1;
@@ -566,38 +623,57 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, 2)
         float wx[4], wy[4];
         keys_weights(g.fx, wx);
         keys_weights(g.fy, wy);
+        const float2 sc2 = make_float2(sc, sc);
+        float2 wx2[4], wy2[4];
 #pragma unroll
-        for (int c = 0; c < NC; c++) {
-            const int x = tid + c * NT;
-            if (x < N) {
-                const int cc = g.d + x;
-                float h[TROWS];
+        for (int k = 0; k < 4; k++) {
+            wx2[k] = make_float2(wx[k], wx[k]);
+            wy2[k] = make_float2(wy[k], wy[k]);
+        }
 #pragma unroll
-                for (int q = 0; q < TROWS; q++)
-                    h[q] = wx[0] * tile[tile_index<TROWS>(q, cc)] + wx[1] * tile[tile_index<TROWS>(q, cc + 1)] +
-                           wx[2] * tile[tile_index<TROWS>(q, cc + 2)] + wx[3] * tile[tile_index<TROWS>(q, cc + 3)];
+        for (int p = 0; p < NP; p++) {
+            const int ca = g.d + tid + p * NTP, cb = ca + NP * NTP;
+            // tile rows stream through: output row r takes taps from rows
+            // r..r+3 in that order, so at most four partial rows are live
+            float2 part[4];
 #pragma unroll
-                for (int r = 0; r < RR; r++) {
-                    const float val = (wy[0] * h[r] + wy[1] * h[r + 1] + wy[2] * h[r + 2] + wy[3] * h[r + 3]) * sc;
-                    float s, e;
-                    two_sum(hi[c][r], val, s, e);
-                    hi[c][r] = s;
-                    lo[c][r] += e;
+            for (int q = 0; q < TROWS; q++) {
+                float2 h = f2mul(wx2[0], make_float2(tile[tile_index<TROWS>(q, ca)], tile[tile_index<TROWS>(q, cb)]));
+#pragma unroll
+                for (int k = 1; k < 4; k++)
+                    h = f2fma(wx2[k], make_float2(tile[tile_index<TROWS>(q, ca + k)], tile[tile_index<TROWS>(q, cb + k)]), h);
+#pragma unroll
+                for (int k = 3; k >= 0; k--) {
+                    const int r = q - k;  // output row receiving tap k
+                    if (r < 0 || r >= RR) continue;
+                    float2& v = part[r & 3];
+                    v = k == 0 ? f2mul(wy2[0], h) : f2fma(wy2[k], h, v);
+                    if (k == 3) {
+                        const float2 val = f2mul(v, sc2);
+                        // two-sum: hi + val = s + e exactly
+                        const float2 s = f2add(hi[p][r], val);
+                        const float2 bp = f2sub(s, hi[p][r]);
+                        const float2 e = f2add(f2sub(hi[p][r], f2sub(s, bp)), f2sub(val, bp));
+                        hi[p][r] = s;
+                        lo[p][r] = f2add(lo[p][r], e);
+                    }
                 }
             }
         }
         __syncthreads();
-        if (tid == 0 && l > 1) tma_issue_layer<N, RR>(maps, 0, l - 2, tile_geom(P[l - 2], 0, y0), tile, &bar[b]);
+        if (l > 1) tma_issue_layer<N, RR>(maps, 0, l - 2, tile_geom(P[l - 2], 0, y0), tile, &bar[b], tid, NTP);
     }
     const int off = I->off, Nout = I->Nout;
 #pragma unroll
-    for (int c = 0; c < NC; c++) {
-        const int x = tid + c * NT;
+    for (int p = 0; p < NP; p++) {
 #pragma unroll
         for (int r = 0; r < RR; r++) {
             const int y = y0 + r;
-            if (x < N && x >= off && x < off + Nout && y >= off && y < off + Nout)
-                I->phisum[(size_t)(y - off) * Nout + (x - off)] = hi[c][r] + lo[c][r];
+            if (y < off || y >= off + Nout) continue;
+            float* row = I->phisum + (size_t)(y - off) * Nout - off;
+            const int xa = tid + p * NTP, xb = xa + NP * NTP;
+            if (xa >= off && xa < off + Nout) row[xa] = hi[p][r].x + lo[p][r].x;
+            if (xb >= off && xb < off + Nout) row[xb] = hi[p][r].y + lo[p][r].y;
         }
     }
 }
@@ -648,7 +724,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
                 if (e != cudaSuccess) return e;
                 attr = true;
             }
-            k_phasum<N, RR><<<grid, block, sm, st>>>(a, m);
+            k_phasum<N, RR><<<grid, dim3(PhasumGeom<N, RR>::NTP), sm, st>>>(a, m);
             return cudaGetLastError();
         }
         default: return cudaErrorInvalidValue;
