@@ -3,6 +3,7 @@
 
 #include "aux_kernels.cuh"
 #include "pass_impl.cuh"
+#include "atan_ff.cuh"
 
 namespace atmwfs {
 
@@ -144,7 +145,7 @@ __device__ float bin_votes(const float* pb, const float* ppf, int nb, int bx, in
 }
 
 __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restrict__ list, unsigned* status,
-                         int* iters_out)
+                         int* iters_out, const float2* __restrict__ atan_tab)
 {
     const InstDev& I = insts[list[blockIdx.x]];
     const int nb = I.nb;
@@ -162,7 +163,8 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
     __shared__ int s_cnt[2];
     const double kTwoPi = 2.0 * 3.14159265358979323846;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const float v = (float)atan2((double)I.bins[n + i], (double)I.bins[i]);
+        // (float)atan2((double)im, (double)re) without FP64 (atan_ff.cuh)
+        const float v = atan2_ff(I.bins[n + i], I.bins[i], atan_tab);
         pb[i] = v;
         ppf[i] = __double2float_rd((double)v + kTwoPi * 0.5);
         I.bins[i] = 0.0f;
@@ -220,7 +222,7 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
 }
 
 cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int maxnb, unsigned* status, int* iters,
-                        cudaStream_t st)
+                        const float2* atan_tab, cudaStream_t st)
 {
     if (nsci <= 0) return cudaSuccess;
     const size_t sm = (size_t)3 * maxnb * maxnb * sizeof(float);
@@ -228,7 +230,7 @@ cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int max
         cudaError_t e = cudaFuncSetAttribute(k_unwrap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    k_unwrap<<<nsci, 512, sm, st>>>(insts, list, status, iters);
+    k_unwrap<<<nsci, 512, sm, st>>>(insts, list, status, iters, atan_tab);
     return cudaGetLastError();
 }
 

@@ -7,8 +7,9 @@ namespace atmwfs {
 cudaError_t pad_screen(const float* S, int M, float* P, int Wp, int Hp, int orient, cudaStream_t st);
 cudaError_t lag_sumsq(const float* S, int M, int dpix, double* acc, cudaStream_t st);
 cudaError_t scale_screen(float* S, long n, double f, cudaStream_t st);
+// atan_tab: atan(k / 1024), k = 0 .. 1024, as (hi, lo) pairs (atan_table_host)
 cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int maxnb, unsigned* status, int* iters,
-                        cudaStream_t st);
+                        const float2* atan_tab, cudaStream_t st);
 cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxnout, const int* d_step, cudaStream_t st);
 cudaError_t step_advance(int* d_step, cudaStream_t st);
 cudaError_t screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, double fi, float2* C, cudaStream_t st);

@@ -3,17 +3,23 @@
 //   * the runtime Stockham stage loop for every supported N (forward,
 //     inverse and the forward -> transfer -> reversed inverse propagation);
 //   * the TMA tile geometry of the screen gather and the separable bicubic,
-//     against a direct periodic Keys bicubic in double.
+//     against a direct periodic Keys bicubic in double;
+//   * the FP32-only atan2 of the science unwrap against (float) of the
+//     double atan2 (count of differing results and the largest difference
+//     in units in the last place).
 // Prints one line per check: "<name> <max error>"; exit code 0.
 #include <array>
 #include <cmath>
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
+#include <cstdint>
 #include <vector>
 
 #include "fft_core.cuh"
 #include "gather_core.cuh"
+#include "atan_ff.cuh"
 
 using namespace atmwfs;
 using cd = std::complex<double>;
@@ -208,8 +214,67 @@ void check_gather(int M, int ix, int iy, float fx, float fy, int orient, int y0)
     printf("gather_%d_c%d_o%d_ix%d_iy%d %.3e\n", N, CFG, orient, ix, iy, inb ? err : 1e9);
 }
 
+static int ulp_distance(float a, float b)
+{
+    if (a == b) return 0;
+    int32_t ia, ib;
+    std::memcpy(&ia, &a, 4);
+    std::memcpy(&ib, &b, 4);
+    if ((ia < 0) != (ib < 0)) return 1 << 30;
+    return std::abs(ia - ib);
+}
+
+// The FP32-only atan2 against (float)atan2 in double on five input families:
+// uniform in the square, log-spread magnitudes (2^-60 .. 2^60) with random
+// signs, near the diagonal |y| ~ |x|, ratios on and beside the table points,
+// and signed zeros / the axes.
+static void check_atan2()
+{
+    std::vector<float2> tab(kAtanTabN + 1);
+    atan_table_host(tab.data());
+    long n = 0, diff = 0;
+    int maxulp = 0;
+    auto one = [&](float y, float x) {
+        const float a = atan2_ff(y, x, tab.data());
+        const float b = (float)std::atan2((double)y, (double)x);
+        const int d = ulp_distance(a, b);
+        n++;
+        if (d) diff++;
+        if (d > maxulp) maxulp = d;
+    };
+    for (int i = 0; i < 1000000; i++) one((float)(2 * urand() - 1), (float)(2 * urand() - 1));
+    for (int i = 0; i < 1000000; i++) {
+        const float y = (float)std::ldexp(urand() + 0.5, (int)(urand() * 120) - 60) * (urand() < 0.5 ? -1.0f : 1.0f);
+        const float x = (float)std::ldexp(urand() + 0.5, (int)(urand() * 120) - 60) * (urand() < 0.5 ? -1.0f : 1.0f);
+        one(y, x);
+    }
+    for (int i = 0; i < 500000; i++) {
+        const float x = (float)(urand() * 100 + 1e-3) * (urand() < 0.5 ? -1.0f : 1.0f);
+        const float y = x * (float)(1.0 + (urand() - 0.5) * 1e-5) * (urand() < 0.5 ? -1.0f : 1.0f);
+        one(y, x);
+        one(x, y);
+    }
+    for (int k = 0; k <= kAtanTabN; k++)
+        for (int j = -3; j <= 3; j++) {
+            const float x = 1024.0f * (1.0f + (float)j * 1.1920929e-7f);
+            const float y = (float)k;
+            one(y, x);
+            one(-y, -x);
+            one(x, y);
+            one(-x, y);
+            one(y * (1.0f + 3e-4f * j), x);
+        }
+    const float zs[] = {0.0f, -0.0f, 1.0f, -1.0f, 1e-38f, -1e-45f, 3e38f, -3e38f};
+    for (float y : zs)
+        for (float x : zs) one(y, x);
+    std::printf("atan2_diff %ld\n", diff);
+    std::printf("atan2_maxulp %d\n", maxulp);
+    std::printf("atan2_count %ld\n", n);
+}
+
 int main()
 {
+    check_atan2();
     check_fft<64>();
     check_fft<128>();
     check_fft<256>();
