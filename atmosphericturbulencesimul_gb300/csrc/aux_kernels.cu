@@ -113,11 +113,20 @@ __device__ __forceinline__ float vote_acc(float ch, double c) { return __double2
 // ppf[i] = (double)pb[i] + pi rounded toward -inf to float: for a float x,
 // x > (double)pb[i] + pi  <=>  x > ppf[i], so the reference's double
 // comparisons run as float comparisons with identical outcomes.
+//
+// The votes are found with float compares only and applied afterwards, in
+// the same order, with the reference's double accumulation: most bins get
+// none (a vote needs two neighbouring bins more than pi apart), so the
+// FP64 additions -- slow on this part, and otherwise evaluated for all 48
+// candidate votes of every bin -- run only where a vote fired.
 __device__ float bin_votes(const float* pb, const float* ppf, int nb, int bx, int by)
 {
-    float ch = 0.0f;
     const float pv = pb[by * nb + bx];
     const float pvp = ppf[by * nb + bx];
+    // bit 4 s + 2 k + m: vote m of role slot k of sweep s fired; the same bit
+    // of neg: that vote is -c
+    unsigned long long fired = 0ull, neg = 0ull;
+#pragma unroll
     for (int s = 0; s < 12; s++) {
         const Sweep w = c_sweeps[s];
         // role A: this bin is index1, partner index2 = (bx + dx, by + dy)
@@ -127,19 +136,28 @@ __device__ float bin_votes(const float* pb, const float* ppf, int nb, int bx, in
         const bool va = ax >= 0 && ax < nb && ay >= 0 && ay < nb;
         const bool vb = bxp >= 0 && bxp < nb && byp >= 0 && byp < nb;
         const bool a_first = (w.dx < 0) || (w.dx == 0 && w.dy < 0);
+#pragma unroll
         for (int k = 0; k < 2; k++) {
             const bool doA = (k == 0) == a_first;
+            const unsigned long long b0 = 1ull << (4 * s + 2 * k), b1 = b0 << 1;
             if (doA && va) {
                 const int j = ay * nb + ax;
-                if (pb[j] > pvp) ch = vote_acc(ch, w.c);          // pv2 > pv + pi
-                if (pv > ppf[j]) ch = vote_acc(ch, -w.c);         // pv > pv2 + pi
+                if (pb[j] > pvp) fired |= b0;                         // pv2 > pv + pi: +c
+                if (pv > ppf[j]) { fired |= b1; neg |= b1; }          // pv > pv2 + pi: -c
             }
             if (!doA && vb) {
                 const int j = byp * nb + bxp;
-                if (pv > ppf[j]) ch = vote_acc(ch, -w.c);         // pv > pv1 + pi
-                if (pb[j] > pvp) ch = vote_acc(ch, w.c);          // pv1 > pv + pi
+                if (pv > ppf[j]) { fired |= b0; neg |= b0; }          // pv > pv1 + pi: -c
+                if (pb[j] > pvp) fired |= b1;                         // pv1 > pv + pi: +c
             }
         }
+    }
+    float ch = 0.0f;
+    while (fired) {
+        const int b = __ffsll((long long)fired) - 1;
+        fired &= fired - 1ull;
+        const double c = c_sweeps[b >> 2].c;
+        ch = vote_acc(ch, ((neg >> b) & 1ull) ? -c : c);
     }
     return ch;
 }
@@ -196,16 +214,12 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
             const int bx = i % nb, by = i / nb;
             const bool interior = bx > 1 && by > 1 && bx < nb - 2 && by < nb - 2;
             const float c = ch[i];
-            float v = pb[i];
-            if (c > plimf) {
-                if (interior) cnt++;
-                v = (float)((double)v + kTwoPi);
-            }
-            if (c < -plimf) {
-                if (interior) cnt++;
-                v = (float)((double)v - kTwoPi);
-            }
-            if (v != pb[i]) {
+            const int dir = c > plimf ? 1 : (c < -plimf ? -1 : 0);
+            if (dir != 0 && interior) cnt++;
+            // the FP64 update only in warps where a bin flips (a plain
+            // branch would be evaluated speculatively for every bin)
+            if (__any_sync(__activemask(), dir != 0) && dir != 0) {
+                const float v = (float)((double)pb[i] + (dir > 0 ? kTwoPi : -kTwoPi));
                 pb[i] = v;
                 ppf[i] = __double2float_rd((double)v + kTwoPi * 0.5);
             }
