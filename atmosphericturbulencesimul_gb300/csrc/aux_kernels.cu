@@ -324,6 +324,8 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
 __global__ void k_screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, double fi, float2* __restrict__ C)
 {
     const long n = (long)M * M;
+    const int lg = __ffs(M) - 1;
+    const float fo2 = (float)(fo * fo), fif = (float)fi;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
         uint32_t c[4] = {(uint32_t)p, stream, 0u, 0u};
         philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
@@ -331,11 +333,11 @@ __global__ void k_screen_spectrum(uint64_t seed, uint32_t stream, int M, double 
         const float u1 = ((float)(c[1] >> 8) + 1.0f) * (1.0f / 16777216.0f);
         const float u2 = (float)(c[2] >> 8) * (1.0f / 16777216.0f);
         const float g = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
-        const int ii = (int)(p % M), jj = (int)(p / M);
+        const int ii = (int)p & (M - 1), jj = (int)(p >> lg);  // M is a power of two
         const float dx = (float)(ii - M / 2), dy = (float)(jj - M / 2);
         const float r2 = dx * dx + dy * dy;
-        const float d = sqrtf(r2 + (float)(fo * fo));
-        const float gi = g * sqrtf(expf(-r2 / (float)fi / (float)fi));
+        const float d = sqrtf(r2 + fo2);
+        const float gi = g * sqrtf(expf(-r2 / fif / fif));
         float a = gi / powf(d, 11.0f / 6.0f);
         if (ii == M / 2 && jj == M / 2) a = 0.0f;
         float s, co;
@@ -353,28 +355,51 @@ cudaError_t screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, do
 
 // Structure function D(lx, ly) of the real and imaginary parts at lags
 // (1..2)^2, circular (fft_structure_function, info.c:1670-1690, from its
-// definition).  acc[8]: [part][lag] sums.
+// definition).  acc[8]: [part][lag] sums.  Each thread keeps its sums in
+// float-float: the difference of two floats exactly (two-sum), its square
+// as an exact product plus the cross term, accumulated by two-sums (about
+// 46 bits, against the 53 of a double sum); the FP64 pipe, slow on this
+// part, is used only for the per-warp totals.
 __global__ void k_strf(const float2* __restrict__ F, int M, double* acc)
 {
-    double loc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float hi[8], lo[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) hi[q] = lo[q] = 0.0f;
     const long n = (long)M * M;
+    const int lg = __ffs(M) - 1, mk = M - 1;  // M is a power of two
+    auto add_sq = [&](int q, float a, float b) {
+        float dh, dl;
+        ff_two_sum(a, -b, dh, dl);
+        const float p = ff_mul(dh, dh);
+        const float pe = ff_fma(ff_add(dh, dh), dl, ff_fma(dh, dh, -p));
+        float s, e;
+        ff_two_sum(hi[q], p, s, e);
+        hi[q] = s;
+        lo[q] = ff_add(lo[q], ff_add(e, pe));
+    };
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < n; p += (long)gridDim.x * blockDim.x) {
-        const int x = (int)(p % M), y = (int)(p / M);
+        const int x = (int)p & mk, y = (int)(p >> lg);
         const float2 a = F[p];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int lx = 1 + (q & 1), ly = 1 + (q >> 1);
-            const float2 b = F[(size_t)((y + ly) % M) * M + (x + lx) % M];
-            const double dr = (double)a.x - (double)b.x, di = (double)a.y - (double)b.y;
-            loc[q] += dr * dr;
-            loc[4 + q] += di * di;
+            const float2 b = F[(size_t)((y + ly) & mk) * M + ((x + lx) & mk)];
+            add_sq(q, a.x, b.x);
+            add_sq(4 + q, a.y, b.y);
         }
     }
+    // warp totals in float-float, then one double atomic per warp and sum
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-        double v = loc[q];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[q], v);
+        float h = hi[q], l = lo[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, h, o), l2 = __shfl_down_sync(0xffffffffu, l, o);
+            float s, e;
+            ff_two_sum(h, h2, s, e);
+            h = s;
+            l = ff_add(l, ff_add(l2, e));
+        }
+        if ((threadIdx.x & 31) == 0) atomicAdd(&acc[q], (double)h + (double)l);
     }
 }
 
@@ -384,18 +409,29 @@ cudaError_t strf_lags(const float2* F, int M, double* acc, cudaStream_t st)
     return cudaGetLastError();
 }
 
-__global__ void k_split_scale(const float2* __restrict__ F, long n, double s1, double s2, float* o1, float* o2)
+// o = v s with s = sh + sl (float pair of the double scale): the exact
+// product v sh (two-product) plus v sl, rounded once -- the float of the
+// double product except when that lies within about 2^-46 of a midpoint.
+__device__ __forceinline__ float scale_ff(float v, float sh, float sl)
+{
+    const float p = ff_mul(v, sh);
+    return ff_add(p, ff_fma(v, sl, ff_fma(v, sh, -p)));
+}
+
+__global__ void k_split_scale(const float2* __restrict__ F, long n, float s1h, float s1l, float s2h, float s2l,
+                              float* o1, float* o2)
 {
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const float2 v = F[i];
-        if (o1) o1[i] = (float)((double)v.x * s1);
-        if (o2) o2[i] = (float)((double)v.y * s2);
+        if (o1) o1[i] = scale_ff(v.x, s1h, s1l);
+        if (o2) o2[i] = scale_ff(v.y, s2h, s2l);
     }
 }
 
 cudaError_t split_scale(const float2* F, long n, double s1, double s2, float* o1, float* o2, cudaStream_t st)
 {
-    k_split_scale<<<4 * 152, 256, 0, st>>>(F, n, s1, s2, o1, o2);
+    const float s1h = (float)s1, s2h = (float)s2;
+    k_split_scale<<<4 * 152, 256, 0, st>>>(F, n, s1h, (float)(s1 - (double)s1h), s2h, (float)(s2 - (double)s2h), o1, o2);
     return cudaGetLastError();
 }
 
