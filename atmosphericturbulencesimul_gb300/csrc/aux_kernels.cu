@@ -319,6 +319,31 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
     }
 }
 
+// ---------------------------------------------------------------------------
+// Frame copy-out into the caller's sink (pinned host or device memory).
+// The host link, not the issuer, bounds a device-to-host copy (about 190
+// GB/s here for the copy engine and for SM stores alike), and 32 CTAs of
+// plain 16-byte stores reach that rate while holding a small share of the
+// SMs; the copy engine reading the frames meanwhile slows the passes more.
+// ---------------------------------------------------------------------------
+__global__ void k_copy_out(const float4* __restrict__ s0, float4* __restrict__ d0, long n0,
+                           const float4* __restrict__ s1, float4* __restrict__ d1, long n1)
+{
+    const long stride = (long)gridDim.x * blockDim.x;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n0; i += stride) d0[i] = s0[i];
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n1; i += stride) d1[i] = s1[i];
+}
+
+cudaError_t copy_out(const float4* src0, float4* dst0, long n0, const float4* src1, float4* dst1, long n1,
+                     cudaStream_t st)
+{
+    if (!dst0) n0 = 0;
+    if (!dst1) n1 = 0;
+    if (n0 + n1 == 0) return cudaSuccess;
+    k_copy_out<<<32, 256, 0, st>>>(src0, dst0, n0, src1, dst1, n1);
+    return cudaGetLastError();
+}
+
 // Spectrum A(k) exp(i 2 pi u), written at its fftshifted position (the
 // reference applies permut() before the FFT, :782).
 __global__ void k_screen_spectrum(uint64_t seed, uint32_t stream, int M, double fo, double fi, float2* __restrict__ C)

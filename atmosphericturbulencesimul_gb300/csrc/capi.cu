@@ -1013,6 +1013,24 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
             AW_CUDA(cudaEventCreateWithFlags(&c->ev_copied[r], cudaEventDisableTiming));
         }
     }
+    // copy kernel when the sink is pinned host or device memory on 16-byte
+    // boundaries (frames are a multiple of four floats); else the copy engine
+    bool by_kernel = copies && c->frame_floats % 4 == 0;
+    float* dev_sink[2] = {nullptr, nullptr};  // the sink as the device addresses it
+    for (int o = 0; o < 2 && by_kernel; o++) {
+        float* p = o == 0 ? sink->pha : sink->amp;
+        if (!p) continue;
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+            cudaGetLastError();
+            by_kernel = false;
+            continue;
+        }
+        const bool reachable = pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeHost ||
+                               pa.type == cudaMemoryTypeManaged;
+        dev_sink[o] = static_cast<float*>(pa.devicePointer);
+        if (!reachable || !dev_sink[o] || (reinterpret_cast<uintptr_t>(dev_sink[o]) & 15) != 0) by_kernel = false;
+    }
     long s = 0;
     int b = 0;
     while (s < nsteps) {
@@ -1049,12 +1067,19 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
                 AW_CUDA(cudaStreamWaitEvent(c->out_st, c->ev_written[slot], 0));
                 const long hs = sink->nslots > 0 ? (s + i) % sink->nslots : (s + i);
                 const size_t ff = c->frame_floats;
-                if (sink->pha)
-                    AW_CUDA(cudaMemcpyAsync(sink->pha + (size_t)hs * ff, c->d_out_pha + slot * ff, sizeof(float) * ff,
-                                            cudaMemcpyDefault, c->out_st));
-                if (sink->amp)
-                    AW_CUDA(cudaMemcpyAsync(sink->amp + (size_t)hs * ff, c->d_out_amp + slot * ff, sizeof(float) * ff,
-                                            cudaMemcpyDefault, c->out_st));
+                if (by_kernel) {
+                    auto f4 = [](const float* q) { return reinterpret_cast<const float4*>(q); };
+                    auto h4 = [&](float* q) { return q ? reinterpret_cast<float4*>(q + (size_t)hs * ff) : nullptr; };
+                    AW_CUDA(copy_out(f4(c->d_out_pha + slot * ff), h4(dev_sink[0]), (long)(ff / 4),
+                                     f4(c->d_out_amp + slot * ff), h4(dev_sink[1]), (long)(ff / 4), c->out_st));
+                } else {
+                    if (sink->pha)
+                        AW_CUDA(cudaMemcpyAsync(sink->pha + (size_t)hs * ff, c->d_out_pha + slot * ff, sizeof(float) * ff,
+                                                cudaMemcpyDefault, c->out_st));
+                    if (sink->amp)
+                        AW_CUDA(cudaMemcpyAsync(sink->amp + (size_t)hs * ff, c->d_out_amp + slot * ff, sizeof(float) * ff,
+                                                cudaMemcpyDefault, c->out_st));
+                }
                 AW_CUDA(cudaEventRecord(c->ev_copied[slot], c->out_st));
             }
         }
