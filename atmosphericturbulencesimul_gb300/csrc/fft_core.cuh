@@ -26,10 +26,15 @@ namespace atmwfs {
 
 // Complex add / subtract.  On sm_100 and later the (re, im) pair is one
 // packed FP32x2 operation (per component the same IEEE rounding as the
-// scalar form; a - b as the exact b * (-1) + a).
+// scalar form; a - b as the exact b * (-1) + a).  A translation unit whose
+// kernels run faster with scalar butterflies defines AW_SCALAR_BUTTERFLY
+// before including this header (the results are the same either way).
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000 && !defined(AW_SCALAR_BUTTERFLY)
+#define AW_PACKED_BUTTERFLY 1
+#endif
 AW_HD float2 cadd(float2 a, float2 b)
 {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+#if defined(AW_PACKED_BUTTERFLY)
     return __fadd2_rn(a, b);
 #else
     return make_float2(a.x + b.x, a.y + b.y);
@@ -37,7 +42,7 @@ AW_HD float2 cadd(float2 a, float2 b)
 }
 AW_HD float2 csub(float2 a, float2 b)
 {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+#if defined(AW_PACKED_BUTTERFLY)
     return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
 #else
     return make_float2(a.x - b.x, a.y - b.y);
