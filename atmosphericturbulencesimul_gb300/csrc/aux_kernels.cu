@@ -181,12 +181,17 @@ __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restric
     __shared__ int s_cnt[2];
     const double kTwoPi = 2.0 * 3.14159265358979323846;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        // (float)atan2((double)im, (double)re) without FP64 (atan_ff.cuh)
-        const float v = atan2_ff(I.bins[n + i], I.bins[i], atan_tab);
+        // the fixed-point sums back to float (one rounding; the scaling by
+        // 2^-kBinFrac is exact), then (float)atan2((double)im, (double)re)
+        // without FP64 (atan_ff.cuh)
+        const float q = 1.0f / (float)(1ull << kBinFrac);
+        const float re = __ll2float_rn((long long)I.bins[i]) * q;
+        const float im = __ll2float_rn((long long)I.bins[n + i]) * q;
+        const float v = atan2_ff(im, re, atan_tab);
         pb[i] = v;
         ppf[i] = __double2float_rd((double)v + kTwoPi * 0.5);
-        I.bins[i] = 0.0f;
-        I.bins[n + i] = 0.0f;
+        I.bins[i] = 0ull;
+        I.bins[n + i] = 0ull;
     }
     if (threadIdx.x < 2) { s_max[threadIdx.x] = 0u; s_cnt[threadIdx.x] = 0; }
     __syncthreads();

@@ -592,7 +592,7 @@ atmwfs_status autotune(atmwfs_ctx* c)
     cudaEventDestroy(e1);
     if (s != ATMWFS_OK) return s;
     for (const InstDev& d : c->hinst)
-        if (d.bins) AW_CUDA(cudaMemsetAsync(d.bins, 0, sizeof(float) * 2 * (d.nb * d.nb > 0 ? d.nb * d.nb : 1), c->st));
+        if (d.bins) AW_CUDA(cudaMemsetAsync(d.bins, 0, sizeof(*d.bins) * 2 * (d.nb * d.nb > 0 ? d.nb * d.nb : 1), c->st));
     AW_CUDA(cudaStreamSynchronize(c->st));
     return check_status(c);
 }
@@ -808,8 +808,8 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                 if (I.mode == ATMWFS_MODE_SCI) {
                     d.nb = No / 20;
                     const int nb2 = d.nb * d.nb > 0 ? d.nb * d.nb : 1;
-                    CK(dalloc(c, (void**)&d.bins, sizeof(float) * 2 * nb2));
-                    CKC(cudaMemset(d.bins, 0, sizeof(float) * 2 * nb2));
+                    CK(dalloc(c, (void**)&d.bins, sizeof(*d.bins) * 2 * nb2));
+                    CKC(cudaMemset(d.bins, 0, sizeof(*d.bins) * 2 * nb2));
                     CK(dalloc(c, (void**)&d.peak, sizeof(float) * nb2));
                     // bin of each output coordinate, as the reference computes it
                     // (long)(1.0 * ii / Wout * nb), and the first coordinate of each bin

@@ -10,6 +10,11 @@
 namespace atmwfs {
 
 constexpr int kMaxLayers = 16;
+// Fractional bits of the fixed-point science bin sums.  A bin is under 40
+// pixels wide (nb = Wout / 20 rounded down, Wout >= 20), so it sums fewer
+// than 1,600 unit phasors per step: |sum| < 2^11 and sum * 2^50 < 2^61 stays
+// inside a signed 64-bit integer.
+constexpr int kBinFrac = 50;
 
 // Integer and fractional sample position of one layer window for one
 // instance at one step, in the screen's own (untransposed) frame:
@@ -29,7 +34,10 @@ struct InstDev {
     float* out_amp;
     long ostride;              // floats between output slots (the frames of all instances)
     float* phisum;             // geometric phase sum of the crop [Nout*Nout] (k_phasum)
-    float* bins;               // science scratch: [2][nb*nb] (re, im) sums
+    // science scratch: [2][nb*nb] (re, im) sums in fixed point, units of
+    // 2^-kBinFrac (integer sums are order-free, so the totals do not depend
+    // on the order in which CTAs add their parts)
+    unsigned long long* bins;
     float* peak;               // science scratch: unwrapped bin phase [nb*nb]
     const short* binx;         // bin index of each output coordinate [Nout]
     const short* binx0;        // first output coordinate of each bin [nb + 1]

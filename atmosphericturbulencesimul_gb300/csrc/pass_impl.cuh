@@ -490,7 +490,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
             __syncthreads();
             const int nj = binx[yb - 1 - off] - jb0 + 1;
             const short* __restrict__ bx0 = I->binx0;
-            float* __restrict__ gb = I->bins;
+            unsigned long long* __restrict__ gb = I->bins;
             for (int k = tid; k < nj * nb; k += NT) {
                 const int j = k / nb, ib = k % nb;
                 float sr = 0.0f, si = 0.0f;
@@ -499,8 +499,11 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                     sr += z.x;
                     si += z.y;
                 }
-                atomicAdd(&gb[(jb0 + j) * nb + ib], sr);
-                atomicAdd(&gb[nb * nb + (jb0 + j) * nb + ib], si);
+                // fixed point (exact scaling by 2^kBinFrac, then the nearest
+                // integer): integer additions give the same totals in any order
+                const float q = (float)(1ull << kBinFrac);
+                atomicAdd(&gb[(jb0 + j) * nb + ib], (unsigned long long)__float2ll_rn(sr * q));
+                atomicAdd(&gb[nb * nb + (jb0 + j) * nb + ib], (unsigned long long)__float2ll_rn(si * q));
             }
         }
         return;

@@ -1,10 +1,10 @@
 """Frames delivered through atmwfs_run into the three kinds of sink: pageable
 host arrays (copy engine), pinned host memory and device memory (the copy
 kernel).  The same seeded series gives bit-identical frames in all three,
-with a host ring shorter than the run (frames reused round-robin).  The
-series is a lambda-ref one: its frames are a deterministic function of the
-inputs (science frames go through bin sums accumulated by float atomics,
-whose order may change the last bit of a bin between runs)."""
+with a host ring shorter than the run (frames reused round-robin).  Every
+frame is a deterministic function of the inputs (the science bins are summed
+in fixed point, so the order in which CTAs add their parts does not matter),
+so the three runs, λref and science instances alike, agree bit for bit."""
 import numpy as np
 import pytest
 
@@ -26,7 +26,7 @@ def _series(case, screens):
 def test_sinks_give_identical_frames(lib, oracle64):
     torch = pytest.importorskip("torch")
     case = Case(alt=[0.0, 1000.0, 5000.0], cn2=[0.6, 0.3, 0.1], speed=[8.0, 12.0, 20.0], direction=[0.0, 1.0, 2.5],
-                sci=[])
+                sci=[(1.6e-6, 0.0, 0.0), (2.2e-6, 1e-5, 0.0)])
     screens = make_screens(case, oracle64)
     nsteps, nslots = 5, 3
     out = {}
