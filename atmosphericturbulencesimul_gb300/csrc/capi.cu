@@ -543,6 +543,16 @@ atmwfs_status launch_step(atmwfs_ctx* c)
 
 atmwfs_status check_status(atmwfs_ctx* c);
 
+// Zero the science bins on the engine stream: a last pass launched outside a
+// step (timing, tuning) adds its bin sums, which the next step's unwrap
+// would otherwise read.
+atmwfs_status clear_bins(atmwfs_ctx* c)
+{
+    for (const InstDev& d : c->hinst)
+        if (d.bins) AW_CUDA(cudaMemsetAsync(d.bins, 0, sizeof(*d.bins) * 2 * (d.nb * d.nb > 0 ? d.nb * d.nb : 1), c->st));
+    return ATMWFS_OK;
+}
+
 // Project autotuner: for every grid class time the representative pass
 // (a middle pass when there is one) in each tile configuration and keep the
 // fastest.  ATMWFS_TILE_CFG=<k> forces configuration k.  Science bins are
@@ -591,8 +601,7 @@ atmwfs_status autotune(atmwfs_ctx* c)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (s != ATMWFS_OK) return s;
-    for (const InstDev& d : c->hinst)
-        if (d.bins) AW_CUDA(cudaMemsetAsync(d.bins, 0, sizeof(*d.bins) * 2 * (d.nb * d.nb > 0 ? d.nb * d.nb : 1), c->st));
+    AW_TRY(clear_bins(c));
     AW_CUDA(cudaStreamSynchronize(c->st));
     return check_status(c);
 }
@@ -1203,6 +1212,7 @@ atmwfs_status atmwfs_time_pass(atmwfs_ctx* c, int k, int ci, int reps, double* m
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (s != ATMWFS_OK) return s;
+    if (k == (int)c->plane_lo.size()) AW_TRY(clear_bins(c));  // the last pass accumulated science bins
     if (ms) *ms = t / reps;
     if (bytes) *bytes = b;
     if (n) *n = cl.N;

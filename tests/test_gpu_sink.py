@@ -23,7 +23,15 @@ def _series(case, screens):
     return s
 
 
-def test_sinks_give_identical_frames(lib, oracle64):
+@pytest.fixture
+def fixed_tiles(monkeypatch):
+    """One tile configuration for every series of a test: the autotuner of
+    each series could otherwise pick another shape, which groups the
+    per-CTA parts of the science bins differently."""
+    monkeypatch.setenv("ATMWFS_TILE_CFG", "2")
+
+
+def test_sinks_give_identical_frames(lib, oracle64, fixed_tiles):
     torch = pytest.importorskip("torch")
     case = Case(alt=[0.0, 1000.0, 5000.0], cn2=[0.6, 0.3, 0.1], speed=[8.0, 12.0, 20.0], direction=[0.0, 1.0, 2.5],
                 sci=[(1.6e-6, 0.0, 0.0), (2.2e-6, 1e-5, 0.0)])
@@ -51,3 +59,25 @@ def test_sinks_give_identical_frames(lib, oracle64):
     for kind in ("pinned", "device"):
         assert np.array_equal(out[kind][0], ref_pha), kind
         assert np.array_equal(out[kind][1], ref_amp), kind
+
+
+def test_time_pass_leaves_the_series_unchanged(lib, oracle64, fixed_tiles):
+    """Timing every pass of every grid class between two runs (the last pass
+    included, which adds science bin sums) leaves the following frames equal
+    to those of a series that was not timed."""
+    case = Case(alt=[0.0, 1000.0, 5000.0], cn2=[0.6, 0.3, 0.1], speed=[8.0, 12.0, 20.0], direction=[0.0, 1.0, 2.5],
+                sci=[(1.6e-6, 0.0, 0.0), (2.2e-6, 1e-5, 0.0)])
+    screens = make_screens(case, oracle64)
+    a, b = _series(case, screens), _series(case, screens)
+    fa = a.run_frames(4)
+    fb1 = b.run_frames(2)
+    nplanes = len(b.planes()[0])
+    for c in range(b.num_classes()):
+        for k in range(nplanes + 1):
+            b.time_pass(k, c, reps=2)
+    fb2 = b.run_frames(2)
+    a.close()
+    b.close()
+    for (pa, aa), (p1, a1), (p2, a2) in zip(fa, fb1, fb2):
+        assert np.array_equal(pa[:2], p1) and np.array_equal(aa[:2], a1)
+        assert np.array_equal(pa[2:], p2) and np.array_equal(aa[2:], a2)
