@@ -133,6 +133,7 @@ SIGNATURES = [
     ("atmwfs_destroy", None, [_ctx]),
     ("atmwfs_load_screen", C.c_int, [_ctx, C.c_int, _fp, C.c_long]),
     ("atmwfs_load_screen_dev", C.c_int, [_ctx, C.c_int, C.c_void_p, C.c_long]),
+    ("atmwfs_read_screen", C.c_int, [_ctx, C.c_int, C.c_void_p]),
     ("atmwfs_normalize_screens", C.c_int, [_ctx, C.c_float, C.c_float, _dp]),
     ("atmwfs_normalize_screens_ext", C.c_int, [_ctx, C.c_float, C.c_float, C.POINTER(_fp), C.c_long, _dp]),
     ("atmwfs_run", C.c_int, [_ctx, C.c_long, C.POINTER(Sink)]),

@@ -939,6 +939,17 @@ atmwfs_status atmwfs_load_screen_dev(atmwfs_ctx* c, int layer, const float* dev,
     return load_common(c, layer, dev, M, cudaMemcpyDeviceToDevice);
 }
 
+atmwfs_status atmwfs_read_screen(atmwfs_ctx* c, int layer, float* host)
+{
+    if (!c || !host) return fail(ATMWFS_ERR_INVALID, "null argument");
+    if (layer < 0 || layer >= c->L) return fail(ATMWFS_ERR_INVALID, "layer %d out of range", layer);
+    if (!c->loaded[layer]) return fail(ATMWFS_ERR_STATE, "screen of layer %d not loaded", layer);
+    AW_CUDA(cudaMemcpyAsync(host, c->d_screen[layer], sizeof(float) * (size_t)c->M * c->M, cudaMemcpyDeviceToHost,
+                            c->st));
+    AW_CUDA(cudaStreamSynchronize(c->st));
+    return ATMWFS_OK;
+}
+
 atmwfs_status atmwfs_normalize_screens(atmwfs_ctx* c, float lambda_ref, float seeing, double* r0_pix)
 {
     return atmwfs_normalize_screens_ext(c, lambda_ref, seeing, nullptr, 0, r0_pix);

@@ -17,8 +17,6 @@
 
 namespace atmwfs {
 void set_error_message(const char* msg);
-int twiddle_count(int N);
-void twiddle_fill(int N, float2* out);
 }
 
 namespace {
@@ -28,7 +26,7 @@ using namespace atmwfs;
 constexpr long kMaxN = ATMWFS_NOALLOC_MAX_N;
 constexpr long kMaxTw = 2 * kMaxN;  // stage twiddle tables of the largest grid
 constexpr int kMaxDevices = 64;
-const double kPi = 3.14159265358979323846264338328;
+constexpr double kPi = 3.14159265358979323846264338328;
 
 // Scratch shared by every call on a device: the field after the first
 // (transposed) pass, the 1-D transfer table and the twiddles of the call's
@@ -72,6 +70,58 @@ atmwfs_status scratch_for_current_device(Scratch** out)
     return ATMWFS_OK;
 }
 
+// One thread per entry of the call's tables, evaluated in double like the
+// host tables of the allocating path:
+//   table[k] = exp(-i c f_k^2) / n, f_k the centred frequency of unshifted
+//   index k, the angle reduced to [-pi, pi] in double before the cosine and
+//   sine (Fresnel_propagate_wavefront, WFpropagate.c:68-152);
+//   twiddles: for each order (o = 0, 1) and stage st >= 1 of the size's plan,
+//   tab[r * ns + k] = exp(-2 pi i k r / (ns R)) at offset tw_offset(o, st).
+template <int N>
+__global__ void k_noalloc_tables(double coeff)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < N) {
+        const long f = j < N / 2 ? j : j - N;
+        double ang = -coeff * (double)(f * f);
+        ang -= 2.0 * kPi * nearbyint(ang / (2.0 * kPi));
+        g_table[j] = make_float2((float)(cos(ang) / N), (float)(sin(ang) / N));
+        return;
+    }
+    const int i = j - N;
+    if (i >= tw_total<N>()) return;
+    for (int o = 0; o < 2; o++)
+        for (int st = 1; st < Stages<N>::S; st++) {
+            const int base = tw_offset<N>(o, st);
+            const int R = stage_radix<N>(st, o), ns = stage_ns<N>(st, o);
+            if (i < base || i >= base + R * ns) continue;
+            const int r = (i - base) / ns, k = (i - base) % ns;
+            const double a = -2.0 * kPi * (double)(k * r) / (double)(ns * R);
+            g_twiddle[i] = make_float2((float)cos(a), (float)sin(a));
+            return;
+        }
+}
+
+template <int N>
+cudaError_t launch_tables_n(double coeff, cudaStream_t cs)
+{
+    if (tw_total<N>() > kMaxTw) return cudaErrorInvalidValue;  // the static twiddle array is too small
+    const int total = N + tw_total<N>();
+    k_noalloc_tables<N><<<(total + 255) / 256, 256, 0, cs>>>(coeff);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tables(long n, double coeff, cudaStream_t cs)
+{
+    switch (n) {
+        case 64: return launch_tables_n<64>(coeff, cs);
+        case 128: return launch_tables_n<128>(coeff, cs);
+        case 256: return launch_tables_n<256>(coeff, cs);
+        case 512: return launch_tables_n<512>(coeff, cs);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 }  // namespace
 
 extern "C" atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long n, double dx, double z, double lambda,
@@ -88,23 +138,12 @@ extern "C" atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long 
     atmwfs_status st = scratch_for_current_device(&s);
     if (st != ATMWFS_OK) return st;
     cudaStream_t cs = (cudaStream_t)stream;
-    // transfer table and twiddles of this size, built on the stack (the same
-    // formulas as the allocating path) and copied into the static arrays
-    float2 h[kMaxN], tw[kMaxTw];
+    // transfer table and twiddles of this size, written into the static
+    // arrays by a kernel on the caller's stream: nothing is copied from host
+    // memory, so the call does not wait for the stream to drain
     const double coeff = kPi * z * lambda / (dx * (double)n) / (dx * (double)n);
-    for (long k = 0; k < n; k++) {
-        const long f = k < n / 2 ? k : k - n;
-        double ang = -coeff * (double)(f * f);
-        ang -= 2.0 * kPi * nearbyint(ang / (2.0 * kPi));
-        h[k] = make_float2((float)(cos(ang) / n), (float)(sin(ang) / n));
-    }
-    const int ntw = twiddle_count((int)n);
-    if (ntw > kMaxTw) return err(ATMWFS_ERR_INVALID, "twiddle tables exceed the static scratch");
-    twiddle_fill((int)n, tw);
-    // pageable sources: each copy is staged before the call returns
-    if (cudaMemcpyAsync(s->table, h, sizeof(float2) * n, cudaMemcpyHostToDevice, cs) != cudaSuccess ||
-        cudaMemcpyAsync(s->twiddle, tw, sizeof(float2) * ntw, cudaMemcpyHostToDevice, cs) != cudaSuccess)
-        return err(ATMWFS_ERR_CUDA, "copy of the transfer table failed");
+    cudaError_t e = launch_tables(n, coeff, cs);
+    if (e != cudaSuccess) return err(ATMWFS_ERR_CUDA, cudaGetErrorString(e));
     const PassLauncher fn = pass_launcher((int)n);
     PassArgs a;
     memset(&a, 0, sizeof a);
@@ -113,7 +152,7 @@ extern "C" atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long 
     a.ext_in = (const float2*)in;
     a.ext_out = s->field;
     const dim3 grid((unsigned)(n / rows_per_cta((int)n)), 1);
-    cudaError_t e = fn(kVarUnitProp, grid, a, nullptr, s->twiddle, cs);
+    e = fn(kVarUnitProp, grid, a, nullptr, s->twiddle, cs);
     if (e == cudaSuccess) {
         a.ext_in = s->field;
         a.ext_out = (float2*)out;

@@ -105,6 +105,13 @@ class Series:
     def load_screen_dev(self, layer: int, ptr: int, M: int) -> None:
         check(self._lib.atmwfs_load_screen_dev(self._ctx, layer, C.c_void_p(ptr), M))
 
+    def read_screen(self, layer: int) -> np.ndarray:
+        """The layer's screen as the frames use it (renormalised and weighted
+        once normalize() has run)."""
+        out = np.empty((self.master_size, self.master_size), np.float32)
+        check(self._lib.atmwfs_read_screen(self._ctx, layer, _f32p(out)))
+        return out
+
     def normalize(self, lambda_ref: float, seeing_arcsec: float) -> tuple[float, float]:
         r0 = np.zeros(2)
         check(self._lib.atmwfs_normalize_screens(self._ctx, lambda_ref, seeing_arcsec, _f64p(r0)))

@@ -100,6 +100,11 @@ void atmwfs_destroy(atmwfs_ctx* ctx);
 atmwfs_status atmwfs_load_screen(atmwfs_ctx* ctx, int layer, const float* host, long M);
 atmwfs_status atmwfs_load_screen_dev(atmwfs_ctx* ctx, int layer, const float* dev, long M);
 
+/* Copy of the screen of layer `layer` as the frames use it (M x M floats
+ * into `host`): after atmwfs_normalize_screens it carries the r0 scale and
+ * the Cn2 weight, as the reference's image of that layer does after :2363. */
+atmwfs_status atmwfs_read_screen(atmwfs_ctx* ctx, int layer, float* host);
+
 /* r0 measurement and renormalisation of the loaded screens, then the
  * per-layer sqrt(Cn2 / cos(zenith)) weights (:2240-2363).  lambda_ref [m]
  * and seeing [arcsec] are TURBULENCE_REF_WAVEL and TURBULENCE_SEEING.
@@ -197,9 +202,11 @@ atmwfs_status atmwfs_fresnel_dev(const void* in, void* out, long n, double dx, d
  * sized for n <= ATMWFS_NOALLOC_MAX_N (2 MiB per GPU that loads the library,
  * kept until exit); larger n is rejected with ATMWFS_ERR_INVALID.  The first
  * call on a device looks the arrays up on that device, so make it before any
- * stream capture.  Every call shares the arrays, which keep the last call's
- * contents (the first pass overwrites the whole region the second reads):
- * calls that overlap on the GPU race, so issue them on one stream. */
+ * stream capture.  The call's transfer table and twiddles are written into
+ * the arrays by a kernel on `stream`; nothing is copied from host memory.
+ * Every call shares the arrays, which keep the last call's contents (the
+ * first pass overwrites the whole region the second reads): calls that
+ * overlap on the GPU race, so issue them on one stream. */
 #define ATMWFS_NOALLOC_MAX_N 512
 atmwfs_status atmwfs_fresnel_noalloc(const void* in, void* out, long n, double dx, double z, double lambda,
                                      void* stream);

@@ -1,7 +1,10 @@
 #!/usr/bin/env python3
 """Build the checker binary oracle/_ref/atmref from the reference's own C
-sources (read in place under /root/reference/src) and the shims of this
+sources (read in place under <reference root>/src) and the shims of this
 directory (FFTW, cfitsio, GSL/libc noise, ncurses stand-ins).
+
+The reference root is the first argument, else $ATMWFS_REFERENCE_ROOT, else
+/root/reference.
 
 Reference functions that the hot path never calls but that the compiled
 modules reference are linked to generated stubs that abort if called.
@@ -9,13 +12,23 @@ Nothing is written outside oracle/_ref/.
 """
 from __future__ import annotations
 
+import os
 import re
 import subprocess
 import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF = Path("/root/reference/src")
+
+
+def reference_root() -> Path:
+    """Where the reference checkout lies (argument, environment, default)."""
+    if len(sys.argv) > 1 and __name__ == "__main__":
+        return Path(sys.argv[1])
+    return Path(os.environ.get("ATMWFS_REFERENCE_ROOT", "/root/reference"))
+
+
+REF = reference_root() / "src"
 OUT = HERE.parent / "_ref"
 
 # modules on the mkwfs path, the PSF consumers and their direct dependencies

@@ -20,7 +20,20 @@ struct atmref_plan {
     long idist, odist;
 };
 
-static void fft1(double *re, double *im, long n, int sign)
+/* Twiddles of every radix-2 level of a length-n transform, evaluated with the
+ * same expression as inline (so the values are bit-identical): level len
+ * keeps exp(sign 2 pi i k / len), k < len/2, at [len/2 + k]. */
+static void twiddles(double *wr, double *wi, long n, int sign)
+{
+    for (long len = 2; len <= n; len <<= 1)
+        for (long k = 0; k < len / 2; k++) {
+            double a = sign * 2.0 * M_PI * (double)k / (double)len;
+            wr[len / 2 + k] = cos(a);
+            wi[len / 2 + k] = sin(a);
+        }
+}
+
+static void fft1(double *re, double *im, long n, int sign, const double *twr, const double *twi)
 {
     if (n <= 1) return;
     if ((n & (n - 1)) == 0) {
@@ -36,8 +49,7 @@ static void fft1(double *re, double *im, long n, int sign)
         for (long len = 2; len <= n; len <<= 1) {
             for (long i = 0; i < n; i += len)
                 for (long k = 0; k < len / 2; k++) {
-                    double a = sign * 2.0 * M_PI * (double)k / (double)len;
-                    double wr = cos(a), wi = sin(a);
+                    double wr = twr[len / 2 + k], wi = twi[len / 2 + k];
                     long p = i + k, q = i + k + len / 2;
                     double tr = re[q] * wr - im[q] * wi, ti = re[q] * wi + im[q] * wr;
                     re[q] = re[p] - tr; im[q] = im[p] - ti;
@@ -65,13 +77,17 @@ static void fft1(double *re, double *im, long n, int sign)
 static void fft2(double *re, double *im, long n0, long n1, int sign)
 {
     double *cr = malloc(sizeof(double) * n0), *ci = malloc(sizeof(double) * n0);
-    for (long r = 0; r < n0; r++) fft1(re + r * n1, im + r * n1, n1, sign);
+    double *t1r = malloc(sizeof(double) * (n1 + 1)), *t1i = malloc(sizeof(double) * (n1 + 1));
+    double *t0r = malloc(sizeof(double) * (n0 + 1)), *t0i = malloc(sizeof(double) * (n0 + 1));
+    if ((n1 & (n1 - 1)) == 0) twiddles(t1r, t1i, n1, sign);
+    if ((n0 & (n0 - 1)) == 0) twiddles(t0r, t0i, n0, sign);
+    for (long r = 0; r < n0; r++) fft1(re + r * n1, im + r * n1, n1, sign, t1r, t1i);
     for (long c = 0; c < n1; c++) {
         for (long r = 0; r < n0; r++) { cr[r] = re[r * n1 + c]; ci[r] = im[r * n1 + c]; }
-        fft1(cr, ci, n0, sign);
+        fft1(cr, ci, n0, sign, t0r, t0i);
         for (long r = 0; r < n0; r++) { re[r * n1 + c] = cr[r]; im[r * n1 + c] = ci[r]; }
     }
-    free(cr); free(ci);
+    free(cr); free(ci); free(t1r); free(t1i); free(t0r); free(t0i);
 }
 
 static struct atmref_plan *mk(int kind, int prec, int rank, const int *n, int howmany, void *in, void *out, int sign,

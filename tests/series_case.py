@@ -25,7 +25,9 @@ class Case:
     zangle: float = 0.0
     lam_ref: float = 0.5e-6
     seeing: float = 0.6875
-    sci: list = field(default_factory=lambda: [(1.6e-6, 0.0, 0.0)])  # (lambda, src_x, src_y)
+    # science instances: (lambda, src_x, src_y) on the case's grid, or
+    # (lambda, src_x, src_y, W, Wout) on a grid of their own
+    sci: list = field(default_factory=lambda: [(1.6e-6, 0.0, 0.0)])
     ref: bool = True
     amplitude: int = 1
     fresnel: int = 1
@@ -63,9 +65,11 @@ def instances(case: Case):
     if case.ref:
         mode = MODE_REF if case.amplitude else MODE_PHASE
         out.append(InstanceSpec(lam=float(np.float32(case.lam_ref)), mode=mode, wf_raw_size=case.W, wf_size=case.Wout))
-    for lam, sx, sy in case.sci:
+    for entry in case.sci:
+        lam, sx, sy = entry[:3]
+        W, Wout = (entry[3], entry[4]) if len(entry) > 3 else (case.W, case.Wout)
         mode = MODE_SCI if case.amplitude else MODE_PHASE
-        out.append(InstanceSpec(lam=lam, mode=mode, src_x=sx, src_y=sy, wf_raw_size=case.W, wf_size=case.Wout,
+        out.append(InstanceSpec(lam=lam, mode=mode, src_x=sx, src_y=sy, wf_raw_size=W, wf_size=Wout,
                                 scoeff=scoeff_for(case, lam)))
     return out
 
@@ -102,12 +106,12 @@ def run_oracle(case: Case, o64, screens, nsteps: int):
             orc.step_positions(st[0], st[1], st[2], st[3], st[4], st[5], case.dt, case.M)
             sc = None if I.scoeff is None else I.scoeff.astype(np.float64)
             phasum, fld = o64.frame(screens, st[0], st[1], sc, sidx, salt, float(np.float32(case.pupil)),
-                                    float(np.float32(case.zangle)), I.lam, case.W, case.amplitude, case.fresnel)
+                                    float(np.float32(case.zangle)), I.lam, I.wf_raw_size, case.amplitude, case.fresnel)
             from atmosphericturbulencesimul_gb300 import MODE_SCI
             if I.mode == MODE_SCI:
-                pha, amp, _, _ = o64.output_sci(phasum, fld, case.Wout, case.amplitude)
+                pha, amp, _, _ = o64.output_sci(phasum, fld, I.wf_size, case.amplitude)
             else:
-                pha, amp = o64.output_ref(phasum, fld, case.Wout, case.amplitude)
+                pha, amp = o64.output_ref(phasum, fld, I.wf_size, case.amplitude)
             step.append((pha, amp))
         res.append(step)
     final_pos = [(st[0].copy(), st[1].copy()) for st in states]
@@ -130,3 +134,42 @@ def metrics(pha_g, amp_g, pha_o, amp_o, lam):
         "opd_rms_rel": float(abs(opd_g.std() - opd_o.std()) / max(opd_o.std(), 1e-30)),
         "amp_var_rel": float(abs(amp_g.var() - amp_o.var()) / max(amp_o.var(), 1e-30)),
     }
+
+
+def compare(case: Case, o64, nsteps: int, wrapped_nm: float = 0.05, flip: float = 2e-3, amp_var: float = 1e-3,
+            screens=None):
+    """Run `case` for `nsteps` on the GPU and in the FP64 oracle from the same
+    screens and assert the parity bars on every frame:
+      * layer positions equal bit for bit (the reference's sequential update);
+      * wrapped phase error < `wrapped_nm` nm rms, amplitude error < 2e-3;
+      * a 2 pi jump of the unwrapped phase on fewer than `flip` of the pixels;
+      * relative OPD rms within 1e-4 (frames without a jump), relative
+        amplitude variance within `amp_var` (frames with a variance above 1e-6).
+    Returns the metrics of every frame, with the instance's grid and step."""
+    if screens is None:
+        screens = make_screens(case, o64)
+    inst_g, frames, pos_g, _ = run_gpu(case, screens, nsteps)
+    inst_o, res, pos_o, _ = run_oracle(case, o64, screens, nsteps)
+    for (xg, yg), (xo, yo) in zip(pos_g, pos_o):
+        assert np.array_equal(xg, xo) and np.array_equal(yg, yo)
+    out = []
+    for i, I in enumerate(inst_g):
+        for s in range(nsteps):
+            pha_g, amp_g = frames[i][0][s], frames[i][1][s]
+            pha_o, amp_o = res[s][i]
+            m = metrics(pha_g, amp_g, pha_o, amp_o, I.lam)
+            m.update(inst=i, step=s, W=I.wf_raw_size, Wout=I.wf_size or I.wf_raw_size, mode=I.mode)
+            out.append(m)
+            assert m["wrapped_rms_nm"] < wrapped_nm, m
+            assert m["amp_max_err"] < 2e-3, m
+            assert m["flip_frac"] < flip, m
+            assert m["opd_rms_rel"] < 1e-4 or m["flip_frac"] > 0, m
+            if amp_o.var() > 1e-6:
+                assert m["amp_var_rel"] < amp_var, m
+    return out
+
+
+def worst(ms: list) -> dict:
+    """Largest value of every error metric over a list of frame metrics."""
+    keys = ["wrapped_rms_nm", "opd_rms_err_nm", "flip_frac", "amp_max_err", "opd_rms_rel", "amp_var_rel"]
+    return {k: max(m[k] for m in ms) for k in keys}

@@ -10,7 +10,7 @@ Tolerances (floating point, FP32 engine vs FP64 oracle):
 import numpy as np
 import pytest
 
-from series_case import Case, make_screens, metrics, run_gpu, run_oracle
+from series_case import Case, compare, make_screens, run_gpu
 
 pytestmark = pytest.mark.gpu
 
@@ -43,26 +43,7 @@ def test_fresnel_matches_oracle(lib, oracle64, n, z, lam):
 
 
 def _compare(case, o64, nsteps, wrapped_nm=0.05, flip=2e-3):
-    screens = make_screens(case, o64)
-    inst_g, frames, pos_g, planes = run_gpu(case, screens, nsteps)
-    inst_o, res, pos_o, _ = run_oracle(case, o64, screens, nsteps)
-    # positions follow the reference's sequential update bit for bit
-    for (xg, yg), (xo, yo) in zip(pos_g, pos_o):
-        assert np.array_equal(xg, xo) and np.array_equal(yg, yo)
-    out = []
-    for i, I in enumerate(inst_g):
-        for s in range(nsteps):
-            pha_g, amp_g = frames[i][0][s], frames[i][1][s]
-            pha_o, amp_o = res[s][i]
-            m = metrics(pha_g, amp_g, pha_o, amp_o, I.lam)
-            out.append(m)
-            assert m["wrapped_rms_nm"] < wrapped_nm, (i, s, m)
-            assert m["amp_max_err"] < 2e-3, (i, s, m)
-            assert m["flip_frac"] < flip, (i, s, m)
-            assert m["opd_rms_rel"] < 1e-4 or m["flip_frac"] > 0, (i, s, m)
-            if amp_o.var() > 1e-6:
-                assert m["amp_var_rel"] < 1e-4 * 10, (i, s, m)
-    return out
+    return compare(case, o64, nsteps, wrapped_nm=wrapped_nm, flip=flip)
 
 
 def test_series_three_planes(lib, oracle64):
