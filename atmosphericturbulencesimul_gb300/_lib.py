@@ -35,6 +35,7 @@ class Instance(C.Structure):
         ("wf_size", C.c_long),
         ("scoeff", C.POINTER(C.c_float)),
         ("roffset", C.POINTER(C.c_double)),
+        ("hop_n", C.POINTER(C.c_double)),
     ]
 
 
@@ -120,6 +121,7 @@ class MkwfsOpts(C.Structure):
         ("seed", C.c_ulonglong),
         ("verbose", C.c_int),
         ("semwait_timeout", C.c_double),
+        ("fresnel_air_index", C.c_int),
     ]
 
 
@@ -212,6 +214,9 @@ SIGNATURES = [
     ("atmwfs_measure_fwhm", C.c_int, [_fp, C.c_long, C.c_long, C.c_float, C.c_float, C.c_float, C.c_long, _fp]),
     ("atmwfs_measure_enc_nrj", C.c_int, [_fp, C.c_long, C.c_long, C.c_float, C.c_float, C.c_float, _fp]),
     ("atmwfs_expoframes", C.c_int, [C.c_char_p, C.c_float, C.c_char_p, _fp, C.c_long, C.c_int, _dp]),
+    ("atmwfs_fno_pointwise_dev", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_long,
+                                           C.c_float, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    ("atmwfs_fno_umma_status", C.c_uint, [C.c_int]),
     ("atmwfs_gemm_bf16", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_int, C.c_void_p,
                                    C.c_long, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_float, C.c_float, C.c_void_p,
                                    C.c_int, C.c_long, C.c_long, C.c_long, C.c_void_p]),

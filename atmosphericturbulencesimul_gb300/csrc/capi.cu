@@ -5,6 +5,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -277,6 +278,10 @@ struct Class {
     int base = 0;              // first slot in the class-ordered InstDev array
     TmaSet maps[kNumTileCfg];  // per configuration: the box height is RR + 3
     double tuned_ms[kNumTileCfg] = {};
+    // windows of the groups whose side is this class's N (the class that
+    // owns the TMA maps of that size computes them), tile configuration 0
+    std::vector<WinJob> jobs;
+    WinJob* d_jobs = nullptr;
 };
 
 }  // namespace atmwfs
@@ -300,6 +305,7 @@ struct atmwfs_ctx {
     std::vector<int> sidx;
     std::vector<int> plane_lo, plane_hi;  // layers [lo, hi)
     std::vector<double> hop_z;            // hop i: plane i -> plane i + 1
+    std::vector<std::vector<double>> hop_n;  // per instance: air index of each hop (1 = vacuum lambda)
     // frozen-flow state [inst * L + layer]
     std::vector<double> xpos, ypos, xpos0, ypos0, vx, vy;
     std::vector<long> xcnt, ycnt;
@@ -312,6 +318,12 @@ struct atmwfs_ctx {
     std::vector<char> loaded;
     bool normalized = false, committed = false;
     std::vector<Class> classes;
+    // window groups: instances whose layer positions are identical at every
+    // step (same start positions and offsets) share the per-step bicubic
+    // windows of the screens; group g has side wg[g] (its largest grid)
+    std::vector<int> group_of;           // global instance -> group
+    std::vector<int> group_leader, wg;
+    std::vector<float*> d_win[2];        // [orient][group * L + layer], or null
     std::vector<InstDev> hinst;          // class order
     std::vector<int> slot_of;            // global index -> class-order slot
     InstDev* d_inst = nullptr;
@@ -376,6 +388,36 @@ void init_positions(atmwfs_ctx* c)
         }
 }
 
+// Window groups: instances with bit-identical start positions and source
+// offsets on every layer move identically at every step (the same updates
+// from the same values), so their bicubic windows are the same samples.
+void make_groups(atmwfs_ctx* c)
+{
+    const int L = c->L;
+    c->group_of.assign(c->ninst, -1);
+    c->group_leader.clear();
+    c->wg.clear();
+    for (int i = 0; i < c->ninst; i++) {
+        for (size_t g = 0; g < c->group_leader.size() && c->group_of[i] < 0; g++) {
+            const int j = c->group_leader[g];
+            bool same = true;
+            for (int l = 0; l < L && same; l++) {
+                const size_t a = (size_t)i * L + l, b = (size_t)j * L + l;
+                same = c->xpos[a] == c->xpos[b] && c->ypos[a] == c->ypos[b] && c->xpos0[a] == c->xpos0[b] &&
+                       c->ypos0[a] == c->ypos0[b];
+            }
+            if (same) c->group_of[i] = (int)g;
+        }
+        if (c->group_of[i] < 0) {
+            c->group_of[i] = (int)c->group_leader.size();
+            c->group_leader.push_back(i);
+            c->wg.push_back(0);
+        }
+        int& w = c->wg[c->group_of[i]];
+        w = std::max(w, (int)c->inst[i].wf_raw_size);
+    }
+}
+
 // One step of the frozen-flow update of every layer of every instance
 // (:2700-2756) and the per-window sample origin (the reference evaluates
 // fmod(pos + ii, M) per pixel; at ii = 0 this gives the window origin).
@@ -437,23 +479,38 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
     const int Q = (int)c->plane_lo.size();
     const int P = Q - 1;
     if (k == 0) {
-        // geometric phase sum of all layers over the crop (k_phasum)
+        // geometric phase sum of all layers over the crop (k_phasum), from
+        // the step's windows
         PassArgs a;
         memset(&a, 0, sizeof a);
         a.inst = c->d_inst + cl.base;
+        a.d_step = c->d_step;
+        a.d_status = c->d_status;
+        a.L = c->L;
+        a.ninst_total = c->ninst;
+        a.poscap = c->poscap;
+        if (bytes) *bytes = (4.0 * c->L + 4.0) * cl.Nout * cl.Nout * cl.members.size();
+        AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarPhasum, dim3(phasum_blocks(cl.Nout), (unsigned)cl.members.size()), a,
+                                        nullptr, nullptr, st));
+        return ATMWFS_OK;
+    }
+    if (k == Q + 1) {
+        // the step's windows of the groups this class computes
+        if (bytes) *bytes = 0;
+        if (cl.jobs.empty()) return ATMWFS_OK;
+        PassArgs a;
+        memset(&a, 0, sizeof a);
         a.pos = c->d_pos;
         a.d_step = c->d_step;
         a.d_status = c->d_status;
         a.L = c->L;
         a.ninst_total = c->ninst;
         a.poscap = c->poscap;
-        // always the configuration-0 tile shape (most rows per tile, least halo)
+        a.jobs = cl.d_jobs;
         const int RR0 = tile_cfg(cl.N, 0).rr;
-        const int off = (cl.N - cl.Nout) / 2;
-        a.row0 = off / RR0 * RR0;
-        const int rows = (off + cl.Nout - a.row0 + RR0 - 1) / RR0 * RR0;
-        if (bytes) *bytes = ((double)rows * cl.N * 4.0 * c->L + 4.0 * cl.Nout * cl.Nout) * cl.members.size();
-        AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarPhasum, dim3(rows / RR0, (unsigned)cl.members.size()), a, &cl.maps[0],
+        // screen tiles in (RR0 + 3 rows of the padded width) and windows out
+        if (bytes) *bytes = (4.0 * (RR0 + 3) / RR0 + 4.0) * (double)cl.N * cl.N * cl.jobs.size();
+        AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarWindows, dim3(cl.N / RR0, (unsigned)cl.jobs.size()), a, &cl.maps[0],
                                         nullptr, st));
         return ATMWFS_OK;
     }
@@ -490,8 +547,8 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
             }
             dim3 grid(rows / cl.RR, (unsigned)cl.members.size());
             if (bytes) {
-                // field read / transposed write (8 B/px each), one screen tile
-                // of the window per gathered layer (4 B/px), outputs
+                // field read / transposed write (8 B/px each), the window rows
+                // of every gathered layer (4 B/px), outputs
                 const double px = (double)cl.N * cl.N, npx = (double)rows * cl.N, cnt = (double)cl.members.size();
                 const int ng = a.g_hi - a.g_lo;
                 double b = 0;
@@ -510,15 +567,18 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
     return ATMWFS_OK;
 }
 
-// One step.  The graph forks: the phase sums (independent of the field) on
-// their own branch, every grid class's chain of passes on its own branch; the
-// last pass of each class waits for the phase sums; everything joins before
-// the science unwrap.
+// One step.  The screen windows of every window group come first; then the
+// graph forks: the phase sums (independent of the field) on their own
+// branch, every grid class's chain of passes on its own branch; the last pass
+// of each class waits for the phase sums; everything joins before the
+// science unwrap.
 atmwfs_status launch_step(atmwfs_ctx* c)
 {
     const int Q = (int)c->plane_lo.size();
     const int nc = (int)c->classes.size();
     cudaEvent_t fork = c->gev[0], sums = c->gev[1];
+    // the step's screen windows, read by the phase sums and by every pass
+    for (Class& cl : c->classes) AW_TRY(launch_pass(c, Q + 1, cl, nullptr, c->st));
     AW_CUDA(cudaEventRecord(fork, c->st));
     AW_CUDA(cudaStreamWaitEvent(c->sum_st, fork, 0));
     for (Class& cl : c->classes) AW_TRY(launch_pass(c, 0, cl, nullptr, c->sum_st));
@@ -626,6 +686,48 @@ atmwfs_status commit(atmwfs_ctx* c)
             AW_CUDA(pad_screen(c->d_screen[l], (int)c->M, c->d_pad[o][l], c->Wp, c->Hp, o, c->st));
         }
     }
+    // windows: the screen orientation of every layer (phase sums, passes in
+    // that orientation), the transposed one of the layers gathered by
+    // transposed passes
+    const int G = (int)c->group_leader.size();
+    for (int o = 0; o < 2; o++) c->d_win[o].resize((size_t)G * c->L, nullptr);
+    for (int g = 0; g < G; g++)
+        for (int o = 0; o < 2; o++)
+            for (int l = 0; l < c->L; l++) {
+                if (o == 1 && !need1[l]) continue;
+                float*& w = c->d_win[o][(size_t)g * c->L + l];
+                if (!w) {
+                    const size_t bytes = sizeof(float) * (size_t)c->wg[g] * c->wg[g];
+                    AW_TRY(dalloc(c, (void**)&w, bytes));
+                    AW_CUDA(cudaMemsetAsync(w, 0, bytes, c->st));
+                }
+            }
+    for (Class& cl : c->classes) {
+        cl.jobs.clear();
+        bool owner = true;  // the first class of each size computes its groups' windows
+        for (const Class& other : c->classes) {
+            if (&other == &cl) break;
+            if (other.N == cl.N) owner = false;
+        }
+        if (!owner) continue;
+        for (int g = 0; g < G; g++) {
+            if (c->wg[g] != cl.N) continue;
+            for (int o = 0; o < 2; o++)
+                for (int l = 0; l < c->L; l++)
+                    if (float* w = c->d_win[o][(size_t)g * c->L + l])
+                        cl.jobs.push_back(WinJob{w, c->group_leader[g], l, o, c->wg[g]});
+        }
+        if (cl.jobs.empty()) continue;
+        if (!cl.d_jobs) AW_TRY(dalloc(c, (void**)&cl.d_jobs, sizeof(WinJob) * cl.jobs.size()));
+        AW_CUDA(cudaMemcpyAsync(cl.d_jobs, cl.jobs.data(), sizeof(WinJob) * cl.jobs.size(), cudaMemcpyHostToDevice, c->st));
+    }
+    for (InstDev& d : c->hinst) {
+        const int g = c->group_of[d.gidx];
+        d.wstride = c->wg[g];
+        for (int o = 0; o < 2; o++)
+            for (int l = 0; l < c->L; l++) d.win[o][l] = c->d_win[o][(size_t)g * c->L + l];
+    }
+    AW_CUDA(cudaMemcpyAsync(c->d_inst, c->hinst.data(), sizeof(InstDev) * c->hinst.size(), cudaMemcpyHostToDevice, c->st));
     for (Class& cl : c->classes) {
         memset(cl.maps, 0, sizeof cl.maps);
         for (int g = 0; g < kNumTileCfg; g++)
@@ -724,7 +826,21 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
     group_superlayers(c->alt, c->cn2, p->fresnel_bin, c->salt, c->sidx);
     build_planes(c->salt, c->sidx, c->amplitude, c->fresnel, c->zangle, c->plane_lo, c->plane_hi, c->hop_z);
     const int P = (int)c->hop_z.size();
+    c->hop_n.assign(c->ninst, std::vector<double>(P, 1.0));
+    for (int i = 0; i < c->ninst; i++) {
+        if (p->inst[i].hop_n)
+            for (int k = 0; k < P; k++) {
+                const double n = p->inst[i].hop_n[k];
+                if (!(n >= 1.0 && n < 2.0)) {
+                    delete c;
+                    return fail(ATMWFS_ERR_INVALID, "instance %d: hop_n[%d] must be in [1, 2)", i, k);
+                }
+                c->hop_n[i][k] = n;
+            }
+        c->inst[i].hop_n = nullptr;
+    }
     init_positions(c);
+    make_groups(c);
 
     atmwfs_status s = ATMWFS_OK;
 #define CK(x)                                  \
@@ -794,7 +910,8 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                 if (P > 0) {
                     std::vector<float2> h((size_t)P * N);
                     for (int hh = 0; hh < P; hh++)
-                        transfer_table(h.data() + (size_t)hh * N, N, (double)c->pupil, c->hop_z[hh], I.lambda);
+                        transfer_table(h.data() + (size_t)hh * N, N, (double)c->pupil, c->hop_z[hh],
+                                       I.lambda / c->hop_n[i][hh]);
                     float2* dh = nullptr;
                     CK(dalloc(c, (void**)&dh, sizeof(float2) * h.size()));
                     CKC(cudaMemcpy(dh, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice));
@@ -1205,7 +1322,7 @@ int atmwfs_num_classes(const atmwfs_ctx* c) { return c ? (int)c->classes.size() 
 atmwfs_status atmwfs_time_pass(atmwfs_ctx* c, int k, int ci, int reps, double* ms, double* bytes, int* n, int* count)
 {
     if (!c || ci < 0 || ci >= (int)c->classes.size()) return fail(ATMWFS_ERR_INVALID, "bad class");
-    if (k < 0 || k > (int)c->plane_lo.size() || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
+    if (k < 0 || k > (int)c->plane_lo.size() + 1 || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
     AW_TRY(commit(c));
     Class& cl = c->classes[ci];
     cudaEvent_t e0, e1;

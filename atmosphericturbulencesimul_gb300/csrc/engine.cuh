@@ -45,6 +45,21 @@ struct InstDev {
     int mode;                  // kModeRef / kModeSci / kModePhase
     int ring;                  // output frames kept on the device
     int gidx;                  // global instance index (positions, scratch)
+    // Bicubic windows of the screens at this step, shared by every instance
+    // whose layer positions are identical (a window group: the wavelengths
+    // of one direction): win[orient][layer] is wstride x wstride floats
+    // (wstride = the largest grid of the group), row-major in the pass
+    // orientation; this instance reads its top-left N x N.  Unit-scale
+    // samples: the pass multiplies by scoeff.
+    const float* win[2][kMaxLayers];
+    int wstride;
+};
+
+// One window of the per-step window kernel: layer `layer` of group leader
+// `gidx` in orientation `orient`, written to `out` with row stride `stride`.
+struct WinJob {
+    float* out;
+    int gidx, layer, orient, stride;
 };
 
 enum : int { kModeRef = 0, kModeSci = 1, kModePhase = 2 };
@@ -60,6 +75,7 @@ enum : int {
     OP_FFT_FWD = 64,   // unit: forward 1-D FFT only
     OP_FFT_INV = 128,  // unit: inverse 1-D FFT only
     OP_PHASUM = 256,   // geometric phase sum of all layers (k_phasum)
+    OP_WINDOWS = 512,  // per-step bicubic windows of the window groups (k_layer_windows)
 };
 
 constexpr int kVarFirst = OP_GATHER | OP_PROP2 | OP_STORE_T;
@@ -70,6 +86,7 @@ constexpr int kVarUnitProp = OP_LOAD | OP_PROP2 | OP_STORE_T;
 constexpr int kVarUnitFwd = OP_LOAD | OP_FFT_FWD | OP_STORE_T;
 constexpr int kVarUnitInv = OP_LOAD | OP_FFT_INV | OP_STORE_T;
 constexpr int kVarPhasum = OP_PHASUM;
+constexpr int kVarWindows = OP_WINDOWS;
 
 // Status bits written by kernels.
 enum : unsigned {
@@ -94,6 +111,8 @@ struct PassArgs {
     float2* ext_out;
     const float2* H1;
     const float2* H2;
+    // window kernel: its jobs (blockIdx.y)
+    const WinJob* jobs;
 };
 
 // Tensor maps of the halo-padded screens: [orientation][layer].
@@ -137,6 +156,14 @@ constexpr TileCfg tile_cfg(int N, int c)
          : N == 1024  ? (c == 0 ? TileCfg{8, 1, false} : c == 1 ? TileCfg{4, 3, false} : TileCfg{4, 4, true})
          : N == 2048  ? (c == 0 ? TileCfg{4, 1, false} : c == 1 ? TileCfg{2, 3, false} : TileCfg{2, 3, true})
                       : TileCfg{0, 0, false};
+}
+
+// Threads of a phase-sum CTA and CTAs per instance of its launch.
+constexpr int kPhasumThreads = 256;
+inline int phasum_blocks(int Nout)
+{
+    const long n = ((long)Nout * Nout + kPhasumThreads - 1) / kPhasumThreads;
+    return (int)(n < 1024 ? n : 1024);
 }
 
 // Rows per CTA of configuration 0 (unit operators).

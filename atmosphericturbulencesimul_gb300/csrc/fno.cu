@@ -53,6 +53,14 @@ struct FnoLayout {
     }
 };
 
+namespace atmwfs {
+// tcgen05 pointwise product (fno_umma.cu)
+bool pointwise_umma_supported(int o, int c);
+cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
+                           const float* bias, float* act, unsigned* status, int swap, cudaStream_t st);
+unsigned* umma_status_ptr();
+}  // namespace atmwfs
+
 struct atmwfs_fno {
     atmwfs_fno_cfg cfg;
     FnoLayout L;
@@ -567,6 +575,24 @@ atmwfs_status spectral_bwd(atmwfs_fno* f, int l, const float* ds, float* dh, int
 // activation, so it is that layer's u.
 const float* last_h(const atmwfs_fno* f) { return f->u[f->cfg.layers - 1]; }
 
+// The pointwise products of the forward pass: on the tcgen05 tensor cores for
+// the shapes compiled there (the Fourier layers' width x width mixing and the
+// first projection), unless ATMWFS_FNO_UMMA=0; the mma.sync product otherwise.
+cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
+                          const float* bias, cudaStream_t st, float* act = nullptr)
+{
+    static const bool use = [] {
+        const char* e = getenv("ATMWFS_FNO_UMMA");
+        return !(e && e[0] == '0');
+    }();
+    if (use && pointwise_umma_supported(o, c)) {
+        unsigned* status = umma_status_ptr();
+        if (!status) return cudaErrorUnknown;
+        return pointwise_umma(W, o, c, X, C, B, P, beta, bias, act, status, 0, st);
+    }
+    return pointwise(W, o, c, X, C, B, P, beta, bias, st, act);
+}
+
 atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st)
 {
     const atmwfs_fno_cfg& c = f->cfg;
@@ -579,10 +605,11 @@ atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStre
         // u = S_l(h) + W_l h + b_l; h' = gelu(u) from the same epilogue
         // (the last layer has no activation: its u is the projection's input)
         FN_TRY(spectral_fwd(f, l, f->h[l], f->u[l], B, st));
-        FN_CUDA(pointwise(pb + f->L.W[l], c.width, c.width, f->h[l], f->u[l], B, P, 1.0f, pf + f->L.b[l], st,
-                          l + 1 < c.layers ? f->h[l + 1] : nullptr));
+        FN_CUDA(pointwise_fwd(pb + f->L.W[l], c.width, c.width, f->h[l], f->u[l], B, P, 1.0f, pf + f->L.b[l], st,
+                              l + 1 < c.layers ? f->h[l + 1] : nullptr));
     }
-    FN_CUDA(pointwise(pb + f->L.proj1_W, c.proj, c.width, last_h(f), f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st, f->q));
+    FN_CUDA(pointwise_fwd(pb + f->L.proj1_W, c.proj, c.width, last_h(f), f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st,
+                          f->q));
     FN_CUDA(pointwise(pb + f->L.proj2_W, c.nout, c.proj, f->q, out, B, P, 0.0f, pf + f->L.proj2_b, st));
     return ATMWFS_OK;
 }

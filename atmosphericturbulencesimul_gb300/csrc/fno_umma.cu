@@ -1,0 +1,339 @@
+// fno_umma.cu -- the surrogate's pointwise channel mixing on the 5th-generation
+// tensor cores (tcgen05 / TMEM):
+//
+//   C[b] (o x P) = W (o x c) X[b] (c x P) + bias[o] (+ beta C[b]);  act = gelu(C)
+//
+// the product of every Fourier layer, the lift and the projection
+// (u = W_l h + b_l in each layer of the network).  It is computed as the
+// transposed product D = X[b]^T W^T, a tile of 128 pixels (the MMA's M) by
+// the o output channels (N), K = c input channels:
+//   * A (128 x c, BF16, K-major): the tile's pixels, read from the FP32
+//     channel planes of X and rounded to BF16 by the CTA's threads while they
+//     store it in the canonical no-swizzle layout (8 x 8 core matrices);
+//   * B (o x c, BF16, K-major): the weights, staged once per CTA;
+//   * D (128 x o, FP32) in tensor memory: lane = pixel, column = channel;
+// one thread issues the c/16 MMAs and commits them to an mbarrier; the four
+// warps read their 32 lanes back with tcgen05.ld and write C as coalesced
+// rows of each channel plane, with the bias, the beta term and the GELU.
+//
+// Every wait is bounded (1 s on %globaltimer): a timeout sets a status bit,
+// the CTA frees its tensor memory and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "atmwfs_fno.h"
+#include "fno_gemm.cuh"
+
+namespace atmwfs {
+void set_error_message(const char* msg);
+
+namespace umma {
+
+constexpr int kM = 128;      // pixels per tile (MMA M, one TMEM lane each)
+constexpr int kThreads = 128;
+constexpr uint64_t kWaitNs = 1000000000ull;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t now_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Shared-memory matrix descriptor, no swizzle, K-major: core matrices of 8
+// rows x 16 bytes; `lbo` = byte distance of core matrices along K, `sbo` =
+// along M/N (8-row groups); bits 46-47 = 1 (descriptor version of sm_100).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;  // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor of kind::f16: D FP32, A and B BF16, both K-major,
+// N = n, M = 128.
+__host__ __device__ constexpr uint32_t instr_desc(int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive TMEM columns of this warp's 32 lanes: register j = column c0 + j.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&r)[32])
+{
+    uint32_t u[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]),
+          "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]),
+          "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; j++) r[j] = __uint_as_float(u[j]);
+}
+
+// Byte offset of element (row, k) in a K-major no-swizzle tile with kc = K/8
+// core matrices per 8-row group (LBO = 128 B, SBO = kc * 128 B).
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int kc)
+{
+    return (uint32_t)((row >> 3) * kc * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+template <int O, int C>
+__global__ void __launch_bounds__(kThreads) k_pointwise(const __nv_bfloat16* __restrict__ W, const float* __restrict__ X,
+                                                        float* __restrict__ Cm, float* __restrict__ act,
+                                                        const float* __restrict__ bias, float beta, long P, int ntiles,
+                                                        unsigned* status, int swap)
+{
+    static_assert(O % 16 == 0 && O >= 32 && O <= 256, "N of the MMA: a multiple of 16 in 32..256");
+    static_assert(C % 16 == 0 && C >= 16, "K: a multiple of 16");
+    constexpr int KC = C / 8;                         // core matrices along K
+    constexpr uint32_t A_BYTES = kM * C * 2;
+    constexpr uint32_t kCols = O <= 32 ? 32 : O <= 64 ? 64 : O <= 128 ? 128 : 256;  // TMEM columns (power of 2)
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char* sa = sm;                           // A tile
+    unsigned char* sb = sm + A_BYTES;                 // B (weights)
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init(&bar);
+    // weights: W is o x c, row-major (K contiguous), element loads (the
+    // parameter blocks carry no alignment guarantee)
+    for (int i = tid; i < O * C; i += kThreads) {
+        const int n = i / C, k = i - n * C;
+        *reinterpret_cast<__nv_bfloat16*>(sb + kmajor_off(n, k, KC)) = W[i];
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t a_addr = smem_addr(sa), b_addr = smem_addr(sb);
+    const long tiles_per_sample = (P + kM - 1) / kM;
+    uint32_t parity = 0;
+
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long b = tile / tiles_per_sample;
+        const long p0 = (tile - b * tiles_per_sample) * kM;
+        const float* xs = X + (size_t)b * C * P;
+        // A: 8 channels of one pixel per 16-byte store; a warp's loads of one
+        // channel are 32 consecutive pixels
+        for (int i = tid; i < kM * KC; i += kThreads) {
+            const int kc = i / kM, m = i - kc * kM;
+            const long p = p0 + m;
+            float f[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) f[j] = p < P ? __ldg(xs + (size_t)(kc * 8 + j) * P + p) : 0.0f;
+            uint4 v;
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(f[0], f[1]), h1 = __floats2bfloat162_rn(f[2], f[3]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(f[4], f[5]), h3 = __floats2bfloat162_rn(f[6], f[7]);
+            v.x = *reinterpret_cast<uint32_t*>(&h0);
+            v.y = *reinterpret_cast<uint32_t*>(&h1);
+            v.z = *reinterpret_cast<uint32_t*>(&h2);
+            v.w = *reinterpret_cast<uint32_t*>(&h3);
+            *reinterpret_cast<uint4*>(sa + kmajor_off(m, kc * 8, KC)) = v;
+        }
+        // the tensor core reads shared memory through the async proxy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fence_before();
+        __syncthreads();
+        fence_after();
+        if (tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < C / 16; ks++) {
+                // K step of 16 = two core matrices along K
+                // LBO: core matrices along K (128 B apart), SBO: along M/N
+                // (KC * 128 B apart); `swap` exchanges the two fields
+                const uint32_t lbo = swap ? KC * 128 : 128, sbo = swap ? 128 : KC * 128;
+                const uint64_t da = smem_desc(a_addr + ks * 256, lbo, sbo);
+                const uint64_t db = smem_desc(b_addr + ks * 256, lbo, sbo);
+                const uint32_t acc = ks > 0 ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                    ::"r"(tmem), "l"(da), "l"(db), "r"(instr_desc(O)), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&bar))
+                         : "memory");
+        }
+        // every thread waits for the products (bounded)
+        const uint64_t t0 = now_ns();
+        int timed_out = 0;
+        while (!mbar_try_wait(&bar, parity)) {
+            if (now_ns() - t0 > kWaitNs) {
+                timed_out = 1;
+                break;
+            }
+        }
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0 && status) atomicOr(status, 1u);
+            break;
+        }
+        parity ^= 1;
+        fence_after();
+        // epilogue: this warp's 32 pixels, 32 channels at a time
+        const long p = p0 + warp * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        float* cs = Cm + (size_t)b * O * P;
+        float* as = act ? act + (size_t)b * O * P : nullptr;
+#pragma unroll 1
+        for (int c0 = 0; c0 < O; c0 += 32) {
+            float r[32];
+            tmem_ld32(trow + c0, r);
+            if (p < P) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const size_t o = (size_t)(c0 + j) * P + p;
+                    float v = r[j] + (bias ? bias[c0 + j] : 0.0f);
+                    if (beta != 0.0f) v = fmaf(beta, cs[o], v);
+                    cs[o] = v;
+                    if (as) as[o] = gelu_f(v);
+                }
+            }
+        }
+        // the next tile's MMAs overwrite D and its stores overwrite A
+        fence_before();
+        __syncthreads();
+        fence_after();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    }
+}
+
+template <int O, int C>
+cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act, const float* bias, float beta, int B,
+                   long P, unsigned* status, int swap, cudaStream_t st)
+{
+    // shared memory: A + B, padded so that at most four CTAs share an SM
+    // (four TMEM allocations of at most 128 columns fit the 512 columns)
+    constexpr size_t need = (size_t)kM * C * 2 + (size_t)O * C * 2;
+    constexpr size_t smem = need > 56 * 1024 ? need : 56 * 1024;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_pointwise<O, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const long tiles = (long)B * ((P + kM - 1) / kM);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long grid = tiles < 4L * sms ? tiles : 4L * sms;
+    k_pointwise<O, C><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status, swap);
+    return cudaGetLastError();
+}
+
+}  // namespace umma
+
+// The shapes of the surrogate's pointwise products that run on tcgen05:
+// o x c in {64 x 64 (Fourier layers), 128 x 64 (projection 1)}.  Others
+// (the 8-channel lift, the 2-channel output) return cudaErrorNotSupported
+// and stay on the mma.sync product.
+bool pointwise_umma_supported(int o, int c) { return (o == 64 && c == 64) || (o == 128 && c == 64); }
+
+cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
+                           const float* bias, float* act, unsigned* status, int swap, cudaStream_t st)
+{
+    if (o == 64 && c == 64) return umma::launch<64, 64>(W, X, C, act, bias, beta, B, P, status, swap, st);
+    if (o == 128 && c == 64) return umma::launch<128, 64>(W, X, C, act, bias, beta, B, P, status, swap, st);
+    return cudaErrorNotSupported;
+}
+
+}  // namespace atmwfs
+
+namespace atmwfs {
+// Status bits of the tcgen05 products (a bounded wait that ran out), shared
+// by every launch of the library on this device; read and cleared by
+// atmwfs_fno_umma_status.
+__device__ unsigned g_umma_status;
+
+// Device address of the status word on the current device (looked up per call:
+// a process may use several devices).
+unsigned* umma_status_ptr()
+{
+    unsigned* p = nullptr;
+    return cudaGetSymbolAddress((void**)&p, g_umma_status) == cudaSuccess ? p : nullptr;
+}
+}  // namespace atmwfs
+
+extern "C" atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, const float* X, float* C, int batch,
+                                                  long P, float beta, const float* bias, float* act, int engine,
+                                                  void* stream)
+{
+    using namespace atmwfs;
+    if (!W || !X || !C || o < 1 || c < 1 || batch < 1 || P < 1 || engine < 1 || engine > 2) {
+        set_error_message("atmwfs_fno_pointwise_dev: bad arguments");
+        return ATMWFS_ERR_INVALID;
+    }
+    const cudaStream_t st = (cudaStream_t)stream;
+    const __nv_bfloat16* w = reinterpret_cast<const __nv_bfloat16*>(W);
+    if (!pointwise_umma_supported(o, c)) {
+        set_error_message("atmwfs_fno_pointwise_dev: shape not compiled for the tcgen05 product");
+        return ATMWFS_ERR_INVALID;
+    }
+    unsigned* status = umma_status_ptr();
+    if (!status) {
+        set_error_message("atmwfs_fno_pointwise_dev: status symbol");
+        return ATMWFS_ERR_CUDA;
+    }
+    const cudaError_t e = pointwise_umma(w, o, c, X, C, batch, P, beta, bias, act, status, engine == 2, st);
+    if (e != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return ATMWFS_ERR_CUDA;
+    }
+    return ATMWFS_OK;
+}
+
+extern "C" unsigned atmwfs_fno_umma_status(int clear)
+{
+    unsigned v = 0;
+    if (cudaMemcpyFromSymbol(&v, atmwfs::g_umma_status, sizeof v) != cudaSuccess) return 0xFFFFFFFFu;
+    if (clear) {
+        const unsigned z = 0;
+        cudaMemcpyToSymbol(atmwfs::g_umma_status, &z, sizeof z);
+    }
+    return v;
+}

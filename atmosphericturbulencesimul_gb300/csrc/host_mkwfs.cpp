@@ -267,6 +267,25 @@ extern "C" atmwfs_status atmwfs_mkwfs(const char* conf_file, float slambda_um, l
         isci = ni++;
     }
 
+    // optional lambda / n hops: the air index at the middle of each hop, at
+    // the instance's wavelength (the reference propagates with the vacuum
+    // wavelength, WFpropagate.c:91)
+    std::vector<double> hop_n[2];
+    if (opts.fresnel_air_index) {
+        std::vector<double> salt(L), hz(L > 1 ? L - 1 : 1);
+        std::vector<int> sidx(L), plo(L), phi(L);
+        int ns = 0, npl = 0;
+        MK_TRY(atmwfs_layer_planes(alt.data(), cn2.data(), (int)L, cf.fresnel_propagation_bin,
+                                   cf.wavefront_amplitude == 1, cf.fresnel_propagation, cf.zangle, &ns, salt.data(),
+                                   sidx.data(), &npl, plo.data(), phi.data(), hz.data()));
+        for (int k = 0; k < ni; k++)
+            for (int h = 0; h + 1 < npl; h++) {
+                const double mid = 0.5 * (salt[sidx[plo[h]]] + salt[sidx[plo[h + 1]]]);
+                hop_n[k].push_back(1.0 + N((float)mid, (float)inst[k].lambda, user));
+            }
+        for (int k = 0; k < ni; k++) inst[k].hop_n = hop_n[k].empty() ? nullptr : hop_n[k].data();
+    }
+
     Resources R;
     std::vector<float> hpha, hamp;
     long ff = 0, off_ref = 0, off_sci = 0;

@@ -64,6 +64,16 @@ __device__ __forceinline__ void tma_load_2d(float* dst, const CUtensorMap* map, 
         : "memory");
 }
 
+// 16-byte asynchronous copy global -> shared (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)),
+                 "l"(static_cast<uint64_t>(__cvta_generic_to_global(src)))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Every thread polls the barrier with the same time limit; the CTA agrees
 // on the outcome through __syncthreads_or, so a timeout never splits it.
 __device__ __forceinline__ bool cta_wait_tile(uint64_t* bar, int parity, unsigned* status)
@@ -99,27 +109,22 @@ struct PassGeom {
     static constexpr int NBOX = N / kBoxW + 1;
     static constexpr int TROWS = RR + 3;
     static constexpr size_t XBYTES = size_t(RR) * RS * 8;
-    static constexpr size_t PHI_EPI_BYTES = size_t(RR) * RS * 8;
-    static constexpr size_t TILE_BYTES = size_t(NBOX) * TROWS * kBoxW * 4;
-    static constexpr size_t PHI_BYTES = size_t(RR) * N * 4;          // phase of the plane's layers, [RR][N]
+    static constexpr size_t TILE_BYTES = size_t(NBOX) * TROWS * kBoxW * 4;  // screen tile (window kernel)
+    static constexpr size_t WIN_BYTES = size_t(RR) * N * 4;          // staged window rows, [RR][N]
     static constexpr int NJ = RR > 16 ? 3 : 2;                        // bin rows a tile can touch
     static constexpr size_t COLSUM_BYTES = size_t(NJ) * N * 8;        // epilogue column sums, [NJ][N]
     AW_HD static constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
     AW_HD static constexpr size_t mx(size_t a, size_t b) { return a > b ? a : b; }
-    AW_HD static constexpr size_t region(bool epi) { return round128((epi && PHI_EPI_BYTES > XBYTES) ? PHI_EPI_BYTES : XBYTES); }
-    // Separate layout: [exchange rows | tile]; the epilogue's column sums
-    // reuse the tile.  Overlaid layout (ALIAS): the tile sits after the phi
-    // rows inside the exchange region and the column sums after the staged
-    // exchange rows, so the region is max(phi + tile, rows + column sums).
-    AW_HD static constexpr size_t tile_offset(bool epi, bool alias) { return alias ? round128(PHI_BYTES) : region(epi); }
-    AW_HD static constexpr size_t smem(int ops, bool alias = false)
+    // Layout: [exchange rows | window rows of the plane's first layer]; the
+    // epilogue's column sums reuse the window rows once the phasor is applied.
+    AW_HD static constexpr size_t win_offset() { return round128(XBYTES); }
+    AW_HD static constexpr size_t smem(int ops)
     {
         const bool gather = (ops & (OP_GATHER | OP_EPI)) != 0, epi = (ops & OP_EPI) != 0;
-        if (!alias || !gather) return region(epi) + (gather ? TILE_BYTES + 128 : 0);
-        return mx(round128(PHI_BYTES) + TILE_BYTES, epi ? round128(XBYTES) + COLSUM_BYTES : XBYTES) + 128;
+        if (!gather) return round128(XBYTES);
+        return win_offset() + mx(WIN_BYTES, epi ? COLSUM_BYTES : 0);
     }
     static_assert(N % (RR) == 0, "rows per CTA must divide N");
-    static_assert(COLSUM_BYTES <= TILE_BYTES, "column sums must fit in the tile buffer");
 };
 
 // One layer's tile as NBOX box copies, issued by lane 0 of every warp of the
@@ -316,10 +321,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     constexpr bool kGather = (OPS & (OP_GATHER | OP_EPI)) != 0;
     extern __shared__ __align__(1024) unsigned char sm[];
     float2* xb = reinterpret_cast<float2*>(sm);
-    // TMA destination: 128-byte aligned whatever the dynamic smem base
-    float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm + G::tile_offset(kEpi, ALIAS)) + 127) &
-                                           ~uintptr_t(127));
-    __shared__ __align__(8) uint64_t bar;
+    float* wrows = reinterpret_cast<float*>(sm + G::win_offset());  // [RR][N]
 
     const int tid = threadIdx.x;
     const int t = tid % T;
@@ -328,18 +330,23 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     const int y = y0 + rr;
     const InstDev* I = a.inst ? a.inst + blockIdx.y : nullptr;
     const int step = a.d_step ? *a.d_step : 0;
-    const LayerPos* P = I ? a.pos + ((size_t)(step % a.poscap) * a.ninst_total + I->gidx) * a.L : nullptr;
     float2* xrow = xb + rr * RS;
 
     const int ltop = a.g_hi - 1;
     const int lbot = a.g_lo;
-    int parity = 0;
     if constexpr (kGather) {
-        if (tid == 0) mbar_init(&bar, 1);
-        __syncthreads();
-        // separate tile: its first copy overlaps the first propagation
-        if constexpr (!ALIAS)
-            if (ltop >= lbot) tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar, tid, NT);
+        // this CTA's rows of the window of the plane's first layer, copied
+        // while the first propagation runs
+        if (ltop >= lbot) {
+            const float* src = I->win[a.orient][ltop] + (size_t)y0 * I->wstride;
+            constexpr int C4 = N / 4;
+#pragma unroll 4
+            for (int k = tid; k < RR * C4; k += NT) {
+                const int r = k / C4, c = k - r * C4;
+                cp_async16(wrows + r * N + 4 * c, src + (size_t)r * I->wstride + 4 * c);
+            }
+            cp_async_commit();
+        }
     }
 
     float2 v[E];
@@ -361,32 +368,25 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         for (int ph = 0; ph < 3; ph++) {
             if (ph == 1) {
                 if constexpr (kGather) {
-                    float* phi = reinterpret_cast<float*>(xb);  // [RR][N]
-                    __syncthreads();
-                    if constexpr (ALIAS) {
-                        // overlaid tile: the exchange rows are free now
-                        if (ltop >= lbot && (tid & 31) == 0) {
-                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                            tma_issue_layer<N, RR>(maps, a.orient, ltop, tile_geom(P[ltop], a.orient, y0), tile, &bar, tid, NT);
-                        }
-                    }
-                    for (int l = ltop; l >= lbot; l--) {
-                        if (!cta_wait_tile(&bar, parity, a.d_status)) return;
-                        parity ^= 1;
-                        const bool first = (l == ltop);
-                        gather_tile<N, RR, NT>(tile, tile_geom(P[l], a.orient, y0), I->scoeff[l], tid,
-                                               [=](int r, int x, float val) {
-                                                   phi[r * N + x] = first ? val : phi[r * N + x] + val;
-                                               });
-                        __syncthreads();
-                        if (l > lbot)
-                            tma_issue_layer<N, RR>(maps, a.orient, l - 1, tile_geom(P[l - 1], a.orient, y0), tile, &bar, tid, NT);
-                    }
+                    if (ltop >= lbot) {
+                        cp_async_wait_all();
+                        __syncthreads();  // every thread's copies have landed
+                        // phase of the plane: its layers from the top down,
+                        // each window sample times the layer's Scoeff
+                        const float* wr = wrows + rr * N + t;
+                        const float sc0 = I->scoeff[ltop];
+                        float phs[E];
 #pragma unroll
-                    for (int e = 0; e < E; e++) v[e] = cmul(v[e], phasor(phi[rr * N + t + e * T]));
-                    // phi spans the exchange rows of other threads: all reads
-                    // end before the next transform's row-local exchanges
-                    __syncthreads();
+                        for (int e = 0; e < E; e++) phs[e] = __fmul_rn(wr[e * T], sc0);
+                        for (int l = ltop - 1; l >= lbot; l--) {
+                            const float* g = I->win[a.orient][l] + (size_t)y * I->wstride + t;
+                            const float sc = I->scoeff[l];
+#pragma unroll
+                            for (int e = 0; e < E; e++) phs[e] = __fadd_rn(phs[e], __fmul_rn(__ldg(g + e * T), sc));
+                        }
+#pragma unroll
+                        for (int e = 0; e < E; e++) v[e] = cmul(v[e], phasor(phs[e]));
+                    }
                 }
                 continue;
             }
@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         float* __restrict__ opha = I->out_pha + (size_t)slot * I->ostride;
         float* __restrict__ oamp = I->out_amp + (size_t)slot * I->ostride;
         const float* __restrict__ psum = I->phisum;
-        __syncthreads();  // phasor reads of phi are done
+        __syncthreads();  // phasor reads of the window rows are done
 #pragma unroll
         for (int e = 0; e < E; e++) xrow[padi(t + e * T)] = v[e];
         const int ya = max(y0, off), yb = min(y0 + RR, off + Nout);
@@ -437,7 +437,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         // bins are at least 20 rows tall: RR rows touch at most NJ bin rows
         constexpr int NJ = G::NJ;
         // [NJ][N]: per bin row, per column; clear of the staged rows in xb
-        float2* colsum = ALIAS ? reinterpret_cast<float2*>(sm + G::round128(G::XBYTES)) : reinterpret_cast<float2*>(tile);
+        float2* colsum = reinterpret_cast<float2*>(wrows);
 #pragma unroll
         for (int c = 0; c < CPT; c++) {
             const int x = off + tid + c * NT;
@@ -530,154 +530,64 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
 }
 
 // ---------------------------------------------------------------------------
-// geometric phase sum over all layers for the crop (reference array1 /
-// sarray1, AtmosphericTurbulence.c:2909-2916, 3237-3245): gather only, one
-// TMA tile per layer, compensated (two-sum) accumulation in registers.
-// Independent of the field, so it runs beside the propagation passes.
-//
-// Each thread owns column pairs (x, x + N/2 ... strided by the block): the
-// two columns share the layer's interpolation weights, so the Keys taps,
-// the scaling and the two-sum run as packed FP32x2 operations (sm_100+),
-// which round each component exactly like the scalar forms.
+// Per-step bicubic windows (the reference's window sampling,
+// AtmosphericTurbulence.c:2806-2917 / :3133-3246, without the Scoeff factor):
+// one job per (window group, layer, orientation); the CTA loads its screen
+// tile (RR rows + 3 halo rows) by TMA and writes the RR window rows.  Every
+// instance of a group (the wavelengths of one direction) then reads the same
+// samples instead of interpolating the screen itself.
 // ---------------------------------------------------------------------------
 template <int N, int RR>
-struct PhasumGeom {
-    static constexpr int NT0 = PassGeom<N, RR>::NT;
-    static constexpr int NTP = N >= 2 * NT0 ? NT0 : N / 2;  // threads per CTA
-    static constexpr int NCP = N / NTP;                     // columns per thread
-    static constexpr int NP = NCP / 2;                      // column pairs per thread
-    static_assert(N % NTP == 0 && NCP % 2 == 0, "column pairs must tile the row");
-};
-
-__device__ __forceinline__ float2 f2add(float2 a, float2 b)
-{
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-    return __fadd2_rn(a, b);
-#else
-    return make_float2(a.x + b.x, a.y + b.y);
-#endif
-}
-// a - b, one rounding per component
-__device__ __forceinline__ float2 f2sub(float2 a, float2 b)
-{
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);
-#else
-    return make_float2(a.x - b.x, a.y - b.y);
-#endif
-}
-__device__ __forceinline__ float2 f2mul(float2 a, float2 b)
-{
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-    return __fmul2_rn(a, b);
-#else
-    return make_float2(a.x * b.x, a.y * b.y);
-#endif
-}
-__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c)
-{
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
-    return __ffma2_rn(a, b, c);
-#else
-    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
-#endif
-}
-
-template <int N, int RR>
-__global__ void __launch_bounds__(PhasumGeom<N, RR>::NTP, 2)
-    k_phasum(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps)
+__global__ void __launch_bounds__(PassGeom<N, RR>::NT)
+    k_layer_windows(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps)
 {
     using G = PassGeom<N, RR>;
-    using H = PhasumGeom<N, RR>;
-    constexpr int NTP = H::NTP, NP = H::NP, TROWS = G::TROWS;
-    constexpr int TILE_FLOATS = (int)(G::TILE_BYTES / 4);
+    constexpr int NT = G::NT;
     extern __shared__ __align__(1024) unsigned char sm[];
-    // two tile buffers: the next layer's copy overlaps this layer's sums
-    float* tiles = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
-    __shared__ __align__(8) uint64_t bar[2];
+    float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) uint64_t bar;
+    const WinJob J = a.jobs[blockIdx.y];
     const int tid = threadIdx.x;
-    const int y0 = a.row0 + blockIdx.x * RR;
-    const InstDev* I = a.inst + blockIdx.y;
+    const int y0 = blockIdx.x * RR;
     const int step = *a.d_step;
-    const LayerPos* P = a.pos + ((size_t)(step % a.poscap) * a.ninst_total + I->gidx) * a.L;
-    const int L = a.L;
-    if (tid == 0) { mbar_init(&bar[0], 1); mbar_init(&bar[1], 1); }
+    const LayerPos p = a.pos[((size_t)(step % a.poscap) * a.ninst_total + J.gidx) * a.L + J.layer];
+    const TileGeom g = tile_geom(p, J.orient, y0);
+    if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
-    tma_issue_layer<N, RR>(maps, 0, L - 1, tile_geom(P[L - 1], 0, y0), tiles, &bar[0], tid, NTP);
-    if (L > 1) tma_issue_layer<N, RR>(maps, 0, L - 2, tile_geom(P[L - 2], 0, y0), tiles + TILE_FLOATS, &bar[1], tid, NTP);
-    // pair p: columns tid + p NTP (.x) and tid + (p + NP) NTP (.y)
-    float2 hi[NP][RR], lo[NP][RR];
-#pragma unroll
-    for (int p = 0; p < NP; p++)
-#pragma unroll
-        for (int r = 0; r < RR; r++) hi[p][r] = lo[p][r] = make_float2(0.0f, 0.0f);
-    int parity = 0;  // bit b: phase parity of buffer b
-    for (int l = L - 1; l >= 0; l--) {
-        const int b = (L - 1 - l) & 1;
-        float* tile = tiles + b * TILE_FLOATS;
-        if (!cta_wait_tile(&bar[b], (parity >> b) & 1, a.d_status)) {
-            // the other buffer may still be in flight: let it land first
-            if (l > 0) cta_wait_tile(&bar[b ^ 1], (parity >> (b ^ 1)) & 1, nullptr);
-            return;
+    tma_issue_layer<N, RR>(maps, J.orient, J.layer, g, tile, &bar, tid, NT);
+    if (!cta_wait_tile(&bar, 0, a.d_status)) return;
+    float* out = J.out + (size_t)y0 * J.stride;
+    const int stride = J.stride;
+    gather_tile<N, RR, NT>(tile, g, 1.0f, tid, [=](int r, int x, float val) { out[(size_t)r * stride + x] = val; });
+}
+
+// ---------------------------------------------------------------------------
+// geometric phase sum over all layers for the crop (reference array1 /
+// sarray1, AtmosphericTurbulence.c:2909-2916, 3237-3245) from the step's
+// windows in the screen orientation: per pixel the layers from the top
+// down, each window sample times the layer's Scoeff, accumulated with a
+// two-sum (compensated FP32; the reference keeps a float sum).  Independent
+// of the field, so it runs beside the propagation passes.
+// ---------------------------------------------------------------------------
+template <int N>
+__global__ void __launch_bounds__(kPhasumThreads) k_phasum(const __grid_constant__ PassArgs a)
+{
+    const InstDev* I = a.inst + blockIdx.y;
+    const int off = I->off, Nout = I->Nout, L = a.L;
+    const size_t ws = (size_t)I->wstride;
+    const long npx = (long)Nout * Nout;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < npx; k += (long)gridDim.x * blockDim.x) {
+        const int yy = (int)(k / Nout), xx = (int)(k - (long)yy * Nout);
+        const size_t o = (size_t)(yy + off) * ws + (size_t)(xx + off);
+        float hi = 0.0f, lo = 0.0f;
+        for (int l = L - 1; l >= 0; l--) {
+            const float val = __fmul_rn(__ldg(I->win[0][l] + o), I->scoeff[l]);
+            float sum, err;
+            two_sum(hi, val, sum, err);
+            hi = sum;
+            lo = __fadd_rn(lo, err);
         }
-        parity ^= 1 << b;
-        const TileGeom g = tile_geom(P[l], 0, y0);
-        const float sc = I->scoeff[l];
-        float wx[4], wy[4];
-        keys_weights(g.fx, wx);
-        keys_weights(g.fy, wy);
-        const float2 sc2 = make_float2(sc, sc);
-        float2 wx2[4], wy2[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            wx2[k] = make_float2(wx[k], wx[k]);
-            wy2[k] = make_float2(wy[k], wy[k]);
-        }
-#pragma unroll
-        for (int p = 0; p < NP; p++) {
-            const int ca = g.d + tid + p * NTP, cb = ca + NP * NTP;
-            // tile rows stream through: output row r takes taps from rows
-            // r..r+3 in that order, so at most four partial rows are live
-            float2 part[4];
-#pragma unroll
-            for (int q = 0; q < TROWS; q++) {
-                float2 h = f2mul(wx2[0], make_float2(tile[tile_index<TROWS>(q, ca)], tile[tile_index<TROWS>(q, cb)]));
-#pragma unroll
-                for (int k = 1; k < 4; k++)
-                    h = f2fma(wx2[k], make_float2(tile[tile_index<TROWS>(q, ca + k)], tile[tile_index<TROWS>(q, cb + k)]), h);
-#pragma unroll
-                for (int k = 3; k >= 0; k--) {
-                    const int r = q - k;  // output row receiving tap k
-                    if (r < 0 || r >= RR) continue;
-                    float2& v = part[r & 3];
-                    v = k == 0 ? f2mul(wy2[0], h) : f2fma(wy2[k], h, v);
-                    if (k == 3) {
-                        const float2 val = f2mul(v, sc2);
-                        // two-sum: hi + val = s + e exactly
-                        const float2 s = f2add(hi[p][r], val);
-                        const float2 bp = f2sub(s, hi[p][r]);
-                        const float2 e = f2add(f2sub(hi[p][r], f2sub(s, bp)), f2sub(val, bp));
-                        hi[p][r] = s;
-                        lo[p][r] = f2add(lo[p][r], e);
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        if (l > 1) tma_issue_layer<N, RR>(maps, 0, l - 2, tile_geom(P[l - 2], 0, y0), tile, &bar[b], tid, NTP);
-    }
-    const int off = I->off, Nout = I->Nout;
-#pragma unroll
-    for (int p = 0; p < NP; p++) {
-#pragma unroll
-        for (int r = 0; r < RR; r++) {
-            const int y = y0 + r;
-            if (y < off || y >= off + Nout) continue;
-            float* row = I->phisum + (size_t)(y - off) * Nout - off;
-            const int xa = tid + p * NTP, xb = xa + NP * NTP;
-            if (xa >= off && xa < off + Nout) row[xa] = hi[p][r].x + lo[p][r].x;
-            if (xb >= off && xb < off + Nout) row[xb] = hi[p][r].y + lo[p][r].y;
-        }
+        I->phisum[k] = __fadd_rn(hi, lo);
     }
 }
 
@@ -691,7 +601,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
     dim3 block(G::NT);
 #define AW_CASE(VAR)                                                                                   \
     case VAR: {                                                                                        \
-        constexpr size_t sm = G::smem(VAR, ALIAS);                                                     \
+        constexpr size_t sm = G::smem(VAR);                                                            \
         static bool attr = false;                                                                      \
         if (!attr) {                                                                                   \
             cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS, HP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
@@ -720,14 +630,18 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         AW_CASE(kVarUnitFwd)
         AW_CASE(kVarUnitInv)
         case kVarPhasum: {
-            constexpr size_t sm = 2 * G::TILE_BYTES + 128;
+            k_phasum<N><<<grid, kPhasumThreads, 0, st>>>(a);
+            return cudaGetLastError();
+        }
+        case kVarWindows: {
+            constexpr size_t sm = G::TILE_BYTES + 128;
             static bool attr = false;
             if (!attr) {
-                cudaError_t e = cudaFuncSetAttribute(k_phasum<N, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                cudaError_t e = cudaFuncSetAttribute(k_layer_windows<N, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
                 if (e != cudaSuccess) return e;
                 attr = true;
             }
-            k_phasum<N, RR><<<grid, dim3(PhasumGeom<N, RR>::NTP), sm, st>>>(a, m);
+            k_layer_windows<N, RR><<<grid, dim3(G::NT), sm, st>>>(a, m);
             return cudaGetLastError();
         }
         default: return cudaErrorInvalidValue;

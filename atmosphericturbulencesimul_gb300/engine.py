@@ -41,6 +41,7 @@ class InstanceSpec:
     wf_size: int | None = None      # output crop (default: wf_raw_size)
     scoeff: np.ndarray | None = None   # per-layer phase multiplier (float32)
     roffset: np.ndarray | None = None  # per-layer refraction offset [m]
+    hop_n: np.ndarray | None = None    # per-hop air index (optional lambda / n hops); None = vacuum lambda
 
 
 class Series:
@@ -69,6 +70,8 @@ class Series:
                 I.scoeff = _f32p(self._hold(np.ascontiguousarray(s.scoeff, np.float32)))
             if s.roffset is not None:
                 I.roffset = _f64p(self._hold(np.ascontiguousarray(s.roffset, np.float64)))
+            if s.hop_n is not None:
+                I.hop_n = _f64p(self._hold(np.ascontiguousarray(s.hop_n, np.float64)))
         p = _lib.Params()
         p.nlayers = self.L
         p.alt, p.cn2, p.speed, p.dir = _f64p(self.alt), _f64p(self.cn2), _f64p(self.speed), _f64p(self.dir)

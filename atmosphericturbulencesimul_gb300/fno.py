@@ -165,6 +165,7 @@ class PairSource:
         speed = list(rng.uniform(5.0, 30.0, 7))
         direction = list(rng.uniform(0.0, 2 * np.pi, 7))
         self.L, self.G, self.count = len(alt), grid, count
+        self.alt, self.cn2, self.fresnel_bin, self.pupil = alt, cn2, 100.0, 0.01
         self.lam = rng.uniform(lam_lo, lam_hi, count)
         specs = [InstanceSpec(lam=float(l), mode=MODE_REF, src_x=float(rng.uniform(-spread, spread) * ARCSEC),
                               src_y=float(rng.uniform(-spread, spread) * ARCSEC), wf_raw_size=grid, wf_size=grid,
@@ -315,6 +316,10 @@ def main(argv=None) -> int:
     ap.add_argument("--pairs", type=int, default=50000)
     ap.add_argument("--test", type=int, default=5000)
     ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--width", type=int, default=64)
+    ap.add_argument("--modes", type=int, default=32)
+    ap.add_argument("--layers", type=int, default=4)
+    ap.add_argument("--proj", type=int, default=128)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--count", type=int, default=64, help="plain-path instances per engine step")
@@ -322,7 +327,7 @@ def main(argv=None) -> int:
     ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
     a = ap.parse_args(argv)
-    cfg = FnoConfig(grid=a.grid)
+    cfg = FnoConfig(grid=a.grid, width=a.width, modes=a.modes, layers=a.layers, proj=a.proj)
     src = PairSource(count=a.count, grid=a.grid, seed=a.seed)
     test = PairSource(count=a.count, grid=a.grid, seed=a.seed + 1000)
     model = Surrogate(cfg, seed=a.seed)

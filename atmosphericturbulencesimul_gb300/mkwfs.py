@@ -128,12 +128,14 @@ def shm_semwait(name: str, index: int = 0, timeout_s: float = 0.0) -> None:
 
 
 def mkwfs(slambda_um: float, precision: int = 0, conf_file="WFsim.conf", *, refractivity=None, scoeff=None,
-          roffset=None, seed: int = 0, verbose: bool = False, semwait_timeout: float = 0.0) -> None:
+          roffset=None, seed: int = 0, verbose: bool = False, semwait_timeout: float = 0.0,
+          fresnel_air_index: bool = False) -> None:
     """Run the series command in the current directory (see atmwfs_mkwfs).
 
     refractivity: optional callable N(alt_m, lambda_m) -> n - 1 (the
     reference's AtmosphereModel_stdAtmModel_N); scoeff / roffset: per-layer
-    overrides of the science phase multipliers and refraction offsets [m]."""
+    overrides of the science phase multipliers and refraction offsets [m];
+    fresnel_air_index: hops with lambda / n(air) instead of the vacuum lambda."""
     lib = _lib.load()
     o = _lib.MkwfsOpts()
     keep = []
@@ -152,6 +154,7 @@ def mkwfs(slambda_um: float, precision: int = 0, conf_file="WFsim.conf", *, refr
     o.seed = seed
     o.verbose = int(verbose)
     o.semwait_timeout = float(semwait_timeout)
+    o.fresnel_air_index = int(fresnel_air_index)
     _lib.check(lib.atmwfs_mkwfs(_b(conf_file), float(slambda_um), int(precision), C.byref(o)))
 
 
@@ -205,12 +208,20 @@ def refraction_path(lam: float, zangle: float, site_alt: float, refractivity, ab
     return r.value, t.value
 
 
+# Tables with fewer rays than this run on the host cores under where="auto":
+# one FP64 ray per GPU thread is a serial chain of double transcendentals,
+# and the GPU overtakes 16 Grace cores only once the table fills many warps
+# on every SM (the crossover measured by the benchmark's refraction scan).
+REFRACTION_GPU_MIN_RAYS = 1 << 30
+
+
 def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: np.ndarray | None, dh: float,
-                     host_threads: int | None = None):
+                     host_threads: int | None = None, where: str = "auto"):
     """Refraction [arcsec] and transmission of every (wavelength, zenith
-    angle) pair, one GPU thread per ray (or host_threads CPU threads, 0 =
-    all); Ntab[i] / Ktab[i] tabulate the model of wavelength i at altitudes
-    k * dh.  Returns two [nlambda, nzangle] arrays."""
+    angle) pair; Ntab[i] / Ktab[i] tabulate the model of wavelength i at
+    altitudes k * dh.  where: "gpu" (one GPU thread per ray), "host"
+    (host_threads CPU threads, 0 or None = all) or "auto" (the host when
+    host_threads is given or below REFRACTION_GPU_MIN_RAYS rays).  Returns two [nlambda, nzangle] arrays."""
     lib = _lib.load()
     lam = np.ascontiguousarray(lambdas, np.float64)
     za = np.ascontiguousarray(zangles, np.float64)
@@ -221,8 +232,14 @@ def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: 
     dp = C.POINTER(C.c_double)
     args = (lam.ctypes.data_as(dp), len(lam), za.ctypes.data_as(dp), len(za), site_alt,
             N.ctypes.data_as(C.POINTER(C.c_float)), None if K is None else K.ctypes.data_as(dp), N.shape[1], dh)
-    if host_threads is None:
+    if where not in ("auto", "gpu", "host"):
+        raise ValueError(f"where must be auto, gpu or host, not {where!r}")
+    if where == "auto":
+        big = len(lam) * len(za) >= REFRACTION_GPU_MIN_RAYS
+        where = "gpu" if big and host_threads is None else "host"
+    if where == "gpu":
         _lib.check(lib.atmwfs_refraction_table(*args, r.ctypes.data_as(dp), t.ctypes.data_as(dp)))
     else:
-        _lib.check(lib.atmwfs_refraction_table_host(*args, int(host_threads), r.ctypes.data_as(dp), t.ctypes.data_as(dp)))
+        _lib.check(lib.atmwfs_refraction_table_host(*args, int(host_threads or 0), r.ctypes.data_as(dp),
+                                                    t.ctypes.data_as(dp)))
     return r, t

@@ -32,3 +32,23 @@ def scoeff(lam_ref: float, lam: float, nlayers: int) -> np.ndarray:
     n_r = np.float32(n_minus_1_std_air(float(lr)))
     v = float(lr) / float(lam) * float(n_l) / float(n_r)
     return np.full(nlayers, v, dtype=np.float32)
+
+
+def n_air(alt_m, lam_m, scale_height: float = 8000.0):
+    """Refractive index of dry standard air at altitude alt [m]: the Ciddor
+    refractivity scaled by an exponential density profile (the host driver's
+    default model)."""
+    return 1.0 + n_minus_1_std_air(lam_m) * np.exp(-np.asarray(alt_m, dtype=np.float64) / scale_height)
+
+
+def hop_air_index(alt, cn2, fresnel_bin: float, lam: float, model=None, amplitude: int = 1, fresnel: int = 1,
+                  zangle: float = 0.0) -> np.ndarray:
+    """Air index of every propagation hop of a profile (the optional lambda / n
+    hops of atmwfs_instance.hop_n), in the engine's hop order: n at the
+    middle of the hop between the altitudes of its two super-layers.
+    model(alt, lam) -> n defaults to n_air."""
+    from .engine import layer_planes
+    salt, sidx, planes, _ = layer_planes(alt, cn2, fresnel_bin, amplitude, fresnel, zangle)
+    model = model or n_air
+    mids = [0.5 * (salt[sidx[planes[h][0]]] + salt[sidx[planes[h + 1][0]]]) for h in range(len(planes) - 1)]
+    return np.array([float(model(m, lam)) for m in mids], np.float64)

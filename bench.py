@@ -59,6 +59,13 @@ def workload(name: str, seed: int = 0) -> dict:
                 k += 1
         base.update(name="batched: 7 layers, 2048^2 screens, 16 lambda x 9 directions, W mixed 256/512/1024",
                     inst=inst, steps_nominal=5000)
+    elif name == "single":
+        # one turbulent layer at 5 km over a Cn2 = 0 layer at the ground, so
+        # that the field is propagated to the ground (the reference never
+        # propagates below its lowest super-layer)
+        base.update(alt=[0.0, 5000.0], cn2=[0.0, 1.0], speed=[0.0, 10.0], direction=[0.0, np.deg2rad(30.0)], M=1024,
+                    inst=[dict(lam=1.6e-6, src=(0.0, 0.0), W=256)], steps_nominal=1000,
+                    name="single: 1 layer at 5 km, 1024^2 screen, 256^2 pupil, 1.6 um")
     elif name == "multilayer":
         inst = [dict(lam=l, src=(0.0, 0.0), W=512) for l in (0.5e-6, 0.8e-6, 1.25e-6, 2.2e-6)]
         base.update(name="multilayer: 7 layers, 2048^2 screens, 512^2 pupils, 4 lambda, on-axis", inst=inst,
@@ -77,14 +84,21 @@ def workload(name: str, seed: int = 0) -> dict:
     return base
 
 
-def make_series(wl: dict, ring: int = 1):
+def num_hops(wl: dict) -> int:
+    """Propagation hops per frame of the workload's profile (host grouping)."""
+    from atmosphericturbulencesimul_gb300.engine import layer_planes
+    return len(layer_planes(wl["alt"], wl["cn2"], wl["fresnel_bin"])[3])
+
+
+def make_series(wl: dict, ring: int = 1, fft_fp16: bool = False):
     from atmosphericturbulencesimul_gb300 import MODE_SCI, InstanceSpec, Series, master_screen
     from atmosphericturbulencesimul_gb300.refractivity import scoeff
     L = len(wl["alt"])
     specs = [InstanceSpec(lam=I["lam"], mode=MODE_SCI, src_x=I["src"][0], src_y=I["src"][1], wf_raw_size=I["W"],
                           wf_size=I["W"], scoeff=scoeff(wl["lam_ref"], I["lam"], L)) for I in wl["inst"]]
     s = Series(wl["alt"], wl["cn2"], wl["speed"], wl["direction"], master_size=wl["M"], instances=specs,
-               pupil_scale=wl["pupil"], time_step=wl["dt"], fresnel_bin=wl["fresnel_bin"], ring=ring)
+               pupil_scale=wl["pupil"], time_step=wl["dt"], fresnel_bin=wl["fresnel_bin"], ring=ring,
+               fft_fp16=int(fft_fp16))
     M = wl["M"]
     screens = []
     for l in range(L):
@@ -143,7 +157,7 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def surrogate_section(pairs: int = 4096) -> dict:
+def surrogate_section(pairs: int = 50000) -> dict:
     """The learned surrogate at 256^2 (7 layers): inference frames/s and
     tensor-core roofline, and its held-out error against the plain Fresnel
     path beside that of the geometric field.  Uses the model file named by
@@ -164,6 +178,7 @@ def surrogate_section(pairs: int = 4096) -> dict:
     t_train = time.time() - t0
     test = F.PairSource(count=32, grid=256, seed=1001)
     ev = F.evaluate(model, test, steps=2, batch=8)
+    ev_fp64 = surrogate_vs_fp64(model, test)
     # inference throughput on resident inputs, batch 16
     x, *_ = test.step()
     xb = torch.cat([x, x])[:16].contiguous()
@@ -206,6 +221,7 @@ def surrogate_section(pairs: int = 4096) -> dict:
            "model": {k: v for k, v in model.cfg.__dict__.items()}, "params": model.num_params, "weights": "bf16 (fp32 master)",
            "how": how, "setup_s": round(t_train, 1), "roofline": roof, "plain_same_grid_fps": round(plain_fps, 1),
            "error_vs_plain": {k: {m: round(v, 5) for m, v in d.items()} for k, d in ev.items()},
+           "error_vs_fp64": ev_fp64,
            "error_note": "held-out seeds; 'model' = surrogate, 'geometric' = exp(i phi) without diffraction; "
                          "opd_wrms_nm weights the wrapped phase error by the plain path's intensity"}
     test.close()
@@ -213,6 +229,40 @@ def surrogate_section(pairs: int = 4096) -> dict:
         src.close()
     model.close()
     return res
+
+
+def surrogate_vs_fp64(model, test, n: int = 8) -> dict:
+    """Held-out frames of the surrogate and of the plain FP32 path against the
+    FP64 oracle's field (same screens, positions and Scoeff as the engine that
+    made the surrogate's inputs): wrapped OPD rms (nm) and amplitude rms,
+    averaged over the first n instances of one more step.  The checker runs
+    outside every timed region."""
+    import torch
+    from atmosphericturbulencesimul_gb300 import fno as F
+    from oracle import oracle as orc
+    o64 = orc.Oracle(64)
+    o64.set_threads(os.cpu_count() or 1)
+    x, _, phi, amp, pha, lam = test.step()
+    out = model.forward(x[:n].contiguous())
+    a_m, p_m = F.assemble(out, phi[:n].contiguous())
+    torch.cuda.synchronize()
+    s = test.series
+    screens = [s.read_screen(l) for l in range(test.L)]
+    salt, sidx = o64.superlayers(test.alt, np.asarray(test.cn2) / np.sum(test.cn2), test.fresnel_bin)
+    acc = {"surrogate": [], "plain": []}
+    for i in range(n):
+        xi, yi = s.positions(i)
+        sc = np.asarray(s.instances[i].scoeff, np.float32).astype(np.float64)
+        li = float(s.instances[i].lam)
+        _, fld = o64.frame(screens, xi, yi, sc, sidx, salt, float(np.float32(test.pupil)), 0.0, li, test.G)
+        ao, po = np.abs(fld), np.angle(fld)
+        nm = li / (2 * np.pi) * 1e9
+        for key, (a, p_) in (("surrogate", (a_m[i], p_m[i])), ("plain", (amp[i], pha[i]))):
+            a = a.double().cpu().numpy()
+            d = np.angle(np.exp(1j * (p_.double().cpu().numpy() - po)))
+            acc[key].append((float(np.sqrt(np.mean(d ** 2)) * nm), float(np.sqrt(np.mean((a - ao) ** 2)))))
+    return {k: {"opd_wrapped_rms_nm": float(f"{np.mean([e[0] for e in v]):.4g}"),
+                "amp_rms": float(f"{np.mean([e[1] for e in v]):.4g}"), "frames": n} for k, v in acc.items()}
 
 
 def rows_section() -> dict:
@@ -274,25 +324,32 @@ def rows_section() -> dict:
                                       "frac": round(byt / (ms * 1e-3) / 1e9 / pk["hbm_gbs"], 4), "bytes": byt,
                                       "note": "rows, transpose, rows, transpose: four read+write passes"}}
     del a, b
-    # refraction: 16 wavelengths x 64 zenith angles on the GPU, one ray on the host
+    # refraction: tables of 16 wavelengths x nz zenith angles, FP64 traces,
+    # on the GPU (one ray per thread) and on every host core
     alt = np.arange(10001) * 10.0
     lams = 0.4e-6 * (2.4 / 0.4) ** (np.arange(16) / 15.0)
     Ntab = np.stack([(2.7e-4 * (1 + 0.0056 / (l * 1e6) ** 2) * np.exp(-alt / 8000.0)).astype(np.float32) for l in lams])
-    za = np.linspace(0.0, np.deg2rad(75.0), 64)
-    refraction_table(lams[:1], za[:1], 0.0, Ntab[:1], None, 10.0)
-    t0 = time.perf_counter()
-    refraction_table(lams, za, 0.0, Ntab, None, 10.0)
-    t_gpu = time.perf_counter() - t0
     threads = os.cpu_count() or 1
-    sub = slice(0, 16, 4)                    # a 4 x 64 sample on the host
-    t0 = time.perf_counter()
-    refraction_table(lams[sub], za, 0.0, Ntab[sub], None, 10.0, host_threads=threads)
-    t_host = time.perf_counter() - t0
-    out["refraction"] = {"value": round(len(lams) * len(za) / t_gpu, 1), "unit": "rays/s",
-                         "rays": len(lams) * len(za),
-                         "cpu": {"value": round(4 * len(za) / t_host, 1), "unit": "rays/s", "cores": threads,
-                                 "sample": "4 wavelengths x 64 zenith angles, the same table model"},
-                         "note": "FP64 traces, wall time of the call; one ray per GPU thread (one warp per block)"}
+    refraction_table(lams[:1], [0.1], 0.0, Ntab[:1], None, 10.0, where="gpu")
+    scan = []
+    for nz in (64, 256, 1024, 4096):
+        za = np.linspace(0.0, np.deg2rad(75.0), nz)
+        t0 = time.perf_counter()
+        refraction_table(lams, za, 0.0, Ntab, None, 10.0, where="gpu")
+        t_gpu = time.perf_counter() - t0
+        # the host on a sample of the same table (every 16th zenith angle)
+        sub = za[::max(1, nz // 64)]
+        t0 = time.perf_counter()
+        refraction_table(lams, sub, 0.0, Ntab, None, 10.0, where="host", host_threads=threads)
+        t_host = time.perf_counter() - t0
+        scan.append({"rays": 16 * nz, "gpu_rays_per_s": round(16 * nz / t_gpu, 1),
+                     "host_rays_per_s": round(16 * len(sub) / t_host, 1)})
+    out["refraction"] = {"value": scan[0]["gpu_rays_per_s"], "unit": "rays/s", "rays": scan[0]["rays"],
+                         "cpu": {"value": scan[0]["host_rays_per_s"], "unit": "rays/s", "cores": threads,
+                                 "sample": "the same table model; host rays on every thread"},
+                         "scan": scan,
+                         "note": "FP64 traces, wall time of the call; one ray per GPU thread (one warp per block); "
+                                 "refraction_table(where='auto') takes the host below the crossover of this scan"}
     return out
 
 
@@ -337,7 +394,11 @@ class CpuSeries:
             self.state.append([x, y, [0] * L, [0] * L, vx, vy,
                                scoeff(wl["lam_ref"], I["lam"], L).astype(np.float64)])
         self.order = sorted(range(len(wl["inst"])), key=lambda i: -wl["inst"][i]["W"])
-        self.pool = cf.ThreadPoolExecutor(max_workers=threads)
+        # one frame per thread; with fewer instances than threads each frame
+        # spreads over its share of the threads (OpenMP inside the frame)
+        self.workers = min(threads, len(wl["inst"]))
+        self.per_frame = max(1, threads // self.workers)
+        self.pool = cf.ThreadPoolExecutor(max_workers=self.workers)
 
     def _frame(self, i: int, x, y, threads: int = 1) -> None:
         # the OpenMP team size is a per-thread setting: one thread per frame
@@ -353,7 +414,7 @@ class CpuSeries:
         for i in self.order:
             st = self.state[i]
             self.orc.step_positions(st[0], st[1], st[2], st[3], st[4], st[5], self.wl["dt"], self.wl["M"])
-            jobs.append(self.pool.submit(self._frame, i, st[0].copy(), st[1].copy()))
+            jobs.append(self.pool.submit(self._frame, i, st[0].copy(), st[1].copy(), self.per_frame))
         for j in jobs:
             j.result()
 
@@ -374,17 +435,23 @@ class CpuSeries:
         self.pool.shutdown()
 
 
-def cpu_step_sample(wl: dict, threads: int, nsteps: int = 1) -> tuple[float, str]:
-    """The CPU baseline of the GPU arm's line: `nsteps` whole steps of the
-    workload (every instance, one frame each) on `threads` host threads."""
+def cpu_step_sample(wl: dict, threads: int, min_s: float = 10.0) -> tuple[float, str]:
+    """The CPU baseline of the GPU arm's line: whole steps of the workload
+    (every instance, one frame each) on `threads` host threads, as many as
+    fit in about `min_s` seconds (at least one)."""
     cs = CpuSeries(wl, cpu_screens(wl, threads), threads)
+    cs.step()  # warm-up
     t0 = time.perf_counter()
-    for _ in range(nsteps):
+    nsteps = 0
+    while nsteps == 0 or time.perf_counter() - t0 < min_s:
         cs.step()
+        nsteps += 1
     t = time.perf_counter() - t0
     cs.close()
     n = nsteps * len(wl["inst"])
-    return n / t, f"{nsteps} whole step(s) of the workload ({n} frames, {t:.1f} s), one instance per host thread"
+    how = ("one instance per host thread" if cs.per_frame == 1 else
+           f"{cs.workers} instance(s) at a time, {cs.per_frame} threads per frame")
+    return n / t, f"{nsteps} whole step(s) of the workload ({n} frames, {t:.2f} s), {how}"
 
 
 def accuracy_section(s, wl: dict) -> dict:
@@ -441,10 +508,12 @@ def main():
     ap.add_argument("--workload", default="batched")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the error check against the FP64 oracle")
+    ap.add_argument("--fft-fp16", action="store_true", help="FFT stages in FP16 with per-stage scaling")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-only", action="store_true",
                     help="time only the surrogate section (profiling); prints its JSON object")
-    ap.add_argument("--surrogate-pairs", type=int, default=4096, help="training pairs of the surrogate section")
+    ap.add_argument("--surrogate-pairs", type=int, default=50000,
+                    help="training pairs of the surrogate section (50k: the specified training set)")
     ap.add_argument("--no-rows", action="store_true", help="skip the PSF / large-transform / refraction section")
     ap.add_argument("--rows-only", action="store_true", help="time only that section (profiling)")
     args = ap.parse_args()
@@ -464,8 +533,12 @@ def main():
     cfg = {"workload": wl["name"], "instances": len(wl["inst"]), "layers": len(wl["alt"]),
            "master": wl["M"], "grids": {str(W): sum(1 for i in wl["inst"] if i["W"] == W)
                                          for W in sorted({i["W"] for i in wl["inst"]})},
-           "hops": 6, "path": "plain (Fresnel, FP32)", "l2": "inputs larger than L2 (screens + fields > 1 GB)",
+           "hops": num_hops(wl),
+           "path": "plain (Fresnel, FP16 FFT stages)" if args.fft_fp16 else "plain (Fresnel, FP32)",
+           "l2": "inputs larger than L2 (screens + fields > 1 GB)" if len(wl["inst"]) > 8 else
+                 "small workload: inputs not larger than L2",
            "parallelism": f"replicas x{args.gpus}"}
+    dtype = "f16/f32" if args.fft_fp16 else "f32"
 
     if args.impl == "reference":
         if rank != 0:
@@ -489,7 +562,9 @@ def main():
                 "config": cfg, "impl": "reference",
                 "cpu_baseline": {"value": v, "unit": "frames/s", "cores": threads, "kind": "port",
                                  "sample": f"{args.steps} whole steps of the workload after {args.warmup} warm-up "
-                                           f"steps, one instance per host thread",
+                                           f"steps, " + ("one instance per host thread" if cs.per_frame == 1 else
+                                                         f"{cs.workers} instance(s) at a time, {cs.per_frame} "
+                                                         f"threads per frame"),
                                  "single_core": {"value": round(one, 4), "unit": "frames/s",
                                                  "sample": "one frame per grid class on one thread (" + one_sample
                                                            + "), weighted by the workload's mix"}},
@@ -505,7 +580,7 @@ def main():
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     # two device output slots: the e2e copies of a step overlap the next step
-    s, screens = make_series(wl, ring=2)
+    s, screens = make_series(wl, ring=2, fft_fp16=args.fft_fp16)
     ninst = len(wl["inst"])
     L = len(wl["alt"])
     # warm-up (also captures the step graph)
@@ -546,14 +621,17 @@ def main():
     npl = len(s.planes()[0])
     passes = []
     for c in range(s.num_classes()):
-        for k in range(0, npl + 1):
+        for k in range(0, npl + 2):
             r = s.time_pass(k, c, reps=5)
             r.update(k=k, c=c)
+            if k == npl + 1 and r["bytes"] == 0:
+                continue  # this class computes no windows
             passes.append(r)
     # group launches by kernel (grid size, pass kind); the dominant kernel has
     # the largest total time per step
     def kind(k):
-        return "phase-sum" if k == 0 else "first" if k == 1 else "last" if k == npl else "mid"
+        return ("phase-sum" if k == 0 else "windows" if k == npl + 1 else "first" if k == 1 else "last" if k == npl
+                else "mid")
     groups = {}
     for p in passes:
         g = groups.setdefault((p["n"], kind(p["k"])), {"ms": 0.0, "bytes": 0.0, "launches": 0, "count": p["count"]})
@@ -577,14 +655,15 @@ def main():
             "algorithmic_bytes_per_launch": dom["bytes"] / dom["launches"],
             "ms_per_launch": round(dom["ms"] / dom["launches"], 4), "share_of_step": round(dom["ms"] / tot, 3),
             "peak_source": pk["source"]}
-    launches = (npl + 1) * s.num_classes() + 3
+    # per class: phase sum and passes; the window launches; unwrap, apply, step counter
+    launches = (npl + 1) * s.num_classes() + sum(1 for p in passes if p["k"] == npl + 1) + 3
     cfg["tiles"] = {str(ci["n"]): {"rows_per_cta": ci["rows_per_cta"], "tuned_ms": [round(x, 4) for x in ci["tuned_ms"]]}
                     for ci in (s.class_info(c) for c in range(s.num_classes()))}
     cfg["pass_ms"] = {f"n{p['n']}_k{p['k']}": round(p["ms"], 4) for p in passes}
 
     line = {"metric": metric, "value": round(value, 2), "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(1e3 * t / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox screens)",
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded Philox screens)",
             "config": cfg, "clocks": clk.summary(),
             "e2e": {"value": round(e2e, 2), "unit": "frames/s", "h2d_bytes_per_step": ninst * L * 16,
                     "d2h_bytes_per_step": 2 * ff * 4},

@@ -49,6 +49,11 @@ typedef struct atmwfs_instance {
     long wf_size;           /* output crop, <= wf_raw_size (WFsize)                                 */
     const float* scoeff;    /* [nlayers] phase multiplier (Scoeff, :2661-2663); NULL = 1            */
     const double* roffset;  /* [nlayers] refraction offset [m] added to y (:2163-2183); NULL = 0    */
+    const double* hop_n;    /* [hops] optional refractive index of the air along each hop, in the
+                               engine's hop order (top plane down, atmwfs_plane_info): the hop's
+                               transfer function then uses lambda / n.  NULL = the vacuum lambda
+                               of the reference's hops (WFpropagate.c:91, quirk of its :2672/:2685
+                               calls: the air index enters only through Scoeff)               */
 } atmwfs_instance;
 
 /* Parsed configuration (the WFsim.conf keywords the path reads) and the
@@ -165,9 +170,11 @@ atmwfs_status atmwfs_layer_planes(const double* alt, const double* cn2, int L, d
 void* atmwfs_stream(atmwfs_ctx* ctx);
 
 /* Diagnostics: launch pass k (1-based, of atmwfs_num_planes passes; k = 0 is
- * the geometric phase-sum kernel) for the instances of grid class c `reps` times, timed with CUDA events on the
- * context stream.  Returns the mean duration [ms], the algorithmic bytes of
- * one launch (field in/out, screen tiles, outputs), and the class's grid
+ * the geometric phase-sum kernel, k = atmwfs_num_planes + 1 the kernel that
+ * computes the step's screen windows of the window groups of this grid size)
+ * for the instances of grid class c `reps` times, timed with CUDA events on
+ * the context stream.  Returns the mean duration [ms], the algorithmic bytes
+ * of one launch (field in/out, window rows, outputs), and the class's grid
  * size and instance count.  Does not advance the simulation. */
 atmwfs_status atmwfs_time_pass(atmwfs_ctx* ctx, int k, int c, int reps, double* ms, double* bytes, int* n,
                                int* count);

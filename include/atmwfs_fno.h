@@ -81,6 +81,20 @@ atmwfs_status atmwfs_gemm_bf16(int M, int N, int K, const void* A, long lda, int
                                int tb, int b_bf16, float* C, long ldc, float alpha, float beta, const float* bias,
                                int batch, long sA, long sB, long sC, void* stream);
 
+/* The pointwise channel mixing of the network (device pointers; no
+ * counterpart in the reference, whose path has no network):
+ * C[b] (o x P) = W (o x c, BF16) X[b] (c x P, FP32) + bias[o] + beta C[b],
+ * act[b] = gelu(C[b]) if act is not NULL, on the tcgen05 tensor cores
+ * (accumulator in tensor memory), compiled for o x c = 64 x 64 and 128 x 64.
+ * engine 1: the product the network uses; 2: the same with the two
+ * core-matrix strides of its shared-memory descriptors exchanged (a check
+ * that only engine 1 matches the FP32 product). */
+atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, const float* X, float* C, int batch, long P,
+                                       float beta, const float* bias, float* act, int engine, void* stream);
+/* Status bits of the tcgen05 products since the last clear (1: a bounded
+ * wait for the tensor cores ran out); clear != 0 resets them. */
+unsigned atmwfs_fno_umma_status(int clear);
+
 #ifdef __cplusplus
 }
 #endif

@@ -177,6 +177,10 @@ typedef struct atmwfs_mkwfs_opts {
     /* Seconds a WAITFORSEM wait may take before the run stops with
      * ATMWFS_ERR_TIMEOUT; <= 0 waits without limit, as the reference. */
     double semwait_timeout;
+    /* 1: every Fresnel hop propagates with lambda / n, n the air index of
+     * the refractivity model at the middle of the hop (atmwfs_instance.hop_n);
+     * 0 (default): the vacuum wavelength, as the reference (WFpropagate.c:91). */
+    int fresnel_air_index;
 } atmwfs_mkwfs_opts;
 
 /* Replaces make_AtmosphericTurbulence_wavefront_series(slambdaum,

@@ -321,22 +321,27 @@ OR_EXPORT void or_position_step(double *pos, long *cnt, double v, float dt, long
 /*   xpos/ypos  : positions of every layer for this frame (already updated) */
 /*   scoeff     : per-layer phase multiplier (NULL = none, lambda_ref path) */
 /*   sidx/salt  : super-layer index of each layer and super-layer altitudes  */
+/*   hop_n      : optional air index of each hop in the order they run (top */
+/*                down): the hop uses lambda / hop_n[h] instead of the      */
+/*                vacuum lambda of the reference (WFpropagate.c:91)         */
 /* outputs: phase sum (W x W real) and complex field (W x W).               */
 /* ------------------------------------------------------------------------ */
-OR_EXPORT void or_frame(const real_t *const *screens, long M, long L,
-                        const double *xpos, const double *ypos, const double *scoeff,
-                        const long *sidx, const double *salt,
-                        double dx, double zangle, double lambda, long W,
-                        int amplitude, int fresnel, int bicubic,
-                        real_t *phasum, cplx_t *field)
+OR_EXPORT void or_frame_n(const real_t *const *screens, long M, long L,
+                          const double *xpos, const double *ypos, const double *scoeff,
+                          const long *sidx, const double *salt,
+                          double dx, double zangle, double lambda, long W,
+                          int amplitude, int fresnel, int bicubic, const double *hop_n,
+                          real_t *phasum, cplx_t *field)
 {
     long n = W * W;
+    long hop = 0;
     for (long i = 0; i < n; i++) { phasum[i] = 0; field[i].re = 1; field[i].im = 0; }
     double *win = (double *)malloc(sizeof(double) * (size_t)n);
     for (long layer = L - 1; layer >= 0; layer--) {
         if (layer != L - 1 && sidx[layer + 1] != sidx[layer] && amplitude && fresnel) {
             double z = (salt[sidx[layer + 1]] - salt[sidx[layer]]) / cos(zangle);
-            or_fresnel(field, field, W, dx, z, lambda);
+            or_fresnel(field, field, W, dx, z, hop_n ? lambda / hop_n[hop] : lambda);
+            hop++;
         }
         or_window(screens[layer], M, xpos[layer], ypos[layer], W, scoeff ? scoeff[layer] : 1.0, bicubic, win);
 #pragma omp parallel for schedule(static)
@@ -352,6 +357,17 @@ OR_EXPORT void or_frame(const real_t *const *screens, long M, long L,
         }
     }
     free(win);
+}
+
+OR_EXPORT void or_frame(const real_t *const *screens, long M, long L,
+                        const double *xpos, const double *ypos, const double *scoeff,
+                        const long *sidx, const double *salt,
+                        double dx, double zangle, double lambda, long W,
+                        int amplitude, int fresnel, int bicubic,
+                        real_t *phasum, cplx_t *field)
+{
+    or_frame_n(screens, M, L, xpos, ypos, scoeff, sidx, salt, dx, zangle, lambda, W, amplitude, fresnel, bicubic, NULL,
+               phasum, field);
 }
 
 /* reference's rounding idiom  (long)(x + 1000.5) - 1000  */

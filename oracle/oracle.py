@@ -54,6 +54,8 @@ class Oracle:
         L.or_position_step.argtypes = [_dp, _lp, C.c_double, C.c_float, C.c_long]
         L.or_frame.argtypes = [_vp, C.c_long, C.c_long, _dp, _dp, _dp, _lp, _dp, C.c_double, C.c_double, C.c_double,
                                C.c_long, C.c_int, C.c_int, C.c_int, _vp, _vp]
+        L.or_frame_n.argtypes = [_vp, C.c_long, C.c_long, _dp, _dp, _dp, _lp, _dp, C.c_double, C.c_double, C.c_double,
+                                 C.c_long, C.c_int, C.c_int, C.c_int, _dp, _vp, _vp]
         L.or_output_ref.argtypes = [_vp, _vp, C.c_long, C.c_long, C.c_int, _vp, _vp]
         L.or_output_sci.argtypes = [_vp, _vp, C.c_long, C.c_long, C.c_int, _vp, _vp, _vp]
         L.or_output_sci.restype = C.c_long
@@ -112,7 +114,7 @@ class Oracle:
         return p.value, c.value
 
     def frame(self, screens, xpos, ypos, scoeff, sidx, salt, dx, zangle, lam, W, amplitude=1, fresnel=1,
-              bicubic=1):
+              bicubic=1, hop_n=None):
         L = len(screens)
         M = screens[0].shape[0]
         arrs = [np.ascontiguousarray(s, dtype=self.real) for s in screens]
@@ -124,10 +126,11 @@ class Oracle:
         salt = np.ascontiguousarray(salt, np.float64)
         phasum = np.empty((W, W), self.real)
         field = np.empty((W, W), self.cplx)
-        self.lib.or_frame(C.cast(ptrs, C.c_void_p), M, L, xpos.ctypes.data_as(_dp), ypos.ctypes.data_as(_dp),
-                          None if sc is None else sc.ctypes.data_as(_dp), sidx.ctypes.data_as(_lp),
-                          salt.ctypes.data_as(_dp), dx, zangle, lam, W, amplitude, fresnel, bicubic,
-                          _ptr(phasum), _ptr(field))
+        hn = None if hop_n is None else np.ascontiguousarray(hop_n, np.float64)
+        self.lib.or_frame_n(C.cast(ptrs, C.c_void_p), M, L, xpos.ctypes.data_as(_dp), ypos.ctypes.data_as(_dp),
+                            None if sc is None else sc.ctypes.data_as(_dp), sidx.ctypes.data_as(_lp),
+                            salt.ctypes.data_as(_dp), dx, zangle, lam, W, amplitude, fresnel, bicubic,
+                            None if hn is None else hn.ctypes.data_as(_dp), _ptr(phasum), _ptr(field))
         return phasum, field
 
     def output_ref(self, phasum, field, Wout, amplitude=1):

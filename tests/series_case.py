@@ -32,6 +32,7 @@ class Case:
     amplitude: int = 1
     fresnel: int = 1
     seed: int = 7
+    air_index: bool = False   # hops with lambda / n(air) (atmwfs_instance.hop_n)
 
 
 def make_screens(case: Case, o64) -> list[np.ndarray]:
@@ -61,6 +62,7 @@ def scoeff_for(case: Case, lam: float) -> np.ndarray:
 
 def instances(case: Case):
     from atmosphericturbulencesimul_gb300 import MODE_PHASE, MODE_REF, MODE_SCI, InstanceSpec
+    from atmosphericturbulencesimul_gb300.refractivity import hop_air_index
     out = []
     if case.ref:
         mode = MODE_REF if case.amplitude else MODE_PHASE
@@ -71,6 +73,10 @@ def instances(case: Case):
         mode = MODE_SCI if case.amplitude else MODE_PHASE
         out.append(InstanceSpec(lam=lam, mode=mode, src_x=sx, src_y=sy, wf_raw_size=W, wf_size=Wout,
                                 scoeff=scoeff_for(case, lam)))
+    if case.air_index:
+        for I in out:
+            I.hop_n = hop_air_index(case.alt, case.cn2, case.fresnel_bin, I.lam, amplitude=case.amplitude,
+                                    fresnel=case.fresnel, zangle=case.zangle)
     return out
 
 
@@ -106,7 +112,8 @@ def run_oracle(case: Case, o64, screens, nsteps: int):
             orc.step_positions(st[0], st[1], st[2], st[3], st[4], st[5], case.dt, case.M)
             sc = None if I.scoeff is None else I.scoeff.astype(np.float64)
             phasum, fld = o64.frame(screens, st[0], st[1], sc, sidx, salt, float(np.float32(case.pupil)),
-                                    float(np.float32(case.zangle)), I.lam, I.wf_raw_size, case.amplitude, case.fresnel)
+                                    float(np.float32(case.zangle)), I.lam, I.wf_raw_size, case.amplitude, case.fresnel,
+                                    hop_n=I.hop_n)
             from atmosphericturbulencesimul_gb300 import MODE_SCI
             if I.mode == MODE_SCI:
                 pha, amp, _, _ = o64.output_sci(phasum, fld, I.wf_size, case.amplitude)

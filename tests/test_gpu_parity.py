@@ -71,6 +71,21 @@ def test_series_every_tile_configuration(lib, oracle64, monkeypatch, cfg):
     _compare(case, oracle64, 2)
 
 
+def test_series_air_index_hops(lib, oracle64):
+    """The optional lambda / n(air) hops: each hop's transfer function uses
+    the air index at its middle (WFpropagate.c:91 uses the vacuum lambda);
+    the oracle runs the same hops.  The frames must also differ from the
+    vacuum-lambda frames by more than the parity bar."""
+    kw = dict(alt=[0.0, 2000.0, 8000.0], cn2=[0.6, 0.25, 0.15], speed=[10.0, 20.0, 15.0], direction=[0.5236, 2.0, 4.0],
+              M=256, W=128, Wout=128, fresnel_bin=100.0, sci=[(0.5e-6, 0.0, 0.0), (2.2e-6, 4.85e-5, 0.0)])
+    case = Case(air_index=True, **kw)
+    _compare(case, o64 := oracle64, 2)
+    screens = make_screens(case, o64)
+    _, fa, _, _ = run_gpu(case, screens, 1)
+    _, fv, _, _ = run_gpu(Case(**kw), screens, 1)
+    assert max(np.abs(a[1] - v[1]).max() for a, v in zip(fa, fv)) > 1e-4
+
+
 def test_series_single_layer_no_hop(lib, oracle64):
     case = Case(alt=[5000.0], cn2=[1.0], speed=[10.0], direction=[0.5236], M=256, W=256, Wout=256)
     _compare(case, oracle64, 3)

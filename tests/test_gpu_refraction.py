@@ -18,7 +18,7 @@ def test_table_matches_reference(lib):
     from atmosphericturbulencesimul_gb300.mkwfs import refraction_table
     for k in range(3):
         lam, za, site, ref, tr = G[f"case{k}"]
-        r, t = refraction_table([lam], [za], site, G[f"N{k}"][None], G[f"K{k}"][None], DH)
+        r, t = refraction_table([lam], [za], site, G[f"N{k}"][None], G[f"K{k}"][None], DH, where="gpu")
         assert abs(r[0, 0] - ref) < 1e-4, (k, r, ref)
         assert abs(t[0, 0] - tr) < 1e-12
 
@@ -32,7 +32,7 @@ def test_table_grid_matches_host_trace(lib):
     alt = np.arange(Ntab.shape[1]) * DH
     Ktab = np.stack([1e-6 * (1 + k) * np.exp(-alt / 8000.0) for k in range(3)])
     za = np.linspace(0.0, np.deg2rad(80.0), 24)
-    r, t = refraction_table(lams, za, 0.0, Ntab, Ktab, DH)
+    r, t = refraction_table(lams, za, 0.0, Ntab, Ktab, DH, where="gpu")
     assert r.shape == (3, 24) and np.all(np.diff(r, axis=1) > 0)     # refraction grows with zenith angle
     assert r[0, 0] == 0.0 and np.all(t <= 1.0)
     for k, z in [(0, 5), (1, 17), (2, 23)]:

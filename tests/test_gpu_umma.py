@@ -1,0 +1,64 @@
+"""The surrogate's pointwise channel mixing on the tcgen05 tensor cores
+(accumulator in tensor memory), called through the C ABI, against a plain
+PyTorch FP32/FP64 product of the same BF16-rounded operands.
+
+C[b] = W X[b] + bias + beta C[b] with W (o x c) BF16 and X[b] (c x P) FP32
+rounded to BF16 on the way into shared memory; act = gelu(C) (tanh form).
+Tolerance: products of BF16 values are exact in FP32 and c <= 128 of them
+are summed, so the result matches to 1e-5 of the largest |C|; the GELU to
+1e-5 absolute."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _run(lib, W, X, Cm, act, bias, beta, engine):
+    B, c, P = X.shape
+    o = W.shape[0]
+    st = lib.atmwfs_fno_pointwise_dev(C.c_void_p(W.data_ptr()), o, c, C.c_void_p(X.data_ptr()),
+                                      C.c_void_p(Cm.data_ptr()), B, P, beta, C.c_void_p(bias.data_ptr()),
+                                      C.c_void_p(act.data_ptr() if act is not None else 0), engine,
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    return st
+
+
+@pytest.mark.parametrize("o,c,P", [(64, 64, 65536), (128, 64, 4160), (64, 64, 200)])
+def test_tcgen05_pointwise_matches_fp32(lib, o, c, P):
+    from atmosphericturbulencesimul_gb300 import _lib
+    g = torch.Generator(device="cuda").manual_seed(o * 1000 + P)
+    B = 2
+    W = (torch.randn((o, c), device="cuda", generator=g) / 8).to(torch.bfloat16)
+    X = torch.randn((B, c, P), device="cuda", generator=g)
+    bias = torch.randn((o,), device="cuda", generator=g)
+    C0 = torch.randn((B, o, P), device="cuda", generator=g)
+    ref = torch.einsum("oc,bcp->bop", W.double(), X.to(torch.bfloat16).double()) + bias.double()[None, :, None]
+    ref = ref + 0.5 * C0.double()
+    scale = float(ref.abs().max())
+    lib.atmwfs_fno_umma_status(1)
+    errs = {}
+    for engine in (1, 2):
+        Cm = C0.clone()
+        act = torch.empty_like(C0)
+        _lib.check(_run(lib, W, X, Cm, act, bias, 0.5, engine))
+        errs[engine] = float((Cm.double() - ref).abs().max()) / scale
+        if engine == 1:
+            gelu = torch.nn.functional.gelu(Cm, approximate="tanh")
+            assert float((act - gelu).abs().max()) < 1e-5
+    print(f"\no={o} c={c} P={P}: relative error {errs[1]:.3g} (strides as laid out), {errs[2]:.3g} (exchanged)")
+    assert lib.atmwfs_fno_umma_status(1) == 0
+    assert errs[1] < 1e-5, errs
+    assert errs[2] > 1e-2, errs
+
+
+def test_tcgen05_pointwise_rejects_other_shapes(lib):
+    W = torch.zeros((2, 128), device="cuda", dtype=torch.bfloat16)
+    X = torch.zeros((1, 128, 256), device="cuda")
+    Cm = torch.zeros((1, 2, 256), device="cuda")
+    bias = torch.zeros((2,), device="cuda")
+    assert _run(lib, W, X, Cm, None, bias, 0.0, 1) == 1
