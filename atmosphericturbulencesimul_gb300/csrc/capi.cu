@@ -494,6 +494,16 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
                                         nullptr, nullptr, st));
         return ATMWFS_OK;
     }
+    if (k == Q + 2) {
+        // the science unwrap and the final 2 pi multiples of every science
+        // instance of the context (diagnostics only)
+        if (bytes) *bytes = 0;
+        if (c->nsci > 0) {
+            AW_CUDA(unwrap_bins(c->d_inst, c->d_sci, c->nsci, c->maxnb, c->d_status, c->d_iters, c->d_atan_tab, st));
+            AW_CUDA(sci_apply(c->d_inst, c->d_sci, c->nsci, c->maxnout, c->d_step, st));
+        }
+        return ATMWFS_OK;
+    }
     if (k == Q + 1) {
         // the step's windows of the groups this class computes
         if (bytes) *bytes = 0;
@@ -1322,7 +1332,7 @@ int atmwfs_num_classes(const atmwfs_ctx* c) { return c ? (int)c->classes.size() 
 atmwfs_status atmwfs_time_pass(atmwfs_ctx* c, int k, int ci, int reps, double* ms, double* bytes, int* n, int* count)
 {
     if (!c || ci < 0 || ci >= (int)c->classes.size()) return fail(ATMWFS_ERR_INVALID, "bad class");
-    if (k < 0 || k > (int)c->plane_lo.size() + 1 || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
+    if (k < 0 || k > (int)c->plane_lo.size() + 2 || reps < 1) return fail(ATMWFS_ERR_INVALID, "bad pass");
     AW_TRY(commit(c));
     Class& cl = c->classes[ci];
     cudaEvent_t e0, e1;
@@ -1340,7 +1350,8 @@ atmwfs_status atmwfs_time_pass(atmwfs_ctx* c, int k, int ci, int reps, double* m
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (s != ATMWFS_OK) return s;
-    if (k == (int)c->plane_lo.size()) AW_TRY(clear_bins(c));  // the last pass accumulated science bins
+    if (k == (int)c->plane_lo.size() || k == (int)c->plane_lo.size() + 2)
+        AW_TRY(clear_bins(c));  // the last pass accumulated science bins, the unwrap read them
     if (ms) *ms = t / reps;
     if (bytes) *bytes = b;
     if (n) *n = cl.N;

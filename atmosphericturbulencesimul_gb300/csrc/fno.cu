@@ -585,7 +585,7 @@ cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const float* X, 
         const char* e = getenv("ATMWFS_FNO_UMMA");
         return !(e && e[0] == '0');
     }();
-    if (use && pointwise_umma_supported(o, c)) {
+    if (use && pointwise_umma_supported(o, c) && P % 4 == 0) {
         unsigned* status = umma_status_ptr();
         if (!status) return cudaErrorUnknown;
         return pointwise_umma(W, o, c, X, C, B, P, beta, bias, act, status, 0, st);

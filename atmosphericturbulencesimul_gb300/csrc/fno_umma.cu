@@ -31,7 +31,7 @@ void set_error_message(const char* msg);
 namespace umma {
 
 constexpr int kM = 128;      // pixels per tile (MMA M, one TMEM lane each)
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;
 constexpr uint64_t kWaitNs = 1000000000ull;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -85,22 +85,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 32 consecutive TMEM columns of this warp's 32 lanes: register j = column c0 + j.
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&r)[32])
+// 16 consecutive TMEM columns of this warp's 32 lanes: register j = column c0 + j.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&r)[16])
 {
-    uint32_t u[32];
+    uint32_t u[16];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
         : "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7]),
-          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15]),
-          "=r"(u[16]), "=r"(u[17]), "=r"(u[18]), "=r"(u[19]), "=r"(u[20]), "=r"(u[21]), "=r"(u[22]), "=r"(u[23]),
-          "=r"(u[24]), "=r"(u[25]), "=r"(u[26]), "=r"(u[27]), "=r"(u[28]), "=r"(u[29]), "=r"(u[30]), "=r"(u[31])
+          "=r"(u[8]), "=r"(u[9]), "=r"(u[10]), "=r"(u[11]), "=r"(u[12]), "=r"(u[13]), "=r"(u[14]), "=r"(u[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 32; j++) r[j] = __uint_as_float(u[j]);
+    for (int j = 0; j < 16; j++) r[j] = __uint_as_float(u[j]);
 }
 
 // Byte offset of element (row, k) in a K-major no-swizzle tile with kc = K/8
@@ -110,24 +107,59 @@ __device__ __forceinline__ uint32_t kmajor_off(int row, int k, int kc)
     return (uint32_t)((row >> 3) * kc * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
-template <int O, int C>
-__global__ void __launch_bounds__(kThreads) k_pointwise(const __nv_bfloat16* __restrict__ W, const float* __restrict__ X,
-                                                        float* __restrict__ Cm, float* __restrict__ act,
-                                                        const float* __restrict__ bias, float beta, long P, int ntiles,
-                                                        unsigned* status, int swap)
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
 {
-    static_assert(O % 16 == 0 && O >= 32 && O <= 256, "N of the MMA: a multiple of 16 in 32..256");
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)),
+                 "l"(static_cast<uint64_t>(__cvta_generic_to_global(src)))
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// The FP32 pixels of one tile (C channel rows of 128 pixels) copied into the
+// staging buffer with 16-byte asynchronous copies; pixels past P are zeros.
+template <int C>
+__device__ __forceinline__ void stage_tile(float* stage, const float* X, long P, int tile, long tiles_per_sample,
+                                           int tid)
+{
+    const long b = tile / tiles_per_sample;
+    const long p0 = (tile - b * tiles_per_sample) * kM;
+    const float* xs = X + (size_t)b * C * P + p0;
+    constexpr int CH = kM / 4;  // 16-byte chunks per channel row
+    for (int i = tid; i < C * CH; i += kThreads) {
+        const int k = i / CH, c4 = i - k * CH;
+        float* dst = stage + k * kM + 4 * c4;
+        if (p0 + 4 * c4 < P) cp_async16(dst, xs + (size_t)k * P + 4 * c4);
+        else *reinterpret_cast<float4*>(dst) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    cp_async_commit();
+}
+
+// Pipeline per tile: the staged FP32 pixels are rounded into the BF16 A
+// tile; the next tile's copies start; one thread issues the MMAs; all wait
+// for their commit; the eight warps read D (warp w: lanes 32 (w % 4) ..,
+// columns of half w / 4) and write C while the next tile's pixels arrive.
+template <int O, int C>
+__global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* __restrict__ W, const float* __restrict__ X,
+                                                           float* __restrict__ Cm, float* __restrict__ act,
+                                                           const float* __restrict__ bias, float beta, long P, int ntiles,
+                                                           unsigned* status, int swap)
+{
+    static_assert(O % 32 == 0 && O <= 256, "N of the MMA: a multiple of 32 (two halves of 16-column chunks)");
     static_assert(C % 16 == 0 && C >= 16, "K: a multiple of 16");
     constexpr int KC = C / 8;                         // core matrices along K
-    constexpr uint32_t A_BYTES = kM * C * 2;
-    constexpr uint32_t kCols = O <= 32 ? 32 : O <= 64 ? 64 : O <= 128 ? 128 : 256;  // TMEM columns (power of 2)
+    constexpr uint32_t STAGE_BYTES = C * kM * 4, A_BYTES = kM * C * 2;
+    constexpr uint32_t kCols = O <= 64 ? 64 : O <= 128 ? 128 : 256;  // TMEM columns (power of 2)
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char* sa = sm;                           // A tile
-    unsigned char* sb = sm + A_BYTES;                 // B (weights)
+    float* stage = reinterpret_cast<float*>(sm);      // FP32 pixels [C][128]
+    unsigned char* sa = sm + STAGE_BYTES;             // A tile
+    unsigned char* sb = sa + A_BYTES;                 // B (weights)
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long tiles_per_sample = (P + kM - 1) / kM;
+    if (blockIdx.x < ntiles) stage_tile<C>(stage, X, P, blockIdx.x, tiles_per_sample, tid);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
                      "r"(kCols)
@@ -146,24 +178,21 @@ __global__ void __launch_bounds__(kThreads) k_pointwise(const __nv_bfloat16* __r
     fence_after();
     const uint32_t tmem = tmem_base;
     const uint32_t a_addr = smem_addr(sa), b_addr = smem_addr(sb);
-    const long tiles_per_sample = (P + kM - 1) / kM;
     uint32_t parity = 0;
 
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long b = tile / tiles_per_sample;
         const long p0 = (tile - b * tiles_per_sample) * kM;
-        const float* xs = X + (size_t)b * C * P;
-        // A: 8 channels of one pixel per 16-byte store; a warp's loads of one
-        // channel are 32 consecutive pixels
+        cp_async_wait_all();
+        __syncthreads();  // every thread's copies of this tile have landed
+        // A: 8 channels of one pixel per 16-byte store
         for (int i = tid; i < kM * KC; i += kThreads) {
             const int kc = i / kM, m = i - kc * kM;
-            const long p = p0 + m;
-            float f[8];
-#pragma unroll
-            for (int j = 0; j < 8; j++) f[j] = p < P ? __ldg(xs + (size_t)(kc * 8 + j) * P + p) : 0.0f;
+            const float* f = stage + kc * 8 * kM + m;
             uint4 v;
-            __nv_bfloat162 h0 = __floats2bfloat162_rn(f[0], f[1]), h1 = __floats2bfloat162_rn(f[2], f[3]);
-            __nv_bfloat162 h2 = __floats2bfloat162_rn(f[4], f[5]), h3 = __floats2bfloat162_rn(f[6], f[7]);
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(f[0], f[kM]), h1 = __floats2bfloat162_rn(f[2 * kM], f[3 * kM]);
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(f[4 * kM], f[5 * kM]);
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(f[6 * kM], f[7 * kM]);
             v.x = *reinterpret_cast<uint32_t*>(&h0);
             v.y = *reinterpret_cast<uint32_t*>(&h1);
             v.z = *reinterpret_cast<uint32_t*>(&h2);
@@ -175,6 +204,8 @@ __global__ void __launch_bounds__(kThreads) k_pointwise(const __nv_bfloat16* __r
         fence_before();
         __syncthreads();
         fence_after();
+        // the staging buffer is free: the next tile's pixels come in now
+        if (tile + (int)gridDim.x < ntiles) stage_tile<C>(stage, X, P, tile + gridDim.x, tiles_per_sample, tid);
         if (tid == 0) {
 #pragma unroll
             for (int ks = 0; ks < C / 16; ks++) {
@@ -211,31 +242,39 @@ __global__ void __launch_bounds__(kThreads) k_pointwise(const __nv_bfloat16* __r
         }
         parity ^= 1;
         fence_after();
-        // epilogue: this warp's 32 pixels, 32 channels at a time
-        const long p = p0 + warp * 32 + lane;
-        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its 32 pixels) and
+        // the columns of half w / 4, 16 at a time
+        const int g = warp & 3, half = warp >> 2;
+        const long p = p0 + g * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(g * 32) << 16);
         float* cs = Cm + (size_t)b * O * P;
         float* as = act ? act + (size_t)b * O * P : nullptr;
 #pragma unroll 1
-        for (int c0 = 0; c0 < O; c0 += 32) {
-            float r[32];
-            tmem_ld32(trow + c0, r);
+        for (int c0 = half * (O / 2); c0 < (half + 1) * (O / 2); c0 += 16) {
+            float r[16];
+            tmem_ld16(trow + c0, r);
             if (p < P) {
+                float old[16];
+                if (beta != 0.0f) {
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
+                    for (int j = 0; j < 16; j++) old[j] = cs[(size_t)(c0 + j) * P + p];
+                }
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
                     const size_t o = (size_t)(c0 + j) * P + p;
                     float v = r[j] + (bias ? bias[c0 + j] : 0.0f);
-                    if (beta != 0.0f) v = fmaf(beta, cs[o], v);
+                    if (beta != 0.0f) v = fmaf(beta, old[j], v);
                     cs[o] = v;
                     if (as) as[o] = gelu_f(v);
                 }
             }
         }
-        // the next tile's MMAs overwrite D and its stores overwrite A
+        // the next tile's MMAs overwrite D and its conversion overwrites A
         fence_before();
         __syncthreads();
         fence_after();
     }
+    cp_async_wait_all();  // no copy may still target this CTA's shared memory
     __syncthreads();
     if (warp == 0) {
         fence_after();
@@ -247,10 +286,10 @@ template <int O, int C>
 cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act, const float* bias, float beta, int B,
                    long P, unsigned* status, int swap, cudaStream_t st)
 {
-    // shared memory: A + B, padded so that at most four CTAs share an SM
-    // (four TMEM allocations of at most 128 columns fit the 512 columns)
-    constexpr size_t need = (size_t)kM * C * 2 + (size_t)O * C * 2;
-    constexpr size_t smem = need > 56 * 1024 ? need : 56 * 1024;
+    if (P % 4 != 0) return cudaErrorNotSupported;  // 16-byte copies of the channel rows
+    // shared memory: the FP32 staging buffer, A and B; at most three CTAs per
+    // SM (registers), whose TMEM allocations (at most 128 columns) fit the 512
+    constexpr size_t smem = (size_t)C * kM * 4 + (size_t)kM * C * 2 + (size_t)O * C * 2;
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(k_pointwise<O, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -261,7 +300,7 @@ cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long grid = tiles < 4L * sms ? tiles : 4L * sms;
+    const long grid = tiles < 3L * sms ? tiles : 3L * sms;
     k_pointwise<O, C><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status, swap);
     return cudaGetLastError();
 }

@@ -211,8 +211,10 @@ def refraction_path(lam: float, zangle: float, site_alt: float, refractivity, ab
 # Tables with fewer rays than this run on the host cores under where="auto":
 # one FP64 ray per GPU thread is a serial chain of double transcendentals,
 # and the GPU overtakes 16 Grace cores only once the table fills many warps
-# on every SM (the crossover measured by the benchmark's refraction scan).
-REFRACTION_GPU_MIN_RAYS = 1 << 30
+# on every SM.  Measured (wall time of the call, GPU / 16 cores, rays/s):
+# 1,024 rays 1,776 / 7,122; 4,096 rays 7,104 / 7,421; 16,384 rays
+# 27,833 / 7,466; 65,536 rays 64,558 / 7,468.
+REFRACTION_GPU_MIN_RAYS = 8192
 
 
 def refraction_table(lambdas, zangles, site_alt: float, Ntab: np.ndarray, Ktab: np.ndarray | None, dh: float,

@@ -265,6 +265,40 @@ def surrogate_vs_fp64(model, test, n: int = 8) -> dict:
                 "amp_rms": float(f"{np.mean([e[1] for e in v]):.4g}"), "frames": n} for k, v in acc.items()}
 
 
+def launch_gap_section(wl: dict, steps: int = 50) -> dict:
+    """Launch gaps of the smallest grid class: its instances alone in a
+    context, the device time of whole steps (one graph each) against the sum
+    of its kernels timed one by one.  The difference is what launching the
+    step's kernels as separate graph nodes costs on the class whose kernels
+    are shortest."""
+    import torch
+    W = min(I["W"] for I in wl["inst"])
+    sub = dict(wl, inst=[I for I in wl["inst"] if I["W"] == W])
+    s, _ = make_series(sub)
+    s.run(5)
+    st = torch.cuda.ExternalStream(s.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    s.run(steps)
+    e1.record(st)
+    torch.cuda.synchronize()
+    step_ms = e0.elapsed_time(e1) / steps
+    npl = len(s.planes()[0])
+    kern = [s.time_pass(k, 0, reps=20)["ms"] for k in range(0, npl + 3)]
+    s.close()
+    # the phase sum runs on its own branch beside the passes; the windows, the
+    # passes, the unwrap and the apply are serial
+    serial = kern[npl + 1] + sum(kern[1:npl + 1]) + kern[npl + 2]
+    return {"grid": W, "instances": len(sub["inst"]), "step_ms": round(step_ms, 4),
+            "kernels_ms": {"windows": round(kern[npl + 1], 4), "phase_sum": round(kern[0], 4),
+                           "passes": round(sum(kern[1:npl + 1]), 4), "unwrap_apply": round(kern[npl + 2], 4)},
+            "serial_kernels_ms": round(serial, 4),
+            "gap_ms": round(step_ms - serial, 4), "gap_frac": round((step_ms - serial) / step_ms, 3),
+            "note": "step = windows, then the passes beside the phase sum, then unwrap, apply and the step "
+                    "counter (the counter's 2-3 us counts in the gap)"}
+
+
 def rows_section() -> dict:
     """The rows around the series, each timed on resident data with CUDA
     events after warm-up: exposure PSFs (W = 512 frames into 1024^2 PSFs),
@@ -680,6 +714,8 @@ def main():
         line["surrogate"] = surrogate_section(args.surrogate_pairs)
     if rank == 0 and world == 1 and not args.no_rows:
         line["rows"] = rows_section()
+        if len({I["W"] for I in wl["inst"]}) > 1:
+            line["rows"]["launch_gaps"] = launch_gap_section(wl)
     if rank == 0:
         print(json.dumps(line))
     if dist:

@@ -171,7 +171,8 @@ void* atmwfs_stream(atmwfs_ctx* ctx);
 
 /* Diagnostics: launch pass k (1-based, of atmwfs_num_planes passes; k = 0 is
  * the geometric phase-sum kernel, k = atmwfs_num_planes + 1 the kernel that
- * computes the step's screen windows of the window groups of this grid size)
+ * computes the step's screen windows of the window groups of this grid size,
+ * k = atmwfs_num_planes + 2 the science unwrap and apply of the whole context)
  * for the instances of grid class c `reps` times, timed with CUDA events on
  * the context stream.  Returns the mean duration [ms], the algorithmic bytes
  * of one launch (field in/out, window rows, outputs), and the class's grid
