@@ -211,13 +211,45 @@ __device__ __forceinline__ void fft2_ct(float2* v, float2* xrow, int t, const fl
     stage_dft<E, RB, -1>(v);
 }
 
-template <int N, int T, int E>
-__device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev)
+// Square two-stage plans with one work item per thread (64 = 8 x 8,
+// 256 = 16 x 16, 1024 = 32 x 32): the second stage's twiddles of a thread,
+// w^(t r) for r = 1 .. R - 1, are the same in every transform of every row the
+// thread holds (forward and inverse alike), so a pass can load them once into
+// registers instead of reading the table in each of its four transforms.
+template <int N>
+AW_HD constexpr bool reg_twiddles()
+{
+    return Stages<N>::S == 2 && Stages<N>::R0 == Stages<N>::R1 && Plan<N>::E == Stages<N>::R1;
+}
+template <int N>
+AW_HD constexpr int reg_twiddle_count() { return reg_twiddles<N>() ? Stages<N>::R1 - 1 : 1; }
+
+// The same transform with the second stage's twiddles in registers:
+// twr[r - 1] = w^((t mod RA) r), RB = E (one work item per thread).
+template <int N, int T, int E, int RA, int RB>
+__device__ __forceinline__ void fft2_ct_r(float2* v, float2* xrow, int t, const float2* twr)
+{
+    static_assert(E == RB, "one work item per thread");
+    stage_dft<E, RA, -1>(v);
+    row_sync<T>();
+    stage_store<N, T, E, RA, 1>(v, xrow, t);
+    row_sync<T>();
+    stage_load<N, T, E, RB>(v, xrow, t);
+#pragma unroll
+    for (int r = 1; r < RB; r++) v[r] = cmul(v[r], twr[r - 1]);
+    stage_dft<E, RB, -1>(v);
+}
+
+template <int N, int T, int E, bool RT = false>
+__device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev,
+                                       const float2* twr = nullptr)
 {
     if (ds > 0.0f) conj_all<E>(v);     // inverse = conj(forward(conj))
     if constexpr (Stages<N>::S == 2) {
         constexpr int R0 = Stages<N>::R0, R1 = Stages<N>::R1;
-        if constexpr (R0 == R1) {
+        if constexpr (RT && reg_twiddles<N>()) {
+            fft2_ct_r<N, T, E, R0, R1>(v, xrow, t, twr);
+        } else if constexpr (R0 == R1) {
             fft2_ct<N, T, E, R0, R1>(v, xrow, t, tw + tw_offset<N>(rev, 1));
         } else {
             if (rev) fft2_ct<N, T, E, R1, R0>(v, xrow, t, tw + tw_offset<N>(1, 1));
@@ -246,16 +278,16 @@ __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const flo
 
 // 1-D Fresnel propagation (forward FFT, transfer table, inverse FFT) with a
 // single copy of the transform code.
-template <int N, int T, int E>
+template <int N, int T, int E, bool RT = false>
 __device__ __forceinline__ void prop_row_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw,
-                                            const float2* __restrict__ h)
+                                            const float2* __restrict__ h, const float2* twr = nullptr)
 {
     constexpr int RL = last_radix<N>();
     // IFFT(H FFT(x)) = conj(FFT(conj(H FFT(x)))): the first conjugation is
     // folded into the transfer multiply, both transforms run the forward code
 #pragma unroll 1
     for (int dir = 0; dir < 2; dir++) {
-        fft_rt<N, T, E>(v, xrow, t, tw, -1.0f, dir);
+        fft_rt<N, T, E, RT>(v, xrow, t, tw, -1.0f, dir, twr);
         if (dir == 0) {
 #pragma unroll
             for (int s = 0; s < E; s++) {
@@ -349,6 +381,17 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
         }
     }
 
+    // second-stage twiddles of the square plans, kept in registers by the
+    // series passes with two propagations (FP32 transforms) in the tile
+    // configurations that leave room for them (at most three CTAs per SM)
+    constexpr bool kRegTw = reg_twiddles<N>() && !HP && MINB <= 3 && (OPS & OP_PROP1) != 0 && (OPS & OP_PROP2) != 0;
+    float2 twr[reg_twiddle_count<N>()];
+    if constexpr (kRegTw) {
+        constexpr int R = Stages<N>::R1;
+#pragma unroll
+        for (int r = 1; r < R; r++) twr[r - 1] = __ldg(tw + tw_offset<N>(0, 1) + r * Stages<N>::R0 + (t % Stages<N>::R0));
+    }
+
     float2 v[E];
     if constexpr ((OPS & OP_LOAD) != 0) {
         const float2* src = (I ? I->fld[a.src] : a.ext_in) + (size_t)y * N + t;
@@ -399,7 +442,8 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                                     reinterpret_cast<const __half2*>(I->Hh) + (size_t)hop * N);
             } else {
                 const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
-                prop_row_rt<N, T, E>(v, xrow, t, tw, h);
+                if constexpr (kRegTw) prop_row_rt<N, T, E, true>(v, xrow, t, tw, h, twr);
+                else prop_row_rt<N, T, E>(v, xrow, t, tw, h);
             }
         }
     }
