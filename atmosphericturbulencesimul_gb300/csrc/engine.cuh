@@ -162,10 +162,9 @@ constexpr TileCfg tile_cfg(int N, int c)
 constexpr int kPhasumThreads = 256;
 inline int phasum_blocks(int Nout)
 {
-    // about eight items per thread: two per iteration, four iterations
     const long items = (long)Nout * Nout / ((Nout % 4) == 0 ? 4 : 1);
-    const long n = (items + 8L * kPhasumThreads - 1) / (8L * kPhasumThreads);
-    return (int)(n < 1 ? 1 : n);
+    const long n = (items + kPhasumThreads - 1) / kPhasumThreads;
+    return (int)(n < 1024 ? n : 1024);
 }
 
 // Rows per CTA of configuration 0 (unit operators).

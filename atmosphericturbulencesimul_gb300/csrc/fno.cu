@@ -57,7 +57,7 @@ namespace atmwfs {
 // tcgen05 pointwise product (fno_umma.cu)
 bool pointwise_umma_supported(int o, int c);
 cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                           const float* bias, float* act, unsigned* status, int swap, cudaStream_t st);
+                           const float* bias, float* act, unsigned* status, int swap, bool write_c, cudaStream_t st);
 unsigned* umma_status_ptr();
 }  // namespace atmwfs
 
@@ -578,8 +578,10 @@ const float* last_h(const atmwfs_fno* f) { return f->u[f->cfg.layers - 1]; }
 // The pointwise products of the forward pass: on the tcgen05 tensor cores for
 // the shapes compiled there (the Fourier layers' width x width mixing and the
 // first projection), unless ATMWFS_FNO_UMMA=0; the mma.sync product otherwise.
+// keep_c = false (inference with an activation output): the pre-activation
+// C is not stored where only the backward pass would read it.
 cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                          const float* bias, cudaStream_t st, float* act = nullptr)
+                          const float* bias, cudaStream_t st, float* act = nullptr, bool keep_c = true)
 {
     static const bool use = [] {
         const char* e = getenv("ATMWFS_FNO_UMMA");
@@ -588,12 +590,14 @@ cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const float* X, 
     if (use && pointwise_umma_supported(o, c) && P % 4 == 0) {
         unsigned* status = umma_status_ptr();
         if (!status) return cudaErrorUnknown;
-        return pointwise_umma(W, o, c, X, C, B, P, beta, bias, act, status, 0, st);
+        return pointwise_umma(W, o, c, X, C, B, P, beta, bias, act, status, 0, keep_c || !act, st);
     }
     return pointwise(W, o, c, X, C, B, P, beta, bias, st, act);
 }
 
-atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st)
+// training = false (inference): pre-activations that only the backward pass
+// reads are not stored.
+atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st, bool training)
 {
     const atmwfs_fno_cfg& c = f->cfg;
     const long P = (long)c.grid * c.grid;
@@ -606,10 +610,10 @@ atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStre
         // (the last layer has no activation: its u is the projection's input)
         FN_TRY(spectral_fwd(f, l, f->h[l], f->u[l], B, st));
         FN_CUDA(pointwise_fwd(pb + f->L.W[l], c.width, c.width, f->h[l], f->u[l], B, P, 1.0f, pf + f->L.b[l], st,
-                              l + 1 < c.layers ? f->h[l + 1] : nullptr));
+                              l + 1 < c.layers ? f->h[l + 1] : nullptr, training));
     }
     FN_CUDA(pointwise_fwd(pb + f->L.proj1_W, c.proj, c.width, last_h(f), f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st,
-                          f->q));
+                          f->q, training));
     FN_CUDA(pointwise(pb + f->L.proj2_W, c.nout, c.proj, f->q, out, B, P, 0.0f, pf + f->L.proj2_b, st));
     return ATMWFS_OK;
 }
@@ -750,7 +754,7 @@ atmwfs_status atmwfs_fno_zero_grads(atmwfs_fno* f, void* stream)
 atmwfs_status atmwfs_fno_forward(atmwfs_fno* f, const float* in, float* out, int batch, void* stream)
 {
     if (!f || !in || !out || batch < 1) return err(ATMWFS_ERR_INVALID, "bad arguments");
-    return forward(f, in, out, batch, (cudaStream_t)stream);
+    return forward(f, in, out, batch, (cudaStream_t)stream, false);
 }
 
 atmwfs_status atmwfs_fno_loss_grad(atmwfs_fno* f, const float* in, const float* target, float* out, int batch,
@@ -758,7 +762,7 @@ atmwfs_status atmwfs_fno_loss_grad(atmwfs_fno* f, const float* in, const float* 
 {
     if (!f || !in || !target || !out || batch < 1) return err(ATMWFS_ERR_INVALID, "bad arguments");
     cudaStream_t st = (cudaStream_t)stream;
-    FN_TRY(forward(f, in, out, batch, st));
+    FN_TRY(forward(f, in, out, batch, st, true));
     const long n = (long)batch * f->cfg.nout * f->cfg.grid * f->cfg.grid;
     FN_CUDA(cudaMemsetAsync(f->d_loss, 0, sizeof(double), st));
     k_mse<<<grid_for(n), 256, 0, st>>>(out, target, f->dout, n, f->d_loss);

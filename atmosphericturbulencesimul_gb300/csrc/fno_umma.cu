@@ -143,7 +143,7 @@ template <int O, int C>
 __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* __restrict__ W, const float* __restrict__ X,
                                                            float* __restrict__ Cm, float* __restrict__ act,
                                                            const float* __restrict__ bias, float beta, long P, int ntiles,
-                                                           unsigned* status, int swap)
+                                                           unsigned* status, int swap, int write_c)
 {
     static_assert(O % 32 == 0 && O <= 256, "N of the MMA: a multiple of 32 (two halves of 16-column chunks)");
     static_assert(C % 16 == 0 && C >= 16, "K: a multiple of 16");
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
                     const size_t o = (size_t)(c0 + j) * P + p;
                     float v = r[j] + (bias ? bias[c0 + j] : 0.0f);
                     if (beta != 0.0f) v = fmaf(beta, old[j], v);
-                    cs[o] = v;
+                    if (write_c) cs[o] = v;
                     if (as) as[o] = gelu_f(v);
                 }
             }
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
 
 template <int O, int C>
 cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act, const float* bias, float beta, int B,
-                   long P, unsigned* status, int swap, cudaStream_t st)
+                   long P, unsigned* status, int swap, int write_c, cudaStream_t st)
 {
     if (P % 4 != 0) return cudaErrorNotSupported;  // 16-byte copies of the channel rows
     // shared memory: the FP32 staging buffer, A and B; at most three CTAs per
@@ -301,7 +301,8 @@ cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long grid = tiles < 3L * sms ? tiles : 3L * sms;
-    k_pointwise<O, C><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status, swap);
+    k_pointwise<O, C><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status, swap,
+                                                              write_c);
     return cudaGetLastError();
 }
 
@@ -314,10 +315,11 @@ cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act
 bool pointwise_umma_supported(int o, int c) { return (o == 64 && c == 64) || (o == 128 && c == 64); }
 
 cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                           const float* bias, float* act, unsigned* status, int swap, cudaStream_t st)
+                           const float* bias, float* act, unsigned* status, int swap, bool write_c, cudaStream_t st)
 {
-    if (o == 64 && c == 64) return umma::launch<64, 64>(W, X, C, act, bias, beta, B, P, status, swap, st);
-    if (o == 128 && c == 64) return umma::launch<128, 64>(W, X, C, act, bias, beta, B, P, status, swap, st);
+    const int wc = write_c ? 1 : 0;
+    if (o == 64 && c == 64) return umma::launch<64, 64>(W, X, C, act, bias, beta, B, P, status, swap, wc, st);
+    if (o == 128 && c == 64) return umma::launch<128, 64>(W, X, C, act, bias, beta, B, P, status, swap, wc, st);
     return cudaErrorNotSupported;
 }
 
@@ -358,7 +360,7 @@ extern "C" atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, c
         set_error_message("atmwfs_fno_pointwise_dev: status symbol");
         return ATMWFS_ERR_CUDA;
     }
-    const cudaError_t e = pointwise_umma(w, o, c, X, C, batch, P, beta, bias, act, status, engine == 2, st);
+    const cudaError_t e = pointwise_umma(w, o, c, X, C, batch, P, beta, bias, act, status, engine == 2, true, st);
     if (e != cudaSuccess) {
         set_error_message(cudaGetErrorString(e));
         return ATMWFS_ERR_CUDA;

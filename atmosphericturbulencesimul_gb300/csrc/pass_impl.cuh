@@ -613,87 +613,52 @@ __global__ void __launch_bounds__(PassGeom<N, RR>::NT)
 // two-sum (compensated FP32; the reference keeps a float sum).  Independent
 // of the field, so it runs beside the propagation passes.
 // ---------------------------------------------------------------------------
-// One item: four pixels of one row (one when the crop breaks 16-byte
-// vectors).
-struct PhasumItem {
-    size_t o;   // window offset
-    long q;     // phase-sum offset
-    bool ok;
-};
-
-// Each thread keeps two items in flight and requests the samples of up to
-// eight layers of both before it sums them (from the top layer down): the
-// kernel is bound by the latency of the window reads, not by arithmetic.
+// Four pixels of one row per thread (one when the crop breaks 16-byte
+// vectors); every layer's samples are requested before the sums, which take
+// the layers from the top down.  The window reads hit L2 (the instances of a
+// direction run one after the other); their rate bounds the kernel.
 template <int N>
-__global__ void __launch_bounds__(kPhasumThreads, 2) k_phasum(const __grid_constant__ PassArgs a)
+__global__ void __launch_bounds__(kPhasumThreads) k_phasum(const __grid_constant__ PassArgs a)
 {
-    constexpr int kChunk = 8;
-    constexpr int kItems = 2;
     const InstDev* I = a.inst + blockIdx.y;
     const int off = I->off, Nout = I->Nout, L = a.L;
     const size_t ws = (size_t)I->wstride;
     const bool v4 = (off % 4) == 0 && (Nout % 4) == 0;
     const int per = v4 ? 4 : 1;
     const long nitems = (long)Nout * Nout / per;
-    const long stride = (long)gridDim.x * blockDim.x;
-    for (long k0 = (long)blockIdx.x * blockDim.x + threadIdx.x; k0 < nitems; k0 += kItems * stride) {
-        PhasumItem it[kItems];
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < nitems; k += (long)gridDim.x * blockDim.x) {
+        const long q = k * per;
+        const int yy = (int)(q / Nout), xx = (int)(q - (long)yy * Nout);
+        const size_t o = (size_t)(yy + off) * ws + (size_t)(xx + off);
+        float4 w[kMaxLayers];
 #pragma unroll
-        for (int u = 0; u < kItems; u++) {
-            const long k = k0 + u * stride;
-            it[u].ok = k < nitems;
-            const long q = (it[u].ok ? k : 0) * per;
-            const int yy = (int)(q / Nout), xx = (int)(q - (long)yy * Nout);
-            it[u].q = q;
-            it[u].o = (size_t)(yy + off) * ws + (size_t)(xx + off);
-        }
-        float hi[kItems][4], lo[kItems][4];
-#pragma unroll
-        for (int u = 0; u < kItems; u++)
-#pragma unroll
-            for (int j = 0; j < 4; j++) hi[u][j] = lo[u][j] = 0.0f;
-        for (int top = L - 1; top >= 0; top -= kChunk) {
-            float4 w[kItems][kChunk];
-#pragma unroll
-            for (int c = 0; c < kChunk; c++) {
-                const int l = top - c;
-                if (l < 0) break;
-                const float* src = I->win[0][l];
-#pragma unroll
-                for (int u = 0; u < kItems; u++)
-                    w[u][c] = !it[u].ok ? make_float4(0.0f, 0.0f, 0.0f, 0.0f)
-                              : v4      ? __ldg(reinterpret_cast<const float4*>(src + it[u].o))
-                                        : make_float4(__ldg(src + it[u].o), 0.0f, 0.0f, 0.0f);
-            }
-#pragma unroll
-            for (int c = 0; c < kChunk; c++) {
-                const int l = top - c;
-                if (l < 0) break;
-                const float sc = I->scoeff[l];
-#pragma unroll
-                for (int u = 0; u < kItems; u++) {
-                    const float wv[4] = {w[u][c].x, w[u][c].y, w[u][c].z, w[u][c].w};
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        const float val = __fmul_rn(wv[j], sc);
-                        float sum, err;
-                        two_sum(hi[u][j], val, sum, err);
-                        hi[u][j] = sum;
-                        lo[u][j] = __fadd_rn(lo[u][j], err);
-                    }
-                }
+        for (int l = 0; l < kMaxLayers; l++) {
+            if (l < L) {
+                const float* src = I->win[0][l] + o;
+                w[l] = v4 ? __ldg(reinterpret_cast<const float4*>(src)) : make_float4(__ldg(src), 0.0f, 0.0f, 0.0f);
             }
         }
+        float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int u = 0; u < kItems; u++) {
-            if (!it[u].ok) continue;
-            float* dst = I->phisum + it[u].q;
-            if (v4) {
-                *reinterpret_cast<float4*>(dst) = make_float4(__fadd_rn(hi[u][0], lo[u][0]), __fadd_rn(hi[u][1], lo[u][1]),
-                                                              __fadd_rn(hi[u][2], lo[u][2]), __fadd_rn(hi[u][3], lo[u][3]));
-            } else {
-                dst[0] = __fadd_rn(hi[u][0], lo[u][0]);
+        for (int l = kMaxLayers - 1; l >= 0; l--) {
+            if (l >= L) continue;
+            const float sc = I->scoeff[l];
+            const float wv[4] = {w[l].x, w[l].y, w[l].z, w[l].w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float val = __fmul_rn(wv[j], sc);
+                float sum, err;
+                two_sum(hi[j], val, sum, err);
+                hi[j] = sum;
+                lo[j] = __fadd_rn(lo[j], err);
             }
+        }
+        float* dst = I->phisum + q;
+        if (v4) {
+            *reinterpret_cast<float4*>(dst) = make_float4(__fadd_rn(hi[0], lo[0]), __fadd_rn(hi[1], lo[1]),
+                                                          __fadd_rn(hi[2], lo[2]), __fadd_rn(hi[3], lo[3]));
+        } else {
+            dst[0] = __fadd_rn(hi[0], lo[0]);
         }
     }
 }

@@ -284,8 +284,9 @@ def frame_flops(cfg: FnoConfig) -> float:
 def frame_bytes(cfg: FnoConfig) -> float:
     """HBM bytes one inference frame moves in the library's dataflow (FP32
     activations, each product reading its operands and writing its result
-    once, the residual add and the activation in the pointwise epilogue):
-    the algorithmic figure of the surrogate's HBM roofline."""
+    once, the residual add and the activation in the pointwise epilogue,
+    pre-activations that only training reads not stored): the algorithmic
+    figure of the surrogate's HBM roofline."""
     G, m, w, P = cfg.grid, cfg.modes, cfg.width, cfg.grid * cfg.grid
     spec_rows = 4.0 * w * G * 2 * m           # one x-DFT image (2m columns per row)
     modes = 4.0 * w * 2 * m * m               # one mode image (complex m x m per channel)
@@ -295,9 +296,9 @@ def frame_bytes(cfg: FnoConfig) -> float:
                  + 2 * modes                  # z -> y (mode mixing)
                  + modes + spec_rows          # y -> bb
                  + spec_rows + 4.0 * w * P    # bb -> u
-                 + 4 * 4.0 * w * P)           # pointwise: read h, u; write u, gelu(u)
+                 + 3 * 4.0 * w * P)           # pointwise: read h, u; write gelu(u) (the last layer: u)
     b += cfg.layers * per_layer
-    b += 4.0 * w * P + 2 * 4.0 * cfg.proj * P  # projection 1 (+ gelu)
+    b += 4.0 * w * P + 4.0 * cfg.proj * P      # projection 1: gelu output only
     b += 4.0 * cfg.proj * P + 4.0 * cfg.nout * P
     return b
 
