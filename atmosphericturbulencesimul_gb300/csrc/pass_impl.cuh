@@ -343,6 +343,9 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // ---------------------------------------------------------------------------
 // the pass kernel
 // ---------------------------------------------------------------------------
+// series passes (as opposed to the unit operators, which have no instance)
+#define I_SERIES(ops) (((ops) & (OP_GATHER | OP_EPI)) != 0)
+
 template <int N, int RR, int MINB, int OPS, bool ALIAS, bool HP = false>
 __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     k_pass(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps, const float2* __restrict__ tw)
@@ -382,9 +385,10 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     }
 
     // second-stage twiddles of the square plans, kept in registers by the
-    // series passes with two propagations (FP32 transforms) in the tile
-    // configurations that leave room for them (at most three CTAs per SM)
-    constexpr bool kRegTw = reg_twiddles<N>() && !HP && MINB <= 3 && (OPS & OP_PROP1) != 0 && (OPS & OP_PROP2) != 0;
+    // series passes (FP32 transforms) in the tile configurations that leave
+    // room for them (at most three CTAs per SM)
+    constexpr bool kRegTw = reg_twiddles<N>() && !HP && MINB <= 3 && I_SERIES(OPS) &&
+                            (OPS & (OP_PROP1 | OP_PROP2)) != 0;
     float2 twr[reg_twiddle_count<N>()];
     if constexpr (kRegTw) {
         constexpr int R = Stages<N>::R1;

@@ -76,3 +76,19 @@ def test_w2048_step(lib, oracle64):
     case = bench_case(W=2048, Wout=2048, sci=[(1.6e-6, TEN, 0.0)])
     ms = compare(case, oracle64, 1)
     _report("W=2048", ms)
+
+
+def test_window_group_of_mixed_grids(lib, oracle64):
+    """One direction, wavelengths on 256, 512 and 1024 grids with crops: a
+    single window group whose windows are 1024 x 1024; the smaller grids read
+    its top-left corner, the crops their centre.  A second direction makes a
+    second group."""
+    case = bench_case(W=1024, Wout=1024, sci=[
+        (0.6e-6, 0.0, 0.0, 256, 200),
+        (0.9e-6, 0.0, 0.0, 512, 512),
+        (1.3e-6, 0.0, 0.0, 1024, 800),
+        (2.0e-6, 0.0, 0.0, 256, 256),
+        (1.1e-6, TEN, TEN, 512, 300),
+    ])
+    ms = compare(case, oracle64, 2)
+    _report("one window group, mixed grids", ms)
