@@ -56,8 +56,9 @@ struct FnoLayout {
 namespace atmwfs {
 // tcgen05 pointwise product (fno_umma.cu)
 bool pointwise_umma_supported(int o, int c);
-cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                           const float* bias, float* act, unsigned* status, int swap, bool write_c, cudaStream_t st);
+cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const void* X, int x_bf16, float* C, int B, long P,
+                           float beta, const float* bias, void* act, int a_bf16, unsigned* status, int swap, bool write_c,
+                           cudaStream_t st);
 unsigned* umma_status_ptr();
 }  // namespace atmwfs
 
@@ -502,7 +503,7 @@ static cudaError_t gemm_args(GemmArgs& g, float beta, cudaStream_t st)
 }
 
 // spectral convolution of layer l: spec = S_l(h)
-atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, float* spec, int B, cudaStream_t st)
+atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const void* h, int h_bf16, float* spec, int B, cudaStream_t st)
 {
     const atmwfs_fno_cfg& c = f->cfg;
     const int G = c.grid, m = c.modes, w = c.width;
@@ -512,7 +513,7 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const float* h, float* spec, in
     {   // a[p][y][bc][kx] = sum_x h[bc][y][x] Fx[x][p m + kx]
         GemmArgs g{};
         g.M = (int)(BW * G); g.N = 2 * m; g.K = G;
-        g.A = h; g.lda = G; g.B = f->Fx; g.ldb = 2 * m; g.C = a; g.ldc = 2 * m;
+        g.A = h; g.a_bf16 = h_bf16; g.lda = G; g.B = f->Fx; g.ldb = 2 * m; g.C = a; g.ldc = 2 * m;
         g.rdiv = G; g.c_lo = Nc; g.c_hi = m; g.cdiv = m; g.cc_hi = (long)G * Nc;
         FN_CUDA(gemm_args(g, 0.0f, st));
     }
@@ -575,28 +576,39 @@ atmwfs_status spectral_bwd(atmwfs_fno* f, int l, const float* ds, float* dh, int
 // activation, so it is that layer's u.
 const float* last_h(const atmwfs_fno* f) { return f->u[f->cfg.layers - 1]; }
 
-// The pointwise products of the forward pass: on the tcgen05 tensor cores for
-// the shapes compiled there (the Fourier layers' width x width mixing and the
-// first projection), unless ATMWFS_FNO_UMMA=0; the mma.sync product otherwise.
-// keep_c = false (inference with an activation output): the pre-activation
-// C is not stored where only the backward pass would read it.
-cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                          const float* bias, cudaStream_t st, float* act = nullptr, bool keep_c = true)
+// The pointwise products of the forward pass run on the tcgen05 tensor cores
+// for the shapes compiled there (the Fourier layers' width x width mixing and
+// the first projection), unless ATMWFS_FNO_UMMA=0; on the mma.sync product
+// otherwise.
+bool umma_enabled()
 {
     static const bool use = [] {
         const char* e = getenv("ATMWFS_FNO_UMMA");
         return !(e && e[0] == '0');
     }();
-    if (use && pointwise_umma_supported(o, c) && P % 4 == 0) {
+    return use;
+}
+
+// keep_c = false (inference with an activation output): the pre-activation C
+// is not stored where only the backward pass would read it.  x_bf16 / a_bf16:
+// the input and the activation output are stored as BF16 (tcgen05 path only).
+cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const void* X, int x_bf16, float* C, int B, long P,
+                          float beta, const float* bias, cudaStream_t st, void* act = nullptr, int a_bf16 = 0,
+                          bool keep_c = true)
+{
+    if (umma_enabled() && pointwise_umma_supported(o, c) && P % 8 == 0) {
         unsigned* status = umma_status_ptr();
         if (!status) return cudaErrorUnknown;
-        return pointwise_umma(W, o, c, X, C, B, P, beta, bias, act, status, 0, keep_c || !act, st);
+        return pointwise_umma(W, o, c, X, x_bf16, C, B, P, beta, bias, act, a_bf16, status, 0, keep_c || !act, st);
     }
-    return pointwise(W, o, c, X, C, B, P, beta, bias, st, act);
+    if (x_bf16 || a_bf16) return cudaErrorNotSupported;
+    return pointwise(W, o, c, (const float*)X, C, B, P, beta, bias, st, (float*)act);
 }
 
 // training = false (inference): pre-activations that only the backward pass
-// reads are not stored.
+// reads are not stored, and on the tcgen05 path the activations between the
+// Fourier layers (h[1..]) and of the projection (q) are stored as BF16.  That
+// changes no value: every product that reads them rounds its operands to BF16.
 atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st, bool training)
 {
     const atmwfs_fno_cfg& c = f->cfg;
@@ -604,17 +616,23 @@ atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStre
     FN_TRY(ensure_batch(f, B));
     const __nv_bfloat16* pb = f->pbf;
     const float* pf = f->params;
+    const int bf = (!training && umma_enabled() && P % 8 == 0 && pointwise_umma_supported(c.width, c.width) &&
+                    pointwise_umma_supported(c.proj, c.width))
+                       ? 1
+                       : 0;
     FN_CUDA(pointwise(pb + f->L.lift_W, c.width, c.nin, x, f->h[0], B, P, 0.0f, pf + f->L.lift_b, st));
     for (int l = 0; l < c.layers; l++) {
         // u = S_l(h) + W_l h + b_l; h' = gelu(u) from the same epilogue
         // (the last layer has no activation: its u is the projection's input)
-        FN_TRY(spectral_fwd(f, l, f->h[l], f->u[l], B, st));
-        FN_CUDA(pointwise_fwd(pb + f->L.W[l], c.width, c.width, f->h[l], f->u[l], B, P, 1.0f, pf + f->L.b[l], st,
-                              l + 1 < c.layers ? f->h[l + 1] : nullptr, training));
+        const int hb = l > 0 ? bf : 0;  // h[0] comes from the lift in FP32
+        FN_TRY(spectral_fwd(f, l, f->h[l], hb, f->u[l], B, st));
+        FN_CUDA(pointwise_fwd(pb + f->L.W[l], c.width, c.width, f->h[l], hb, f->u[l], B, P, 1.0f, pf + f->L.b[l], st,
+                              l + 1 < c.layers ? f->h[l + 1] : nullptr, bf, training));
     }
-    FN_CUDA(pointwise_fwd(pb + f->L.proj1_W, c.proj, c.width, last_h(f), f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st,
-                          f->q, training));
-    FN_CUDA(pointwise(pb + f->L.proj2_W, c.nout, c.proj, f->q, out, B, P, 0.0f, pf + f->L.proj2_b, st));
+    FN_CUDA(pointwise_fwd(pb + f->L.proj1_W, c.proj, c.width, last_h(f), 0, f->qpre, B, P, 0.0f, pf + f->L.proj1_b, st,
+                          f->q, bf, training));
+    FN_CUDA(gemm(c.nout, (int)P, c.proj, pb + f->L.proj2_W, c.proj, 0, 1, f->q, P, 0, bf, out, P, 0.0f, B, 0,
+                 (long)c.proj * P, (long)c.nout * P, pf + f->L.proj2_b, 1, st));
     return ATMWFS_OK;
 }
 

@@ -116,42 +116,48 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// The FP32 pixels of one tile (C channel rows of 128 pixels) copied into the
-// staging buffer with 16-byte asynchronous copies; pixels past P are zeros.
-template <int C>
-__device__ __forceinline__ void stage_tile(float* stage, const float* X, long P, int tile, long tiles_per_sample,
-                                           int tid)
+// The pixels of one tile (C channel rows of 128 pixels, FP32 or BF16 as
+// stored) copied into the staging buffer with 16-byte asynchronous copies;
+// pixels past P are zeros.
+template <int C, typename TX>
+__device__ __forceinline__ void stage_tile(TX* stage, const TX* X, long P, int tile, long tiles_per_sample, int tid)
 {
+    constexpr int EPC = 16 / sizeof(TX);  // elements per 16-byte chunk
     const long b = tile / tiles_per_sample;
     const long p0 = (tile - b * tiles_per_sample) * kM;
-    const float* xs = X + (size_t)b * C * P + p0;
-    constexpr int CH = kM / 4;  // 16-byte chunks per channel row
+    const TX* xs = X + (size_t)b * C * P + p0;
+    constexpr int CH = kM / EPC;  // chunks per channel row
     for (int i = tid; i < C * CH; i += kThreads) {
-        const int k = i / CH, c4 = i - k * CH;
-        float* dst = stage + k * kM + 4 * c4;
-        if (p0 + 4 * c4 < P) cp_async16(dst, xs + (size_t)k * P + 4 * c4);
-        else *reinterpret_cast<float4*>(dst) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const int k = i / CH, ch = i - k * CH;
+        TX* dst = stage + k * kM + EPC * ch;
+        if (p0 + EPC * ch < P) cp_async16(dst, xs + (size_t)k * P + EPC * ch);
+        else *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
     }
     cp_async_commit();
 }
+
+__device__ __forceinline__ float to_f(float x) { return x; }
+__device__ __forceinline__ float to_f(__nv_bfloat16 x) { return __bfloat162float(x); }
+__device__ __forceinline__ void put(float* p, float v) { *p = v; }
+__device__ __forceinline__ void put(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
 
 // Pipeline per tile: the staged FP32 pixels are rounded into the BF16 A
 // tile; the next tile's copies start; one thread issues the MMAs; all wait
 // for their commit; the eight warps read D (warp w: lanes 32 (w % 4) ..,
 // columns of half w / 4) and write C while the next tile's pixels arrive.
-template <int O, int C>
-__global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* __restrict__ W, const float* __restrict__ X,
-                                                           float* __restrict__ Cm, float* __restrict__ act,
+template <int O, int C, typename TX, typename TA>
+__global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* __restrict__ W, const TX* __restrict__ X,
+                                                           float* __restrict__ Cm, TA* __restrict__ act,
                                                            const float* __restrict__ bias, float beta, long P, int ntiles,
                                                            unsigned* status, int swap, int write_c)
 {
     static_assert(O % 32 == 0 && O <= 256, "N of the MMA: a multiple of 32 (two halves of 16-column chunks)");
     static_assert(C % 16 == 0 && C >= 16, "K: a multiple of 16");
     constexpr int KC = C / 8;                         // core matrices along K
-    constexpr uint32_t STAGE_BYTES = C * kM * 4, A_BYTES = kM * C * 2;
+    constexpr uint32_t STAGE_BYTES = C * kM * sizeof(TX), A_BYTES = kM * C * 2;
     constexpr uint32_t kCols = O <= 64 ? 64 : O <= 128 ? 128 : 256;  // TMEM columns (power of 2)
     extern __shared__ __align__(1024) unsigned char sm[];
-    float* stage = reinterpret_cast<float*>(sm);      // FP32 pixels [C][128]
+    TX* stage = reinterpret_cast<TX*>(sm);            // the tile's pixels [C][128]
     unsigned char* sa = sm + STAGE_BYTES;             // A tile
     unsigned char* sb = sa + A_BYTES;                 // B (weights)
     __shared__ __align__(8) uint64_t bar;
@@ -159,7 +165,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long tiles_per_sample = (P + kM - 1) / kM;
-    if (blockIdx.x < ntiles) stage_tile<C>(stage, X, P, blockIdx.x, tiles_per_sample, tid);
+    if (blockIdx.x < ntiles) stage_tile<C, TX>(stage, X, P, blockIdx.x, tiles_per_sample, tid);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
                      "r"(kCols)
@@ -188,11 +194,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
         // A: 8 channels of one pixel per 16-byte store
         for (int i = tid; i < kM * KC; i += kThreads) {
             const int kc = i / kM, m = i - kc * kM;
-            const float* f = stage + kc * 8 * kM + m;
+            const TX* f = stage + kc * 8 * kM + m;
             uint4 v;
-            __nv_bfloat162 h0 = __floats2bfloat162_rn(f[0], f[kM]), h1 = __floats2bfloat162_rn(f[2 * kM], f[3 * kM]);
-            __nv_bfloat162 h2 = __floats2bfloat162_rn(f[4 * kM], f[5 * kM]);
-            __nv_bfloat162 h3 = __floats2bfloat162_rn(f[6 * kM], f[7 * kM]);
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(to_f(f[0]), to_f(f[kM]));
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(to_f(f[2 * kM]), to_f(f[3 * kM]));
+            __nv_bfloat162 h2 = __floats2bfloat162_rn(to_f(f[4 * kM]), to_f(f[5 * kM]));
+            __nv_bfloat162 h3 = __floats2bfloat162_rn(to_f(f[6 * kM]), to_f(f[7 * kM]));
             v.x = *reinterpret_cast<uint32_t*>(&h0);
             v.y = *reinterpret_cast<uint32_t*>(&h1);
             v.z = *reinterpret_cast<uint32_t*>(&h2);
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
         __syncthreads();
         fence_after();
         // the staging buffer is free: the next tile's pixels come in now
-        if (tile + (int)gridDim.x < ntiles) stage_tile<C>(stage, X, P, tile + gridDim.x, tiles_per_sample, tid);
+        if (tile + (int)gridDim.x < ntiles) stage_tile<C, TX>(stage, X, P, tile + gridDim.x, tiles_per_sample, tid);
         if (tid == 0) {
 #pragma unroll
             for (int ks = 0; ks < C / 16; ks++) {
@@ -248,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
         const long p = p0 + g * 32 + lane;
         const uint32_t trow = tmem + ((uint32_t)(g * 32) << 16);
         float* cs = Cm + (size_t)b * O * P;
-        float* as = act ? act + (size_t)b * O * P : nullptr;
+        TA* as = act ? act + (size_t)b * O * P : nullptr;
 #pragma unroll 1
         for (int c0 = half * (O / 2); c0 < (half + 1) * (O / 2); c0 += 16) {
             float r[16];
@@ -265,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
                     float v = r[j] + (bias ? bias[c0 + j] : 0.0f);
                     if (beta != 0.0f) v = fmaf(beta, old[j], v);
                     if (write_c) cs[o] = v;
-                    if (as) as[o] = gelu_f(v);
+                    if (as) put(as + o, gelu_f(v));
                 }
             }
         }
@@ -282,17 +289,18 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
     }
 }
 
-template <int O, int C>
-cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act, const float* bias, float beta, int B,
-                   long P, unsigned* status, int swap, int write_c, cudaStream_t st)
+template <int O, int C, typename TX, typename TA>
+cudaError_t launch(const __nv_bfloat16* W, const TX* X, float* Cm, TA* act, const float* bias, float beta, int B, long P,
+                   unsigned* status, int swap, int write_c, cudaStream_t st)
 {
-    if (P % 4 != 0) return cudaErrorNotSupported;  // 16-byte copies of the channel rows
-    // shared memory: the FP32 staging buffer, A and B; at most three CTAs per
-    // SM (registers), whose TMEM allocations (at most 128 columns) fit the 512
-    constexpr size_t smem = (size_t)C * kM * 4 + (size_t)kM * C * 2 + (size_t)O * C * 2;
+    if (P % 8 != 0) return cudaErrorNotSupported;  // 16-byte copies of the channel rows
+    // shared memory: the staging buffer, A and B; at most three CTAs per SM
+    // (registers), whose TMEM allocations (at most 128 columns) fit the 512
+    constexpr size_t smem = (size_t)C * kM * sizeof(TX) + (size_t)kM * C * 2 + (size_t)O * C * 2;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_pointwise<O, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_pointwise<O, C, TX, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
@@ -301,9 +309,25 @@ cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long grid = tiles < 3L * sms ? tiles : 3L * sms;
-    k_pointwise<O, C><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status, swap,
-                                                              write_c);
+    k_pointwise<O, C, TX, TA><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status,
+                                                                        swap, write_c);
     return cudaGetLastError();
+}
+
+// Storage types of the input (x_bf16) and of the activation output (a_bf16).
+template <int O, int C>
+cudaError_t launch_t(const __nv_bfloat16* W, const void* X, int x_bf16, float* Cm, void* act, int a_bf16,
+                     const float* bias, float beta, int B, long P, unsigned* status, int swap, int write_c,
+                     cudaStream_t st)
+{
+    using bf = __nv_bfloat16;
+    if (x_bf16) {
+        if (a_bf16) return launch<O, C, bf, bf>(W, (const bf*)X, Cm, (bf*)act, bias, beta, B, P, status, swap, write_c, st);
+        return launch<O, C, bf, float>(W, (const bf*)X, Cm, (float*)act, bias, beta, B, P, status, swap, write_c, st);
+    }
+    if (a_bf16)
+        return launch<O, C, float, bf>(W, (const float*)X, Cm, (bf*)act, bias, beta, B, P, status, swap, write_c, st);
+    return launch<O, C, float, float>(W, (const float*)X, Cm, (float*)act, bias, beta, B, P, status, swap, write_c, st);
 }
 
 }  // namespace umma
@@ -314,12 +338,15 @@ cudaError_t launch(const __nv_bfloat16* W, const float* X, float* Cm, float* act
 // and stay on the mma.sync product.
 bool pointwise_umma_supported(int o, int c) { return (o == 64 && c == 64) || (o == 128 && c == 64); }
 
-cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, int B, long P, float beta,
-                           const float* bias, float* act, unsigned* status, int swap, bool write_c, cudaStream_t st)
+cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const void* X, int x_bf16, float* C, int B, long P,
+                           float beta, const float* bias, void* act, int a_bf16, unsigned* status, int swap, bool write_c,
+                           cudaStream_t st)
 {
     const int wc = write_c ? 1 : 0;
-    if (o == 64 && c == 64) return umma::launch<64, 64>(W, X, C, act, bias, beta, B, P, status, swap, wc, st);
-    if (o == 128 && c == 64) return umma::launch<128, 64>(W, X, C, act, bias, beta, B, P, status, swap, wc, st);
+    if (o == 64 && c == 64)
+        return umma::launch_t<64, 64>(W, X, x_bf16, C, act, a_bf16, bias, beta, B, P, status, swap, wc, st);
+    if (o == 128 && c == 64)
+        return umma::launch_t<128, 64>(W, X, x_bf16, C, act, a_bf16, bias, beta, B, P, status, swap, wc, st);
     return cudaErrorNotSupported;
 }
 
@@ -360,7 +387,7 @@ extern "C" atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, c
         set_error_message("atmwfs_fno_pointwise_dev: status symbol");
         return ATMWFS_ERR_CUDA;
     }
-    const cudaError_t e = pointwise_umma(w, o, c, X, C, batch, P, beta, bias, act, status, engine == 2, true, st);
+    const cudaError_t e = pointwise_umma(w, o, c, X, 0, C, batch, P, beta, bias, act, 0, status, engine == 2, true, st);
     if (e != cudaSuccess) {
         set_error_message(cudaGetErrorString(e));
         return ATMWFS_ERR_CUDA;

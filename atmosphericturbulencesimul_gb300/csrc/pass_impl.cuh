@@ -385,9 +385,10 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     }
 
     // second-stage twiddles of the square plans, kept in registers by the
-    // series passes (FP32 transforms) in the tile configurations that leave
-    // room for them (at most three CTAs per SM)
-    constexpr bool kRegTw = reg_twiddles<N>() && !HP && MINB <= 3 && I_SERIES(OPS) &&
+    // series passes (FP32 transforms) without the output epilogue (whose
+    // registers they would crowd: measured slower there) in the tile
+    // configurations that leave room for them (at most three CTAs per SM)
+    constexpr bool kRegTw = reg_twiddles<N>() && !HP && MINB <= 3 && I_SERIES(OPS) && (OPS & OP_EPI) == 0 &&
                             (OPS & (OP_PROP1 | OP_PROP2)) != 0;
     float2 twr[reg_twiddle_count<N>()];
     if constexpr (kRegTw) {

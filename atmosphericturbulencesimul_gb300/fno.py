@@ -282,24 +282,29 @@ def frame_flops(cfg: FnoConfig) -> float:
 
 
 def frame_bytes(cfg: FnoConfig) -> float:
-    """HBM bytes one inference frame moves in the library's dataflow (FP32
-    activations, each product reading its operands and writing its result
-    once, the residual add and the activation in the pointwise epilogue,
-    pre-activations that only training reads not stored): the algorithmic
+    """HBM bytes one inference frame moves in the library's dataflow: FP32
+    spectral images and pre-activations, each product reading its operands
+    and writing its result once, the residual add and the activation in the
+    pointwise epilogue, pre-activations that only training reads not stored,
+    and the activations between Fourier layers (h[1..]) and of the projection
+    (q) stored as BF16 (the tcgen05 path, the default).  The algorithmic
     figure of the surrogate's HBM roofline."""
     G, m, w, P = cfg.grid, cfg.modes, cfg.width, cfg.grid * cfg.grid
     spec_rows = 4.0 * w * G * 2 * m           # one x-DFT image (2m columns per row)
     modes = 4.0 * w * 2 * m * m               # one mode image (complex m x m per channel)
-    b = 4.0 * cfg.nin * P + 4.0 * w * P       # lift
-    per_layer = (4.0 * w * P + spec_rows      # h -> a
-                 + spec_rows + modes          # a -> z
-                 + 2 * modes                  # z -> y (mode mixing)
-                 + modes + spec_rows          # y -> bb
-                 + spec_rows + 4.0 * w * P    # bb -> u
-                 + 3 * 4.0 * w * P)           # pointwise: read h, u; write gelu(u) (the last layer: u)
-    b += cfg.layers * per_layer
-    b += 4.0 * w * P + 4.0 * cfg.proj * P      # projection 1: gelu output only
-    b += 4.0 * cfg.proj * P + 4.0 * cfg.nout * P
+    b = 4.0 * cfg.nin * P + 4.0 * w * P       # lift: x in, h[0] out (FP32)
+    for l in range(cfg.layers):
+        eh = 4.0 if l == 0 else 2.0           # bytes of one element of h[l]
+        last = l == cfg.layers - 1
+        b += (eh * w * P + spec_rows          # h -> a
+              + spec_rows + modes             # a -> z
+              + 2 * modes                     # z -> y (mode mixing)
+              + modes + spec_rows             # y -> bb
+              + spec_rows + 4.0 * w * P       # bb -> u
+              + eh * w * P + 4.0 * w * P      # pointwise: read h, u
+              + (4.0 if last else 2.0) * w * P)  # write u (last layer) or gelu(u) as BF16
+    b += 4.0 * w * P + 2.0 * cfg.proj * P      # projection 1: u in, gelu as BF16 out
+    b += 2.0 * cfg.proj * P + 4.0 * cfg.nout * P  # projection 2
     return b
 
 

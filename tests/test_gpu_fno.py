@@ -58,6 +58,30 @@ def test_forward_matches_oracle(lib, small):
     assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 2e-2
 
 
+def test_inference_dataflow_at_the_tensor_core_shapes(lib):
+    """Width 64 and projection 128: the pointwise products run on tcgen05 and
+    inference stores the activations between layers as BF16 (training keeps
+    FP32).  Every product rounds its operands to BF16, so inference and the
+    training forward give identical outputs; both match the FP64 oracle."""
+    from atmosphericturbulencesimul_gb300 import fno as F
+    cfg = fo.Cfg(nin=8, width=64, modes=8, layers=3, proj=128, nout=2, grid=32)
+    rng = np.random.default_rng(11)
+    p = fo.init_params(cfg, 5)
+    x = rng.standard_normal((2, cfg.nin, cfg.grid, cfg.grid)).astype(np.float32)
+    m = F.Surrogate(F.FnoConfig(**cfg.__dict__), seed=1)
+    m.set_params(p.astype(np.float32))
+    xt = torch.tensor(x, device="cuda")
+    out_inf = m.forward(xt)
+    out_trn = torch.empty_like(out_inf)
+    m.loss_grad(xt, torch.zeros_like(out_inf), out=out_trn)
+    torch.cuda.synchronize()
+    assert torch.equal(out_inf, out_trn)
+    ref = fo.forward(p, x, cfg)
+    got = out_inf.cpu().numpy()
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 2e-2
+    m.close()
+
+
 def test_gradients_match_oracle(lib, small):
     m, p, x, t = small
     m.zero_grads()
