@@ -97,21 +97,46 @@ AW_HD constexpr int brev(int i)
     return r;
 }
 
-// In-register radix-R DFT, natural order in and out (radix-2 decimation in
-// frequency followed by a compile-time bit-reversal relabelling).
+// In-register radix-R DFT, natural order in and out: decimation in frequency
+// taking the radix-2 levels two at a time (radix 2^2), then a last radix-2
+// level when log2 R is odd, followed by a compile-time bit-reversal
+// relabelling.  A pair of levels with span s works on x0..x3 = v[k + {0, s,
+// 2s, 3s}] of each block of 4s:
+//   c0 = x0 + x2, c1 = x1 + x3, c2 = (x0 - x2) + W4 (x1 - x3), c3 = (x0 - x2) - W4 (x1 - x3)
+//   v[k] = c0 + c1,  v[k + s] = (c0 - c1) W^2k,  v[k + 2s] = c2 W^k,  v[k + 3s] = c3 W^3k
+// with W = exp(D 2 pi i / 4s) and W4 = W^s = D i (a register swap): the same
+// values, at the same places, as the two radix-2 levels (whose second level
+// multiplies by W^k and W^(k + s) = W4 W^k), with three twiddle multiplies per
+// group of four instead of four.
 template <int R, int D>
 AW_HD void dft(float2* v)
 {
+    constexpr int L2 = R == 2 ? 1 : R == 4 ? 2 : R == 8 ? 3 : R == 16 ? 4 : R == 32 ? 5 : 6;
+    int span = R / 4;
     AW_UNROLL
-    for (int span = R / 2; span >= 1; span >>= 1) {
+    for (int lv = 0; lv + 1 < L2; lv += 2, span /= 4) {
         AW_UNROLL
-        for (int base = 0; base < R; base += 2 * span) {
+        for (int base = 0; base < R; base += 4 * span) {
             AW_UNROLL
             for (int k = 0; k < span; k++) {
-                const float2 a = v[base + k], b = v[base + k + span];
-                v[base + k] = cadd(a, b);
-                v[base + k + span] = tw_const<D>(csub(a, b), k, 2 * span);
+                const float2 x0 = v[base + k], x1 = v[base + k + span];
+                const float2 x2 = v[base + k + 2 * span], x3 = v[base + k + 3 * span];
+                const float2 c0 = cadd(x0, x2), c1 = cadd(x1, x3);
+                const float2 d0 = csub(x0, x2), d1 = tw_const<D>(csub(x1, x3), 1, 4);
+                v[base + k] = cadd(c0, c1);
+                v[base + k + span] = tw_const<D>(csub(c0, c1), 2 * k, 4 * span);
+                v[base + k + 2 * span] = tw_const<D>(cadd(d0, d1), k, 4 * span);
+                v[base + k + 3 * span] = tw_const<D>(csub(d0, d1), 3 * k, 4 * span);
             }
+        }
+    }
+    if constexpr ((L2 & 1) != 0) {
+        // the last radix-2 level (span 1: no twiddles)
+        AW_UNROLL
+        for (int base = 0; base < R; base += 2) {
+            const float2 a = v[base], b = v[base + 1];
+            v[base] = cadd(a, b);
+            v[base + 1] = csub(a, b);
         }
     }
     float2 t[R];

@@ -607,7 +607,8 @@ cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const void* X, i
 
 // training = false (inference): pre-activations that only the backward pass
 // reads are not stored, and on the tcgen05 path the activations between the
-// Fourier layers (h[1..]) and of the projection (q) are stored as BF16.  That
+// Fourier layers (h[1..]) and of the projection (q) are stored as BF16
+// (unless ATMWFS_FNO_BF16_ACT=0).  That
 // changes no value: every product that reads them rounds its operands to BF16.
 atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st, bool training)
 {
@@ -616,7 +617,11 @@ atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStre
     FN_TRY(ensure_batch(f, B));
     const __nv_bfloat16* pb = f->pbf;
     const float* pf = f->params;
-    const int bf = (!training && umma_enabled() && P % 8 == 0 && pointwise_umma_supported(c.width, c.width) &&
+    static const bool bf_env = [] {
+        const char* e = getenv("ATMWFS_FNO_BF16_ACT");
+        return !(e && e[0] == '0');
+    }();
+    const int bf = (!training && bf_env && umma_enabled() && P % 8 == 0 && pointwise_umma_supported(c.width, c.width) &&
                     pointwise_umma_supported(c.proj, c.width))
                        ? 1
                        : 0;
