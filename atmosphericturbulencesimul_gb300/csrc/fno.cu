@@ -606,10 +606,12 @@ cudaError_t pointwise_fwd(const __nv_bfloat16* W, int o, int c, const void* X, i
 }
 
 // training = false (inference): pre-activations that only the backward pass
-// reads are not stored, and on the tcgen05 path the activations between the
-// Fourier layers (h[1..]) and of the projection (q) are stored as BF16
-// (unless ATMWFS_FNO_BF16_ACT=0).  That
-// changes no value: every product that reads them rounds its operands to BF16.
+// reads are not stored.  With ATMWFS_FNO_BF16_ACT=1 (tcgen05 path) the
+// activations between the Fourier layers (h[1..]) and of the projection (q)
+// are also stored as BF16, which changes no value (every product that reads
+// them rounds its operands to BF16) but measured slower (4,180 against
+// 4,460 frames/s at 256^2: the spectral product reads its BF16 operand in
+// 8-byte pieces), so FP32 storage is the default.
 atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStream_t st, bool training)
 {
     const atmwfs_fno_cfg& c = f->cfg;
@@ -617,10 +619,8 @@ atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStre
     FN_TRY(ensure_batch(f, B));
     const __nv_bfloat16* pb = f->pbf;
     const float* pf = f->params;
-    static const bool bf_env = [] {
-        const char* e = getenv("ATMWFS_FNO_BF16_ACT");
-        return !(e && e[0] == '0');
-    }();
+    const char* bf_var = getenv("ATMWFS_FNO_BF16_ACT");  // read per call: a test switches it
+    const bool bf_env = bf_var && bf_var[0] == '1';
     const int bf = (!training && bf_env && umma_enabled() && P % 8 == 0 && pointwise_umma_supported(c.width, c.width) &&
                     pointwise_umma_supported(c.proj, c.width))
                        ? 1

@@ -281,20 +281,23 @@ def frame_flops(cfg: FnoConfig) -> float:
     return f
 
 
-def frame_bytes(cfg: FnoConfig) -> float:
+def frame_bytes(cfg: FnoConfig, bf16_act: bool | None = None) -> float:
     """HBM bytes one inference frame moves in the library's dataflow: FP32
     spectral images and pre-activations, each product reading its operands
     and writing its result once, the residual add and the activation in the
-    pointwise epilogue, pre-activations that only training reads not stored,
-    and the activations between Fourier layers (h[1..]) and of the projection
-    (q) stored as BF16 (the tcgen05 path, the default).  The algorithmic
-    figure of the surrogate's HBM roofline."""
+    pointwise epilogue, pre-activations that only training reads not stored;
+    with bf16_act (ATMWFS_FNO_BF16_ACT=1; off by default) the activations
+    between Fourier layers (h[1..]) and of the projection (q) stored as BF16.
+    The algorithmic figure of the surrogate's HBM roofline."""
+    if bf16_act is None:
+        bf16_act = os.environ.get("ATMWFS_FNO_BF16_ACT", "0") == "1"
+    ea = 2.0 if bf16_act else 4.0
     G, m, w, P = cfg.grid, cfg.modes, cfg.width, cfg.grid * cfg.grid
     spec_rows = 4.0 * w * G * 2 * m           # one x-DFT image (2m columns per row)
     modes = 4.0 * w * 2 * m * m               # one mode image (complex m x m per channel)
     b = 4.0 * cfg.nin * P + 4.0 * w * P       # lift: x in, h[0] out (FP32)
     for l in range(cfg.layers):
-        eh = 4.0 if l == 0 else 2.0           # bytes of one element of h[l]
+        eh = 4.0 if l == 0 else ea            # bytes of one element of h[l]
         last = l == cfg.layers - 1
         b += (eh * w * P + spec_rows          # h -> a
               + spec_rows + modes             # a -> z
@@ -302,9 +305,9 @@ def frame_bytes(cfg: FnoConfig) -> float:
               + modes + spec_rows             # y -> bb
               + spec_rows + 4.0 * w * P       # bb -> u
               + eh * w * P + 4.0 * w * P      # pointwise: read h, u
-              + (4.0 if last else 2.0) * w * P)  # write u (last layer) or gelu(u) as BF16
-    b += 4.0 * w * P + 2.0 * cfg.proj * P      # projection 1: u in, gelu as BF16 out
-    b += 2.0 * cfg.proj * P + 4.0 * cfg.nout * P  # projection 2
+              + (4.0 if last else ea) * w * P)  # write u (last layer) or gelu(u)
+    b += 4.0 * w * P + ea * cfg.proj * P       # projection 1: u in, gelu out
+    b += ea * cfg.proj * P + 4.0 * cfg.nout * P  # projection 2
     return b
 
 

@@ -110,27 +110,41 @@ def make_series(wl: dict, ring: int = 1, fft_fp16: bool = False):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clock / throttle sampling during the timed regions: samples
+    every 20 ms from before the first region (the tool takes a moment to
+    start) to after the last; only samples stamped inside a region count
+    (mark() opens and closes one)."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.regions = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(1.0)  # the first samples come after the tool has started
         except Exception:
             self.proc = None
         return self
 
+    def mark(self, start: bool) -> None:
+        import datetime
+        now = datetime.datetime.now()
+        if start:
+            self.regions.append([now, None])
+        elif self.regions:
+            self.regions[-1][1] = now
+
     def __exit__(self, *exc):
         self.out = ""
         if self.proc:
+            time.sleep(0.1)
             self.proc.terminate()
             try:
                 self.out, _ = self.proc.communicate(timeout=5)
@@ -138,15 +152,25 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self) -> dict:
-        rows = [r for r in csv.reader(io.StringIO(getattr(self, "out", "") or "")) if len(r) >= 9]
+        import datetime
+        rows = [r for r in csv.reader(io.StringIO(getattr(self, "out", "") or "")) if len(r) >= 10]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
-        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+
+        def stamp(r):
+            try:
+                return datetime.datetime.strptime(r[0].strip(), "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                return None
+        inside = [r for r in rows if stamp(r) and any(a <= stamp(r) <= (b or a) for a, b in self.regions)]
+        use = inside or rows
+        sm = [float(r[2]) for r in use if r[2].strip().replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in use if r[3].strip().replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip().lower() == "active"})
+        reasons = sorted({names[k] for r in use for k in range(4) if r[6 + k].strip().lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(use),
+                "window": "inside the timed regions" if inside else "whole sampling span (none stamped inside)"}
 
 
 def peaks() -> dict:
@@ -629,27 +653,32 @@ def main():
 
     # device-resident throughput
     barrier()
+    ff = s.frame_floats
+    nslots = 2
+    pha_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
+    amp_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
     with ClockSampler(local) as clk:
+        barrier()
+        clk.mark(True)
         torch.cuda.nvtx.range_push("timed")  # profilers can select the timed steps
         e0.record(stream)
         s.run(args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
-    barrier()
+        clk.mark(False)
+        barrier()
+        # end to end through the C ABI with host buffers
+        barrier()
+        clk.mark(True)
+        w0 = time.perf_counter()
+        s.run(args.steps, pha_ptr=pha_h.data_ptr(), amp_ptr=amp_h.data_ptr(), nslots=nslots)
+        torch.cuda.synchronize()
+        w1 = time.perf_counter()
+        clk.mark(False)
     # max over ranks of the device time, frames of all ranks
     t, _, value = aggregate(e0.elapsed_time(e1) / 1e3, args.steps * ninst, device="cuda")
-
-    # end to end through the C ABI with host buffers
-    ff = s.frame_floats
-    nslots = 2
-    pha_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
-    amp_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
-    barrier()
-    w0 = time.perf_counter()
-    s.run(args.steps, pha_ptr=pha_h.data_ptr(), amp_ptr=amp_h.data_ptr(), nslots=nslots)
-    torch.cuda.synchronize()
-    _, _, e2e = aggregate(time.perf_counter() - w0, args.steps * ninst, device="cuda")
+    _, _, e2e = aggregate(w1 - w0, args.steps * ninst, device="cuda")
 
     # roofline of the dominant pass (timed live on the engine stream)
     npl = len(s.planes()[0])

@@ -58,12 +58,16 @@ def test_forward_matches_oracle(lib, small):
     assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 2e-2
 
 
-def test_inference_dataflow_at_the_tensor_core_shapes(lib):
-    """Width 64 and projection 128: the pointwise products run on tcgen05 and
-    inference stores the activations between layers as BF16 (training keeps
-    FP32).  Every product rounds its operands to BF16, so inference and the
-    training forward give identical outputs; both match the FP64 oracle."""
+@pytest.mark.parametrize("bf16_act", ["0", "1"])
+def test_inference_dataflow_at_the_tensor_core_shapes(lib, monkeypatch, bf16_act):
+    """Width 64 and projection 128: the pointwise products run on tcgen05;
+    inference skips the pre-activations only training reads and, with
+    ATMWFS_FNO_BF16_ACT=1, stores the activations between layers as BF16
+    (training keeps FP32).  Every product rounds its operands to BF16, so
+    inference and the training forward give identical outputs; both match the
+    FP64 oracle."""
     from atmosphericturbulencesimul_gb300 import fno as F
+    monkeypatch.setenv("ATMWFS_FNO_BF16_ACT", bf16_act)
     cfg = fo.Cfg(nin=8, width=64, modes=8, layers=3, proj=128, nout=2, grid=32)
     rng = np.random.default_rng(11)
     p = fo.init_params(cfg, 5)
