@@ -110,10 +110,10 @@ def make_series(wl: dict, ring: int = 1, fft_fp16: bool = False):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed regions: samples
-    every 20 ms from before the first region (the tool takes a moment to
-    start) to after the last; only samples stamped inside a region count
-    (mark() opens and closes one)."""
+    """nvidia-smi clock / throttle sampling during the timed region: samples
+    every 20 ms from before the region (the tool takes a moment to start) to
+    after it; only samples stamped inside a region count (mark() opens and
+    closes one)."""
     Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -657,6 +657,9 @@ def main():
     nslots = 2
     pha_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
     amp_h = torch.empty(nslots * ff, dtype=torch.float32, pin_memory=True)
+    # the clock sampler polls the driver every 20 ms: it runs around the
+    # device-resident steps only, since its queries can slow the host-driven
+    # copies of the end-to-end run
     with ClockSampler(local) as clk:
         barrier()
         clk.mark(True)
@@ -667,15 +670,12 @@ def main():
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
         clk.mark(False)
-        barrier()
-        # end to end through the C ABI with host buffers
-        barrier()
-        clk.mark(True)
-        w0 = time.perf_counter()
-        s.run(args.steps, pha_ptr=pha_h.data_ptr(), amp_ptr=amp_h.data_ptr(), nslots=nslots)
-        torch.cuda.synchronize()
-        w1 = time.perf_counter()
-        clk.mark(False)
+    # end to end through the C ABI with host buffers
+    barrier()
+    w0 = time.perf_counter()
+    s.run(args.steps, pha_ptr=pha_h.data_ptr(), amp_ptr=amp_h.data_ptr(), nslots=nslots)
+    torch.cuda.synchronize()
+    w1 = time.perf_counter()
     # max over ranks of the device time, frames of all ranks
     t, _, value = aggregate(e0.elapsed_time(e1) / 1e3, args.steps * ninst, device="cuda")
     _, _, e2e = aggregate(w1 - w0, args.steps * ninst, device="cuda")
