@@ -619,12 +619,14 @@ __global__ void __launch_bounds__(PassGeom<N, RR>::NT)
 // of the field, so it runs beside the propagation passes.
 // ---------------------------------------------------------------------------
 // Four pixels of one row per thread (one when the crop breaks 16-byte
-// vectors); every layer's samples are requested before the sums, which take
-// the layers from the top down.  The window reads hit L2 (the instances of a
-// direction run one after the other); their rate bounds the kernel.
+// vectors); the samples of up to eight layers are requested together before
+// their sums, which take the layers from the top down.  The kernel waits on
+// the window reads (L2 hits: the instances of a direction run one after the
+// other), so it keeps its registers low for four CTAs per SM.
 template <int N>
-__global__ void __launch_bounds__(kPhasumThreads) k_phasum(const __grid_constant__ PassArgs a)
+__global__ void __launch_bounds__(kPhasumThreads, 4) k_phasum(const __grid_constant__ PassArgs a)
 {
+    constexpr int kChunk = 8;
     const InstDev* I = a.inst + blockIdx.y;
     const int off = I->off, Nout = I->Nout, L = a.L;
     const size_t ws = (size_t)I->wstride;
@@ -635,27 +637,28 @@ __global__ void __launch_bounds__(kPhasumThreads) k_phasum(const __grid_constant
         const long q = k * per;
         const int yy = (int)(q / Nout), xx = (int)(q - (long)yy * Nout);
         const size_t o = (size_t)(yy + off) * ws + (size_t)(xx + off);
-        float4 w[kMaxLayers];
-#pragma unroll
-        for (int l = 0; l < kMaxLayers; l++) {
-            if (l < L) {
-                const float* src = I->win[0][l] + o;
-                w[l] = v4 ? __ldg(reinterpret_cast<const float4*>(src)) : make_float4(__ldg(src), 0.0f, 0.0f, 0.0f);
-            }
-        }
         float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int top = L - 1; top >= 0; top -= kChunk) {
+            float4 w[kChunk];
 #pragma unroll
-        for (int l = kMaxLayers - 1; l >= 0; l--) {
-            if (l >= L) continue;
-            const float sc = I->scoeff[l];
-            const float wv[4] = {w[l].x, w[l].y, w[l].z, w[l].w};
+            for (int c = 0; c < kChunk; c++) {
+                if (top - c < 0) break;
+                const float* src = I->win[0][top - c] + o;
+                w[c] = v4 ? __ldg(reinterpret_cast<const float4*>(src)) : make_float4(__ldg(src), 0.0f, 0.0f, 0.0f);
+            }
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float val = __fmul_rn(wv[j], sc);
-                float sum, err;
-                two_sum(hi[j], val, sum, err);
-                hi[j] = sum;
-                lo[j] = __fadd_rn(lo[j], err);
+            for (int c = 0; c < kChunk; c++) {
+                if (top - c < 0) break;
+                const float sc = I->scoeff[top - c];
+                const float wv[4] = {w[c].x, w[c].y, w[c].z, w[c].w};
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float val = __fmul_rn(wv[j], sc);
+                    float sum, err;
+                    two_sum(hi[j], val, sum, err);
+                    hi[j] = sum;
+                    lo[j] = __fadd_rn(lo[j], err);
+                }
             }
         }
         float* dst = I->phisum + q;
