@@ -1,4 +1,5 @@
 // aux_kernels.cu -- setup and per-step helper kernels of the engine.
+#include <cstdlib>
 #include <algorithm>
 
 #include "aux_kernels.cuh"
@@ -347,7 +348,13 @@ cudaError_t copy_out(const float4* src0, float4* dst0, long n0, const float4* sr
     if (!dst0) n0 = 0;
     if (!dst1) n1 = 0;
     if (n0 + n1 == 0) return cudaSuccess;
-    k_copy_out<<<8, 256, 0, st>>>(src0, dst0, n0, src1, dst1, n1);
+    // CTAs of the copy (ATMWFS_COPY_CTAS overrides the measured default)
+    static const int ctas = [] {
+        const char* e = getenv("ATMWFS_COPY_CTAS");
+        const int v = e ? atoi(e) : 0;
+        return v >= 1 && v <= 152 ? v : 8;
+    }();
+    k_copy_out<<<ctas, 256, 0, st>>>(src0, dst0, n0, src1, dst1, n1);
     return cudaGetLastError();
 }
 

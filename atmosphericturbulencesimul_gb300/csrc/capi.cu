@@ -1152,7 +1152,12 @@ atmwfs_status atmwfs_run(atmwfs_ctx* c, long nsteps, const atmwfs_sink* sink)
     const size_t per = (size_t)c->ninst * c->L;
     const bool copies = sink && (sink->pha || sink->amp);
     if (copies && !c->out_st) {
-        AW_CUDA(cudaStreamCreateWithFlags(&c->out_st, cudaStreamNonBlocking));
+        // the copy stream has the highest priority: its few CTAs take the
+        // next free SM slots ahead of the queued pass and phase-sum CTAs, so a
+        // step's frames leave while the next step computes
+        int lo = 0, hi = 0;
+        AW_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        AW_CUDA(cudaStreamCreateWithPriority(&c->out_st, cudaStreamNonBlocking, hi));
         c->ev_written.assign(c->ring, nullptr);
         c->ev_copied.assign(c->ring, nullptr);
         for (long r = 0; r < c->ring; r++) {
