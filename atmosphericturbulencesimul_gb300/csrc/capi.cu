@@ -519,9 +519,7 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
         a.jobs = cl.d_jobs;
         const int RR0 = tile_cfg(cl.N, 0).rr;
         // screen tiles in (RR0 + 3 rows of the padded width) and windows out
-        long nwin = 0;
-        for (const WinJob& j : cl.jobs) nwin += j.nl;
-        if (bytes) *bytes = (4.0 * (RR0 + 3) / RR0 + 4.0) * (double)cl.N * cl.N * nwin;
+        if (bytes) *bytes = (4.0 * (RR0 + 3) / RR0 + 4.0) * (double)cl.N * cl.N * cl.jobs.size();
         AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarWindows, dim3(cl.N / RR0, (unsigned)cl.jobs.size()), a, &cl.maps[0],
                                         nullptr, st));
         return ATMWFS_OK;
@@ -724,21 +722,10 @@ atmwfs_status commit(atmwfs_ctx* c)
         if (!owner) continue;
         for (int g = 0; g < G; g++) {
             if (c->wg[g] != cl.N) continue;
-            for (int o = 0; o < 2; o++) {
-                // one job per group and orientation, its layers in order
-                WinJob j;
-                memset(&j, 0, sizeof j);
-                j.gidx = c->group_leader[g];
-                j.orient = o;
-                j.stride = c->wg[g];
+            for (int o = 0; o < 2; o++)
                 for (int l = 0; l < c->L; l++)
-                    if (float* w = c->d_win[o][(size_t)g * c->L + l]) {
-                        j.out[j.nl] = w;
-                        j.layer[j.nl] = l;
-                        j.nl++;
-                    }
-                if (j.nl > 0) cl.jobs.push_back(j);
-            }
+                    if (float* w = c->d_win[o][(size_t)g * c->L + l])
+                        cl.jobs.push_back(WinJob{w, c->group_leader[g], l, o, c->wg[g]});
         }
         if (cl.jobs.empty()) continue;
         if (!cl.d_jobs) AW_TRY(dalloc(c, (void**)&cl.d_jobs, sizeof(WinJob) * cl.jobs.size()));

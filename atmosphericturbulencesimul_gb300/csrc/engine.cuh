@@ -55,13 +55,11 @@ struct InstDev {
     int wstride;
 };
 
-// One job of the per-step window kernel: the windows of group leader `gidx`
-// in orientation `orient` for the nl layers listed, layer[i] written to out[i]
-// with row stride `stride`.
+// One window of the per-step window kernel: layer `layer` of group leader
+// `gidx` in orientation `orient`, written to `out` with row stride `stride`.
 struct WinJob {
-    float* out[kMaxLayers];
-    int layer[kMaxLayers];
-    int nl, gidx, orient, stride;
+    float* out;
+    int gidx, layer, orient, stride;
 };
 
 enum : int { kModeRef = 0, kModeSci = 1, kModePhase = 2 };

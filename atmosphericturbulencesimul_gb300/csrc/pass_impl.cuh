@@ -592,46 +592,22 @@ __global__ void __launch_bounds__(PassGeom<N, RR>::NT)
 {
     using G = PassGeom<N, RR>;
     constexpr int NT = G::NT;
-    constexpr size_t TB = G::round128(G::TILE_BYTES);
     extern __shared__ __align__(1024) unsigned char sm[];
-    // two tile buffers: the next layer's copy overlaps this layer's samples
-    unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
-    float* tiles[2] = {reinterpret_cast<float*>(base), reinterpret_cast<float*>(base + TB)};
-    __shared__ __align__(8) uint64_t bar[2];
-    const WinJob& J = a.jobs[blockIdx.y];
+    float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) uint64_t bar;
+    const WinJob J = a.jobs[blockIdx.y];
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * RR;
     const int step = *a.d_step;
-    const LayerPos* P = a.pos + ((size_t)(step % a.poscap) * a.ninst_total + J.gidx) * a.L;
-    const int nl = J.nl, orient = J.orient, stride = J.stride;
-    if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
-    }
+    const LayerPos p = a.pos[((size_t)(step % a.poscap) * a.ninst_total + J.gidx) * a.L + J.layer];
+    const TileGeom g = tile_geom(p, J.orient, y0);
+    if (tid == 0) mbar_init(&bar, 1);
     __syncthreads();
-    for (int i = 0; i < nl && i < 2; i++)
-        tma_issue_layer<N, RR>(maps, orient, J.layer[i], tile_geom(P[J.layer[i]], orient, y0), tiles[i], &bar[i], tid,
-                               NT);
-    int parity = 0;  // bit b: phase parity of buffer b
-    for (int i = 0; i < nl; i++) {
-        const int b = i & 1;
-        if (!cta_wait_tile(&bar[b], (parity >> b) & 1, a.d_status)) {
-            // the other buffer may still be in flight: let it land first
-            if (i + 1 < nl) cta_wait_tile(&bar[b ^ 1], (parity >> (b ^ 1)) & 1, nullptr);
-            return;
-        }
-        parity ^= 1 << b;
-        const int l = J.layer[i];
-        float* out = J.out[i] + (size_t)y0 * stride;
-        gather_tile<N, RR, NT>(tiles[b], tile_geom(P[l], orient, y0), 1.0f, tid,
-                               [=](int r, int x, float val) { out[(size_t)r * stride + x] = val; });
-        if (i + 2 < nl) {
-            __syncthreads();  // every thread is done reading this buffer
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            const int ln = J.layer[i + 2];
-            tma_issue_layer<N, RR>(maps, orient, ln, tile_geom(P[ln], orient, y0), tiles[b], &bar[b], tid, NT);
-        }
-    }
+    tma_issue_layer<N, RR>(maps, J.orient, J.layer, g, tile, &bar, tid, NT);
+    if (!cta_wait_tile(&bar, 0, a.d_status)) return;
+    float* out = J.out + (size_t)y0 * J.stride;
+    const int stride = J.stride;
+    gather_tile<N, RR, NT>(tile, g, 1.0f, tid, [=](int r, int x, float val) { out[(size_t)r * stride + x] = val; });
 }
 
 // ---------------------------------------------------------------------------
@@ -738,7 +714,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
             return cudaGetLastError();
         }
         case kVarWindows: {
-            constexpr size_t sm = 2 * G::round128(G::TILE_BYTES) + 128;
+            constexpr size_t sm = G::TILE_BYTES + 128;
             static bool attr = false;
             if (!attr) {
                 cudaError_t e = cudaFuncSetAttribute(k_layer_windows<N, RR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
