@@ -108,9 +108,38 @@ AW_HD constexpr int brev(int i)
 // values, at the same places, as the two radix-2 levels (whose second level
 // multiplies by W^k and W^(k + s) = W4 W^k), with three twiddle multiplies per
 // group of four instead of four.
+// Translation units built with scalar butterflies (AW_SCALAR_BUTTERFLY: the
+// whole-row transforms of the large screens) keep the plain radix-2 levels,
+// which measured faster there (8192^2: 0.98 against 1.10 ms).
+template <int R, int D>
+AW_HD void dft_radix2(float2* v)
+{
+    AW_UNROLL
+    for (int span = R / 2; span >= 1; span >>= 1) {
+        AW_UNROLL
+        for (int base = 0; base < R; base += 2 * span) {
+            AW_UNROLL
+            for (int k = 0; k < span; k++) {
+                const float2 a = v[base + k], b = v[base + k + span];
+                v[base + k] = cadd(a, b);
+                v[base + k + span] = tw_const<D>(csub(a, b), k, 2 * span);
+            }
+        }
+    }
+    float2 t[R];
+    AW_UNROLL
+    for (int i = 0; i < R; i++) t[i] = v[i];
+    AW_UNROLL
+    for (int i = 0; i < R; i++) v[i] = t[brev<R>(i)];
+}
+
 template <int R, int D>
 AW_HD void dft(float2* v)
 {
+#if defined(AW_SCALAR_BUTTERFLY)
+    dft_radix2<R, D>(v);
+    return;
+#endif
     constexpr int L2 = R == 2 ? 1 : R == 4 ? 2 : R == 8 ? 3 : R == 16 ? 4 : R == 32 ? 5 : 6;
     int span = R / 4;
     AW_UNROLL
