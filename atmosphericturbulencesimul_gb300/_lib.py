@@ -16,7 +16,7 @@ OK = 0
 STATUS_NAMES = {0: "OK", 1: "ERR_INVALID", 2: "ERR_NOMEM", 3: "ERR_CUDA", 4: "ERR_IO", 5: "ERR_TIMEOUT",
                 6: "ERR_STATE", 7: "ERR_NODEVICE"}
 MODE_REF, MODE_SCI, MODE_PHASE = 0, 1, 2
-NUM_TILE_CFG = 3  # ATMWFS_NUM_TILE_CFG
+NUM_TILE_CFG = 5  # ATMWFS_NUM_TILE_CFG
 
 
 class AtmwfsError(RuntimeError):
@@ -152,6 +152,7 @@ SIGNATURES = [
     ("atmwfs_stream", C.c_void_p, [_ctx]),
     ("atmwfs_num_classes", C.c_int, [_ctx]),
     ("atmwfs_class_info", C.c_int, [_ctx, C.c_int, _ip, _ip, _ip, _ip, _dp]),
+    ("atmwfs_class_plan", C.c_int, [_ctx, C.c_int, _ip, _ip]),
     ("atmwfs_time_pass", C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip]),
     ("atmwfs_fresnel", C.c_int, [_fp, _fp, C.c_long, C.c_double, C.c_double, C.c_double]),
     ("atmwfs_fresnel_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_double,

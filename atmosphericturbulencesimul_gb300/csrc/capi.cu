@@ -98,10 +98,17 @@ PassLauncherHalf pass_launcher_half(int N)
 
 static bool pow2_in(long n, long lo, long hi) { return n >= lo && n <= hi && (n & (n - 1)) == 0; }
 
-// Concatenated stage twiddle tables of grid size N (build_twiddles).
-static std::vector<float2> host_twiddles(int N)
+// Concatenated stage twiddle tables of grid size N and radix plan V
+// (build_twiddles).
+static std::vector<float2> host_twiddles(int N, int V = 0)
 {
     std::vector<float2> h;
+    if (V == 1 && N == 1024) {
+        h.resize(tw_total<1024, 1>());
+        build_twiddles<1024, 1>(h.data());
+        return h;
+    }
+    if (V != 0) return h;
     switch (N) {
         case 64: h.resize(tw_total<64>()); build_twiddles<64>(h.data()); break;
         case 128: h.resize(tw_total<128>()); build_twiddles<128>(h.data()); break;
@@ -144,19 +151,20 @@ void twiddle_fill(int N, float2* out)
     }
 }
 
-// Stage twiddle tables evaluated in double.  One copy per (device, N) for
-// the life of the process.
-static const float2* twiddles(int N)
+// Stage twiddle tables evaluated in double.  One copy per (device, N, radix
+// plan) for the life of the process.
+static const float2* twiddles(int N, int V = 0)
 {
     static std::mutex mu;
     static std::map<std::pair<int, int>, float2*> cache;
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    auto key = std::make_pair(dev, N);
+    auto key = std::make_pair(dev, N * 4 + V);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
-    const std::vector<float2> h = host_twiddles(N);
+    const std::vector<float2> h = host_twiddles(N, V);
+    if (h.empty()) return nullptr;
     float2* d = nullptr;
     if (cudaMalloc(&d, sizeof(float2) * h.size()) != cudaSuccess) return nullptr;
     if (cudaMemcpy(d, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
@@ -571,7 +579,8 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
             if (c->fp16 && var != kVarSingle)
                 AW_CUDA(pass_launcher_half(cl.N)(var, grid, a, &cl.maps[cl.cfg], twiddles_half(cl.N), st));
             else
-                AW_CUDA(pass_launcher_cfg(cl.N)(cl.cfg, var, grid, a, &cl.maps[cl.cfg], twiddles(cl.N), st));
+                AW_CUDA(pass_launcher_cfg(cl.N)(cl.cfg, var, grid, a, &cl.maps[cl.cfg],
+                                                twiddles(cl.N, tile_cfg(cl.N, cl.cfg).plan), st));
         }
     }
     return ATMWFS_OK;
@@ -624,9 +633,11 @@ atmwfs_status clear_bins(atmwfs_ctx* c)
 }
 
 // Project autotuner: for every grid class time the representative pass
-// (a middle pass when there is one) in each tile configuration and keep the
-// fastest.  ATMWFS_TILE_CFG=<k> forces configuration k.  Science bins are
-// cleared afterwards (a timed last pass accumulates into them).
+// (a middle pass when there is one) in each configuration compiled for its
+// size -- radix plan and tile shape (tile_cfg) -- and keep the fastest.
+// ATMWFS_TILE_CFG=<k> forces configuration k (ignored where the size has
+// none).  Science bins are cleared afterwards (a timed last pass
+// accumulates into them).
 atmwfs_status autotune(atmwfs_ctx* c)
 {
     const int Q = (int)c->plane_lo.size();
@@ -641,13 +652,14 @@ atmwfs_status autotune(atmwfs_ctx* c)
             cl.cfg = 2;  // the FP16-transform passes are compiled for configuration 2
         } else if (force) {
             const int g = atoi(force);
-            cl.cfg = (g >= 0 && g < kNumTileCfg) ? g : 0;
+            cl.cfg = (g >= 0 && g < kNumTileCfg && tile_cfg(cl.N, g).rr > 0) ? g : 0;
         } else {
             // two interleaved rounds over the configurations; each keeps its
             // fastest reading, so one disturbed reading does not decide
             for (int g = 0; g < kNumTileCfg; g++) cl.tuned_ms[g] = 1e30f;
             for (int round = 0; round < 2 && s == ATMWFS_OK; round++) {
                 for (int g = 0; g < kNumTileCfg && s == ATMWFS_OK; g++) {
+                    if (tile_cfg(cl.N, g).rr == 0) continue;  // not compiled at this size
                     cl.cfg = g;
                     cl.RR = tile_cfg(cl.N, g).rr;
                     s = launch_pass(c, k, cl, nullptr, c->st);
@@ -664,6 +676,8 @@ atmwfs_status autotune(atmwfs_ctx* c)
             int bg = 0;
             for (int g = 1; g < kNumTileCfg; g++)
                 if (cl.tuned_ms[g] < cl.tuned_ms[bg]) bg = g;
+            for (int g = 0; g < kNumTileCfg; g++)
+                if (tile_cfg(cl.N, g).rr == 0) cl.tuned_ms[g] = 0;
             cl.cfg = bg;
         }
         cl.RR = tile_cfg(cl.N, cl.cfg).rr;
@@ -743,7 +757,7 @@ atmwfs_status commit(atmwfs_ctx* c)
         for (int g = 0; g < kNumTileCfg; g++)
             for (int o = 0; o < 2; o++)
                 for (int l = 0; l < c->L; l++)
-                    if (c->d_pad[o][l])
+                    if (c->d_pad[o][l] && tile_cfg(cl.N, g).rr > 0)
                         AW_TRY(make_tma_map(&cl.maps[g].m[o][l], c->d_pad[o][l], c->Wp, c->Hp, tile_cfg(cl.N, g).rr + 3));
     }
     AW_CUDA(cudaStreamSynchronize(c->st));
@@ -994,9 +1008,13 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
         }
         for (int b = 0; b < 2; b++) CKC(cudaEventRecord(c->ev[b], c->st));
         for (const Class& cl : c->classes) {
-            if (!twiddles(cl.N)) {
-                s = fail(ATMWFS_ERR_NOMEM, "twiddle table allocation failed");
-                goto fail_out;
+            // the tables of every radix plan the autotuner may pick
+            for (int g = 0; g < kNumTileCfg; g++) {
+                if (tile_cfg(cl.N, g).rr == 0) continue;
+                if (!twiddles(cl.N, tile_cfg(cl.N, g).plan)) {
+                    s = fail(ATMWFS_ERR_NOMEM, "twiddle table allocation failed");
+                    goto fail_out;
+                }
             }
         }
         CKC(cudaStreamCreateWithFlags(&c->sum_st, cudaStreamNonBlocking));
@@ -1327,6 +1345,36 @@ atmwfs_status atmwfs_class_info(const atmwfs_ctx* c, int ci, int* n, int* nout, 
     if (count) *count = (int)cl.members.size();
     if (rows_per_cta) *rows_per_cta = cl.RR;
     for (int g = 0; g < kNumTileCfg && tuned_ms; g++) tuned_ms[g] = cl.tuned_ms[g];
+    return ATMWFS_OK;
+}
+
+atmwfs_status atmwfs_class_plan(const atmwfs_ctx* c, int ci, int* cfg, int* radices)
+{
+    if (!c || ci < 0 || ci >= (int)c->classes.size()) return fail(ATMWFS_ERR_INVALID, "bad class");
+    const Class& cl = c->classes[ci];
+    if (cfg) *cfg = cl.cfg;
+    if (radices) {
+        const int V = tile_cfg(cl.N, cl.cfg).plan;
+        int r[3] = {0, 0, 0};
+        switch (cl.N * 4 + V) {
+#define AW_PLAN(NN, VV)                                                                      \
+    case NN * 4 + VV:                                                                        \
+        r[0] = Stages<NN, VV>::R0;                                                           \
+        r[1] = Stages<NN, VV>::R1;                                                           \
+        r[2] = Stages<NN, VV>::R2;                                                           \
+        break;
+            AW_PLAN(64, 0)
+            AW_PLAN(128, 0)
+            AW_PLAN(256, 0)
+            AW_PLAN(512, 0)
+            AW_PLAN(1024, 0)
+            AW_PLAN(1024, 1)
+            AW_PLAN(2048, 0)
+#undef AW_PLAN
+            default: break;
+        }
+        for (int i = 0; i < 3; i++) radices[i] = r[i];
+    }
     return ATMWFS_OK;
 }
 

@@ -133,29 +133,34 @@ typedef cudaError_t (*PassLauncher)(int var, dim3 grid, const PassArgs& a, const
 typedef cudaError_t (*PassLauncherCfg)(int cfg, int var, dim3 grid, const PassArgs& a, const TmaSet* maps,
                                        const float2* tw, cudaStream_t st);
 
-// Tile configurations compiled for every grid size: rows per CTA, the
-// minimum number of resident CTAs per SM the kernel is register-limited to,
-// and whether the screen tile overlays the exchange rows.  Configuration 0
-// is the one-CTA-per-SM shape; configuration 1 trades halo overhead (fewer
-// rows per tile) for several resident CTAs per SM; configuration 2 also
-// overlays the tile on the exchange buffer (the tile is then loaded after
-// the first propagation instead of during it), which cuts shared memory so
-// that one more CTA fits per SM.  The engine's autotuner picks one per grid
-// class at set-up.
+// Pass configurations compiled per grid size: the radix plan (Plan / Stages
+// variant), rows per CTA, the minimum number of resident CTAs per SM the
+// kernel is register-limited to, and whether the screen tile overlays the
+// exchange rows.  Configurations 0-2 use the default plan: 0 is the
+// one-CTA-per-SM shape; 1 trades rows per tile for several resident CTAs
+// per SM; 2 also overlays the tile on the exchange buffer, which cuts shared
+// memory so that one more CTA fits per SM.  Configurations 3 and 4 run the
+// size's alternative radix plan (where it has one; rr = 0 elsewhere) in two
+// tile shapes.  The engine's autotuner times every compiled configuration of
+// a grid class at set-up and keeps the fastest.
 struct TileCfg {
     int rr, minb;
     bool alias;
+    int plan;
 };
 constexpr int kNumTileCfg = ATMWFS_NUM_TILE_CFG;
 constexpr TileCfg tile_cfg(int N, int c)
 {
-    return N == 64    ? (c == 0 ? TileCfg{32, 1, false} : c == 1 ? TileCfg{16, 2, false} : TileCfg{16, 3, true})
-         : N == 128   ? (c == 0 ? TileCfg{32, 1, false} : c == 1 ? TileCfg{16, 2, false} : TileCfg{16, 3, true})
-         : N == 256   ? (c == 0 ? TileCfg{16, 1, false} : c == 1 ? TileCfg{8, 3, false} : TileCfg{8, 4, true})
-         : N == 512   ? (c == 0 ? TileCfg{16, 1, false} : c == 1 ? TileCfg{8, 3, false} : TileCfg{8, 4, true})
-         : N == 1024  ? (c == 0 ? TileCfg{8, 1, false} : c == 1 ? TileCfg{4, 3, false} : TileCfg{4, 4, true})
-         : N == 2048  ? (c == 0 ? TileCfg{4, 1, false} : c == 1 ? TileCfg{2, 3, false} : TileCfg{2, 3, true})
-                      : TileCfg{0, 0, false};
+    return c == 3 ? (N == 1024 ? TileCfg{4, 3, false, 1} : TileCfg{0, 0, false, 0})
+         : c == 4 ? (N == 1024 ? TileCfg{2, 6, false, 1} : TileCfg{0, 0, false, 0})
+         : c > 4  ? TileCfg{0, 0, false, 0}
+         : N == 64    ? (c == 0 ? TileCfg{32, 1, false, 0} : c == 1 ? TileCfg{16, 2, false, 0} : TileCfg{16, 3, true, 0})
+         : N == 128   ? (c == 0 ? TileCfg{32, 1, false, 0} : c == 1 ? TileCfg{16, 2, false, 0} : TileCfg{16, 3, true, 0})
+         : N == 256   ? (c == 0 ? TileCfg{16, 1, false, 0} : c == 1 ? TileCfg{8, 3, false, 0} : TileCfg{8, 4, true, 0})
+         : N == 512   ? (c == 0 ? TileCfg{16, 1, false, 0} : c == 1 ? TileCfg{8, 3, false, 0} : TileCfg{8, 4, true, 0})
+         : N == 1024  ? (c == 0 ? TileCfg{8, 1, false, 0} : c == 1 ? TileCfg{4, 3, false, 0} : TileCfg{4, 4, true, 0})
+         : N == 2048  ? (c == 0 ? TileCfg{4, 1, false, 0} : c == 1 ? TileCfg{2, 3, false, 0} : TileCfg{2, 3, true, 0})
+                      : TileCfg{0, 0, false, 0};
 }
 
 // Threads of a phase-sum CTA and CTAs per instance of its launch.

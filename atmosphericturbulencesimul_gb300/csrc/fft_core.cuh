@@ -293,7 +293,13 @@ AW_HD int last_index(int t, int s) { return t + T * (s / RL) + (s % RL) * (N / R
 // the coalesced global load x[t + e T] is already the first stage's layout);
 // the inverse uses the reversed sequence so that it can start from the
 // forward's output registers and ends in the same layout x[t + e T].
-template <int N> struct Plan;
+//
+// A grid size can have more than one plan (V = 0 is the default; the engine's
+// autotuner times the others as further configurations): V = 1 at 1024 is
+// 16 x 8 x 8 with 16 values per thread and two warps per row -- one more
+// exchange per transform than 32 x 32, but half the registers, so more
+// warps per SM to hide the exchange and load latencies.
+template <int N, int V = 0> struct Plan;
 template <> struct Plan<64>   { static constexpr int E = 8,  T = 8;  };
 template <> struct Plan<128>  { static constexpr int E = 16, T = 8;  };
 template <> struct Plan<256>  { static constexpr int E = 16, T = 16; };
@@ -302,6 +308,7 @@ template <> struct Plan<1024> { static constexpr int E = 32, T = 32; };
 template <> struct Plan<2048> { static constexpr int E = 32, T = 64; };
 template <> struct Plan<4096> { static constexpr int E = 16, T = 256; };
 template <> struct Plan<8192> { static constexpr int E = 32, T = 256; };
+template <> struct Plan<1024, 1> { static constexpr int E = 16, T = 64; };
 
 template <int... Rs> struct Radices {};
 
@@ -323,7 +330,7 @@ template <> struct InvRadices<2048> { using type = Radices<8, 8, 32>; };
 
 // Radix sequence of the forward transform as a runtime-indexable table; the
 // inverse of a propagation walks it backwards.
-template <int N> struct Stages;
+template <int N, int V = 0> struct Stages;
 template <> struct Stages<64>   { static constexpr int S = 2, R0 = 8, R1 = 8, R2 = 0; };
 template <> struct Stages<128>  { static constexpr int S = 2, R0 = 16, R1 = 8, R2 = 0; };
 template <> struct Stages<256>  { static constexpr int S = 2, R0 = 16, R1 = 16, R2 = 0; };
@@ -333,59 +340,61 @@ template <> struct Stages<2048> { static constexpr int S = 3, R0 = 32, R1 = 8, R
 // whole-row plans of the large 2-D transforms (one CTA of 256 threads per row)
 template <> struct Stages<4096> { static constexpr int S = 3, R0 = 16, R1 = 16, R2 = 16; };
 template <> struct Stages<8192> { static constexpr int S = 3, R0 = 32, R1 = 16, R2 = 16; };
+// alternative plans (see Plan)
+template <> struct Stages<1024, 1> { static constexpr int S = 3, R0 = 16, R1 = 8, R2 = 8; };
 
-template <int N>
+template <int N, int V = 0>
 AW_HD constexpr bool has_radix(int r)
 {
-    return Stages<N>::R0 == r || Stages<N>::R1 == r || Stages<N>::R2 == r;
+    return Stages<N, V>::R0 == r || Stages<N, V>::R1 == r || Stages<N, V>::R2 == r;
 }
 
 // last radix of the forward sequence
-template <int N>
-AW_HD constexpr int last_radix() { return Stages<N>::S == 3 ? Stages<N>::R2 : Stages<N>::R1; }
+template <int N, int V = 0>
+AW_HD constexpr int last_radix() { return Stages<N, V>::S == 3 ? Stages<N, V>::R2 : Stages<N, V>::R1; }
 
 // radix of stage st, forward order (rev = 0) or reversed (rev = 1)
-template <int N>
+template <int N, int V = 0>
 AW_HD int stage_radix(int st, int rev)
 {
-    const int i = rev ? Stages<N>::S - 1 - st : st;
-    return i == 0 ? Stages<N>::R0 : i == 1 ? Stages<N>::R1 : Stages<N>::R2;
+    const int i = rev ? Stages<N, V>::S - 1 - st : st;
+    return i == 0 ? Stages<N, V>::R0 : i == 1 ? Stages<N, V>::R1 : Stages<N, V>::R2;
 }
 
 // Stride (product of the earlier radices) of stage st in the given order.
-template <int N>
+template <int N, int V = 0>
 AW_HD int stage_ns(int st, int rev)
 {
     int ns = 1;
-    for (int i = 0; i < st; i++) ns *= stage_radix<N>(i, rev);
+    for (int i = 0; i < st; i++) ns *= stage_radix<N, V>(i, rev);
     return ns;
 }
 
 // Twiddle tables: for each order (rev = 0, 1) and stage st >= 1 a table of
 // R x ns entries tab[r * ns + k] = exp(-2 pi i k r / (ns R)); this gives the
 // offset of table (rev, st) in the concatenation and the total size.
-template <int N>
+template <int N, int V = 0>
 AW_HD int tw_offset(int rev, int st)
 {
     int off = 0;
     for (int o = 0; o <= rev; o++)
-        for (int i = 1; i < Stages<N>::S; i++) {
+        for (int i = 1; i < Stages<N, V>::S; i++) {
             if (o == rev && i == st) return off;
-            off += stage_radix<N>(i, o) * stage_ns<N>(i, o);
+            off += stage_radix<N, V>(i, o) * stage_ns<N, V>(i, o);
         }
     return off;
 }
-template <int N>
-AW_HD int tw_total() { return tw_offset<N>(1, Stages<N>::S); }
+template <int N, int V = 0>
+AW_HD int tw_total() { return tw_offset<N, V>(1, Stages<N, V>::S); }
 
 // Fill the concatenated stage tables (host side, double precision).
-template <int N>
+template <int N, int V = 0>
 inline void build_twiddles(float2* out)
 {
     for (int o = 0; o < 2; o++)
-        for (int st = 1; st < Stages<N>::S; st++) {
-            const int R = stage_radix<N>(st, o), ns = stage_ns<N>(st, o);
-            float2* tab = out + tw_offset<N>(o, st);
+        for (int st = 1; st < Stages<N, V>::S; st++) {
+            const int R = stage_radix<N, V>(st, o), ns = stage_ns<N, V>(st, o);
+            float2* tab = out + tw_offset<N, V>(o, st);
             for (int r = 0; r < R; r++)
                 for (int k = 0; k < ns; k++) {
                     const double a = -2.0 * 3.14159265358979323846264338328 * (double)(k * r) / (double)(ns * R);
@@ -396,28 +405,28 @@ inline void build_twiddles(float2* out)
 
 // Stage body (twiddles + butterflies) of radix r and stride ns for one
 // thread; a uniform branch selects the code of the radix.
-template <int N, int T, int E>
+template <int N, int T, int E, int V = 0>
 AW_HD void stage_compute(float2* v, int t, const float2* tw, int r, int ns)
 {
-    if constexpr (has_radix<N>(32)) if (r == 32) { stage_twiddle_rt<N, T, E, 32>(v, t, tw, ns); stage_dft_rt<E, 32>(v); return; }
-    if constexpr (has_radix<N>(16)) if (r == 16) { stage_twiddle_rt<N, T, E, 16>(v, t, tw, ns); stage_dft_rt<E, 16>(v); return; }
-    if constexpr (has_radix<N>(8)) if (r == 8) { stage_twiddle_rt<N, T, E, 8>(v, t, tw, ns); stage_dft_rt<E, 8>(v); return; }
+    if constexpr (has_radix<N, V>(32)) if (r == 32) { stage_twiddle_rt<N, T, E, 32>(v, t, tw, ns); stage_dft_rt<E, 32>(v); return; }
+    if constexpr (has_radix<N, V>(16)) if (r == 16) { stage_twiddle_rt<N, T, E, 16>(v, t, tw, ns); stage_dft_rt<E, 16>(v); return; }
+    if constexpr (has_radix<N, V>(8)) if (r == 8) { stage_twiddle_rt<N, T, E, 8>(v, t, tw, ns); stage_dft_rt<E, 8>(v); return; }
 }
 
-template <int N, int T, int E>
+template <int N, int T, int E, int V = 0>
 AW_HD void stage_exchange_store(const float2* v, float2* buf, int t, int r, int ns)
 {
-    if constexpr (has_radix<N>(32)) if (r == 32) { stage_store_rt<N, T, E, 32>(v, buf, t, ns); return; }
-    if constexpr (has_radix<N>(16)) if (r == 16) { stage_store_rt<N, T, E, 16>(v, buf, t, ns); return; }
-    if constexpr (has_radix<N>(8)) if (r == 8) { stage_store_rt<N, T, E, 8>(v, buf, t, ns); return; }
+    if constexpr (has_radix<N, V>(32)) if (r == 32) { stage_store_rt<N, T, E, 32>(v, buf, t, ns); return; }
+    if constexpr (has_radix<N, V>(16)) if (r == 16) { stage_store_rt<N, T, E, 16>(v, buf, t, ns); return; }
+    if constexpr (has_radix<N, V>(8)) if (r == 8) { stage_store_rt<N, T, E, 8>(v, buf, t, ns); return; }
 }
 
-template <int N, int T, int E>
+template <int N, int T, int E, int V = 0>
 AW_HD void stage_exchange_load(float2* v, const float2* buf, int t, int r)
 {
-    if constexpr (has_radix<N>(32)) if (r == 32) { stage_load<N, T, E, 32>(v, buf, t); return; }
-    if constexpr (has_radix<N>(16)) if (r == 16) { stage_load<N, T, E, 16>(v, buf, t); return; }
-    if constexpr (has_radix<N>(8)) if (r == 8) { stage_load<N, T, E, 8>(v, buf, t); return; }
+    if constexpr (has_radix<N, V>(32)) if (r == 32) { stage_load<N, T, E, 32>(v, buf, t); return; }
+    if constexpr (has_radix<N, V>(16)) if (r == 16) { stage_load<N, T, E, 16>(v, buf, t); return; }
+    if constexpr (has_radix<N, V>(8)) if (r == 8) { stage_load<N, T, E, 8>(v, buf, t); return; }
 }
 
 template <int R0, int... Rs> struct LastRadix { static constexpr int value = LastRadix<Rs...>::value; };

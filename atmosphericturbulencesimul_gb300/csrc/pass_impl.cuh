@@ -100,10 +100,10 @@ __device__ __forceinline__ bool cta_wait_tile(uint64_t* bar, int parity, unsigne
 // ---------------------------------------------------------------------------
 // geometry
 // ---------------------------------------------------------------------------
-template <int N, int RR>
+template <int N, int RR, int V = 0>
 struct PassGeom {
-    static constexpr int T = Plan<N>::T;
-    static constexpr int E = Plan<N>::E;
+    static constexpr int T = Plan<N, V>::T;
+    static constexpr int E = Plan<N, V>::E;
     static constexpr int NT = T * RR;
     static constexpr int RS = row_stride<N>();
     static constexpr int NBOX = N / kBoxW + 1;
@@ -147,49 +147,6 @@ __device__ __forceinline__ void tma_issue_layer(const TmaSet& maps, int orient, 
     for (int k = w; k < G::NBOX; k += nw) tma_load_2d(tile + k * G::TROWS * kBoxW, m, g.xs + k * kBoxW, g.ys, bar);
 }
 
-// ---------------------------------------------------------------------------
-// FFT sequencing (device): stages exchange through one padded row of the
-// shared exchange buffer: [sync, store, sync, load] between stages.
-// ---------------------------------------------------------------------------
-template <int N, int T, int E, int D, int NS, int R, int... Rest>
-__device__ __forceinline__ void run_stages(float2* v, float2* xrow, int t, const float2* __restrict__ tw)
-{
-    stage_twiddle<N, T, E, R, NS, D>(v, t, tw);
-    stage_dft<E, R, D>(v);
-    if constexpr (sizeof...(Rest) > 0) {
-        __syncthreads();
-        stage_store<N, T, E, R, NS>(v, xrow, t);
-        __syncthreads();
-        stage_load<N, T, E, FirstRadix<Rest...>::value>(v, xrow, t);
-        run_stages<N, T, E, D, NS * R, Rest...>(v, xrow, t, tw);
-    }
-}
-
-template <int N, int T, int E, int D, int... Rs>
-__device__ __forceinline__ void run_fft(float2* v, float2* xrow, int t, const float2* __restrict__ tw, Radices<Rs...>)
-{
-    run_stages<N, T, E, D, 1, Rs...>(v, xrow, t, tw);
-}
-
-template <int... Rs>
-AW_HD constexpr int last_of(Radices<Rs...>) { return LastRadix<Rs...>::value; }
-
-// 1-D Fresnel propagation of the row held in v (layout x[t + e T]):
-// forward FFT, multiply by the transfer table h[k] (unshifted frequency
-// index k, 1/N included), inverse FFT.  Ends in the same layout.
-template <int N, int T, int E>
-__device__ __forceinline__ void prop_row(float2* v, float2* xrow, int t, const float2* __restrict__ tw,
-                                         const float2* __restrict__ h)
-{
-    using FR = typename FwdRadices<N>::type;
-    using IR = typename InvRadices<N>::type;
-    constexpr int RL = last_of(FR{});
-    run_fft<N, T, E, -1>(v, xrow, t, tw, FR{});
-#pragma unroll
-    for (int s = 0; s < E; s++) v[s] = cmul(v[s], __ldg(h + last_index<N, T, RL>(t, s)));
-    run_fft<N, T, E, +1>(v, xrow, t, tw, IR{});
-}
-
 // One 1-D transform of the row in v through a runtime stage loop: every
 // stage of every transform of the kernel runs through the same code of its
 // radix, which keeps the kernel inside the instruction cache.  ds = -1
@@ -216,13 +173,13 @@ __device__ __forceinline__ void fft2_ct(float2* v, float2* xrow, int t, const fl
 // w^(t r) for r = 1 .. R - 1, are the same in every transform of every row the
 // thread holds (forward and inverse alike), so a pass can load them once into
 // registers instead of reading the table in each of its four transforms.
-template <int N>
+template <int N, int V = 0>
 AW_HD constexpr bool reg_twiddles()
 {
-    return Stages<N>::S == 2 && Stages<N>::R0 == Stages<N>::R1 && Plan<N>::E == Stages<N>::R1;
+    return Stages<N, V>::S == 2 && Stages<N, V>::R0 == Stages<N, V>::R1 && Plan<N, V>::E == Stages<N, V>::R1;
 }
-template <int N>
-AW_HD constexpr int reg_twiddle_count() { return reg_twiddles<N>() ? Stages<N>::R1 - 1 : 1; }
+template <int N, int V = 0>
+AW_HD constexpr int reg_twiddle_count() { return reg_twiddles<N, V>() ? Stages<N, V>::R1 - 1 : 1; }
 
 // The same transform with the second stage's twiddles in registers:
 // twr[r - 1] = w^((t mod RA) r), RB = E (one work item per thread).
@@ -240,11 +197,40 @@ __device__ __forceinline__ void fft2_ct_r(float2* v, float2* xrow, int t, const 
     stage_dft<E, RB, -1>(v);
 }
 
-template <int N, int T, int E, bool RT = false>
+// Three-stage plans with compile-time radices and strides (the alternative
+// plans, see Plan): stage A (stride 1), exchange, stage B (stride RA),
+// exchange, stage C (stride RA RB); twsB / twsC are the stage tables.
+template <int N, int T, int E, int RA, int RB, int RC>
+__device__ __forceinline__ void fft3_ct(float2* v, float2* xrow, int t, const float2* __restrict__ twsB,
+                                        const float2* __restrict__ twsC)
+{
+    stage_dft<E, RA, -1>(v);
+    row_sync<T>();
+    stage_store<N, T, E, RA, 1>(v, xrow, t);
+    row_sync<T>();
+    stage_load<N, T, E, RB>(v, xrow, t);
+    stage_twiddle_rt<N, T, E, RB>(v, t, twsB, RA);
+    stage_dft<E, RB, -1>(v);
+    row_sync<T>();
+    stage_store<N, T, E, RB, RA>(v, xrow, t);
+    row_sync<T>();
+    stage_load<N, T, E, RC>(v, xrow, t);
+    stage_twiddle_rt<N, T, E, RC>(v, t, twsC, RA * RB);
+    stage_dft<E, RC, -1>(v);
+}
+
+template <int N, int T, int E, bool RT = false, int V = 0>
 __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw, float ds, int rev,
                                        const float2* twr = nullptr)
 {
     if (ds > 0.0f) conj_all<E>(v);     // inverse = conj(forward(conj))
+    if constexpr (V != 0 && Stages<N, V>::S == 3) {
+        constexpr int R0 = Stages<N, V>::R0, R1 = Stages<N, V>::R1, R2 = Stages<N, V>::R2;
+        if (rev) fft3_ct<N, T, E, R2, R1, R0>(v, xrow, t, tw + tw_offset<N, V>(1, 1), tw + tw_offset<N, V>(1, 2));
+        else fft3_ct<N, T, E, R0, R1, R2>(v, xrow, t, tw + tw_offset<N, V>(0, 1), tw + tw_offset<N, V>(0, 2));
+        if (ds > 0.0f) conj_all<E>(v);
+        return;
+    }
     if constexpr (Stages<N>::S == 2) {
         constexpr int R0 = Stages<N>::R0, R1 = Stages<N>::R1;
         if constexpr (RT && reg_twiddles<N>()) {
@@ -278,16 +264,16 @@ __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const flo
 
 // 1-D Fresnel propagation (forward FFT, transfer table, inverse FFT) with a
 // single copy of the transform code.
-template <int N, int T, int E, bool RT = false>
+template <int N, int T, int E, bool RT = false, int V = 0>
 __device__ __forceinline__ void prop_row_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw,
                                             const float2* __restrict__ h, const float2* twr = nullptr)
 {
-    constexpr int RL = last_radix<N>();
+    constexpr int RL = last_radix<N, V>();
     // IFFT(H FFT(x)) = conj(FFT(conj(H FFT(x)))): the first conjugation is
     // folded into the transfer multiply, both transforms run the forward code
 #pragma unroll 1
     for (int dir = 0; dir < 2; dir++) {
-        fft_rt<N, T, E, RT>(v, xrow, t, tw, -1.0f, dir, twr);
+        fft_rt<N, T, E, RT, V>(v, xrow, t, tw, -1.0f, dir, twr);
         if (dir == 0) {
 #pragma unroll
             for (int s = 0; s < E; s++) {
@@ -346,11 +332,12 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // series passes (as opposed to the unit operators, which have no instance)
 #define I_SERIES(ops) (((ops) & (OP_GATHER | OP_EPI)) != 0)
 
-template <int N, int RR, int MINB, int OPS, bool ALIAS, bool HP = false>
-__global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
+template <int N, int RR, int MINB, int OPS, bool ALIAS, bool HP = false, int V = 0>
+__global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
     k_pass(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps, const float2* __restrict__ tw)
 {
-    using G = PassGeom<N, RR>;
+    using G = PassGeom<N, RR, V>;
+    static_assert(!HP || V == 0, "FP16 transforms use the default plan");
     constexpr int T = G::T, E = G::E, NT = G::NT, RS = G::RS;
     constexpr bool kEpi = (OPS & OP_EPI) != 0;
     constexpr bool kGather = (OPS & (OP_GATHER | OP_EPI)) != 0;
@@ -388,9 +375,9 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     // series passes (FP32 transforms) without the output epilogue (whose
     // registers they would crowd: measured slower there) in the tile
     // configurations that leave room for them (at most three CTAs per SM)
-    constexpr bool kRegTw = reg_twiddles<N>() && !HP && MINB <= 3 && I_SERIES(OPS) && (OPS & OP_EPI) == 0 &&
+    constexpr bool kRegTw = reg_twiddles<N, V>() && !HP && MINB <= 3 && I_SERIES(OPS) && (OPS & OP_EPI) == 0 &&
                             (OPS & (OP_PROP1 | OP_PROP2)) != 0;
-    float2 twr[reg_twiddle_count<N>()];
+    float2 twr[reg_twiddle_count<N, V>()];
     if constexpr (kRegTw) {
         constexpr int R = Stages<N>::R1;
 #pragma unroll
@@ -408,7 +395,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     }
 
     if constexpr ((OPS & (OP_FFT_FWD | OP_FFT_INV)) != 0) {
-        fft_rt<N, T, E>(v, xrow, t, tw, (OPS & OP_FFT_FWD) ? -1.0f : 1.0f, 0);
+        fft_rt<N, T, E, false, V>(v, xrow, t, tw, (OPS & OP_FFT_FWD) ? -1.0f : 1.0f, 0);
     } else {
         // phase 0: propagation 1; phase 1: screens of this plane; phase 2:
         // propagation 2 -- a runtime loop, so the transform code appears once
@@ -447,8 +434,8 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
                                     reinterpret_cast<const __half2*>(I->Hh) + (size_t)hop * N);
             } else {
                 const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
-                if constexpr (kRegTw) prop_row_rt<N, T, E, true>(v, xrow, t, tw, h, twr);
-                else prop_row_rt<N, T, E>(v, xrow, t, tw, h);
+                if constexpr (kRegTw) prop_row_rt<N, T, E, true, V>(v, xrow, t, tw, h, twr);
+                else prop_row_rt<N, T, E, false, V>(v, xrow, t, tw, h);
             }
         }
     }
@@ -561,7 +548,7 @@ __global__ void __launch_bounds__(Plan<N>::T* RR, MINB)
     if constexpr ((OPS & OP_STORE_T) != 0) {
         __syncthreads();
         constexpr bool kFreq = (OPS & (OP_FFT_FWD | OP_FFT_INV)) != 0;
-        constexpr int RL = last_radix<N>();
+        constexpr int RL = last_radix<N, V>();
 #pragma unroll
         for (int s = 0; s < E; s++) {
             const int x = kFreq ? last_index<N, T, RL>(t, s) : t + s * T;
@@ -671,11 +658,12 @@ __global__ void __launch_bounds__(kPhasumThreads, 4) k_phasum(const __grid_const
     }
 }
 
-// host launcher for one (N, tile configuration)
-template <int N, int RR, int MINB, bool ALIAS, bool HP = false>
+// host launcher for one (N, configuration); SO: the series passes only (the
+// unit operators, phase sums and windows launch in configuration 0)
+template <int N, int RR, int MINB, bool ALIAS, bool HP = false, int V = 0, bool SO = false>
 cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
 {
-    using G = PassGeom<N, RR>;
+    using G = PassGeom<N, RR, V>;
     static TmaSet empty_maps;  // unit passes gather nothing
     const TmaSet& m = maps ? *maps : empty_maps;
     dim3 block(G::NT);
@@ -684,15 +672,16 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         constexpr size_t sm = G::smem(VAR);                                                            \
         static bool attr = false;                                                                      \
         if (!attr) {                                                                                   \
-            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS, HP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS, HP, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
             if (e != cudaSuccess) return e;                                                            \
             attr = true;                                                                               \
         }                                                                                              \
-        k_pass<N, RR, MINB, VAR, ALIAS, HP><<<grid, block, sm, st>>>(a, m, tw);                        \
+        k_pass<N, RR, MINB, VAR, ALIAS, HP, V><<<grid, block, sm, st>>>(a, m, tw);                     \
         return cudaGetLastError();                                                                     \
     }
-    if constexpr (HP) {
-        // FP16 transforms: the series passes only
+    if constexpr (HP || V != 0 || SO) {
+        // FP16 transforms, the alternative radix plans and configurations
+        // other than 0: the series passes only
         switch (var) {
             AW_CASE(kVarFirst)
             AW_CASE(kVarMid)
@@ -700,7 +689,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
             AW_CASE(kVarSingle)
             default: return cudaErrorInvalidValue;
         }
-    }
+    } else {
     switch (var) {
         AW_CASE(kVarFirst)
         AW_CASE(kVarMid)
@@ -726,6 +715,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         }
         default: return cudaErrorInvalidValue;
     }
+    }
 #undef AW_CASE
 }
 
@@ -749,9 +739,13 @@ cudaError_t launch_pass_nc(int cfg, int var, dim3 grid, const PassArgs& a, const
                            cudaStream_t st)
 {
     constexpr TileCfg c0 = tile_cfg(N, 0), c1 = tile_cfg(N, 1), c2 = tile_cfg(N, 2);
-    static_assert(kNumTileCfg == 3, "one branch per tile configuration");
-    if (cfg == 2) return launch_pass_t<N, c2.rr, c2.minb, c2.alias>(var, grid, a, maps, tw, st);
-    if (cfg == 1) return launch_pass_t<N, c1.rr, c1.minb, c1.alias>(var, grid, a, maps, tw, st);
+    constexpr TileCfg c3 = tile_cfg(N, 3), c4 = tile_cfg(N, 4);
+    static_assert(kNumTileCfg == 5, "one branch per configuration");
+    if constexpr (c3.rr > 0) if (cfg == 3) return launch_pass_t<N, c3.rr, c3.minb, c3.alias, false, c3.plan>(var, grid, a, maps, tw, st);
+    if constexpr (c4.rr > 0) if (cfg == 4) return launch_pass_t<N, c4.rr, c4.minb, c4.alias, false, c4.plan>(var, grid, a, maps, tw, st);
+    if (cfg >= 3) return cudaErrorInvalidValue;  // no such configuration at this size
+    if (cfg == 2) return launch_pass_t<N, c2.rr, c2.minb, c2.alias, false, 0, true>(var, grid, a, maps, tw, st);
+    if (cfg == 1) return launch_pass_t<N, c1.rr, c1.minb, c1.alias, false, 0, true>(var, grid, a, maps, tw, st);
     return launch_pass_t<N, c0.rr, c0.minb, c0.alias>(var, grid, a, maps, tw, st);
 }
 

@@ -197,8 +197,10 @@ class Series:
         n, no, cnt, rr = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         t = (C.c_double * NUM_TILE_CFG)()
         check(self._lib.atmwfs_class_info(self._ctx, c, C.byref(n), C.byref(no), C.byref(cnt), C.byref(rr), t))
+        cfg, rad = C.c_int(), (C.c_int * 3)()
+        check(self._lib.atmwfs_class_plan(self._ctx, c, C.byref(cfg), rad))
         return {"n": n.value, "nout": no.value, "count": cnt.value, "rows_per_cta": rr.value,
-                "tuned_ms": list(t)}
+                "tuned_ms": list(t), "cfg": cfg.value, "radices": [r for r in rad if r > 0]}
 
     def time_pass(self, k: int, c: int, reps: int = 10):
         """Mean duration [ms] and algorithmic bytes of pass k of grid class c."""

@@ -723,7 +723,8 @@ def main():
             "peak_source": pk["source"]}
     # per class: phase sum and passes; the window launches; unwrap, apply, step counter
     launches = (npl + 1) * s.num_classes() + sum(1 for p in passes if p["k"] == npl + 1) + 3
-    cfg["tiles"] = {str(ci["n"]): {"rows_per_cta": ci["rows_per_cta"], "tuned_ms": [round(x, 4) for x in ci["tuned_ms"]]}
+    cfg["tiles"] = {str(ci["n"]): {"cfg": ci["cfg"], "radices": ci["radices"], "rows_per_cta": ci["rows_per_cta"],
+                                   "tuned_ms": [round(x, 4) for x in ci["tuned_ms"]]}
                     for ci in (s.class_info(c) for c in range(s.num_classes()))}
     cfg["pass_ms"] = {f"n{p['n']}_k{p['k']}": round(p["ms"], 4) for p in passes}
 

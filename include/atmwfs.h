@@ -181,8 +181,12 @@ atmwfs_status atmwfs_time_pass(atmwfs_ctx* ctx, int k, int c, int reps, double* 
                                int* count);
 int atmwfs_num_classes(const atmwfs_ctx* ctx);
 
-/* Tile configurations the engine compiles for every grid size. */
-#define ATMWFS_NUM_TILE_CFG 3
+/* Pass configurations (radix plan x tile shape) the engine can compile per
+ * grid size: 0-2 the default radix plan in three tile shapes, 3-4 the
+ * size's alternative radix plan where it has one (1024: 16 x 8 x 8 against
+ * the default 32 x 32).  The autotuner times every configuration compiled
+ * for a grid class and keeps the fastest. */
+#define ATMWFS_NUM_TILE_CFG 5
 
 /* Grid class ci (instances sharing wf_raw_size and wf_size): sizes, member
  * count, the rows per CTA the autotuner chose, and the mean time [ms] of the
@@ -190,6 +194,11 @@ int atmwfs_num_classes(const atmwfs_ctx* ctx);
  * forced). */
 atmwfs_status atmwfs_class_info(const atmwfs_ctx* ctx, int ci, int* n, int* nout, int* count, int* rows_per_cta,
                                 double* tuned_ms);
+
+/* The configuration the autotuner chose for grid class ci (0 ..
+ * ATMWFS_NUM_TILE_CFG - 1, see above) and the radix sequence of its
+ * forward transform (radices[0..2], 0 after the last stage). */
+atmwfs_status atmwfs_class_plan(const atmwfs_ctx* ctx, int ci, int* cfg, int* radices);
 
 /* Current layer positions (pixels) of instance i, after the last step. */
 atmwfs_status atmwfs_positions(const atmwfs_ctx* ctx, int i, double* xpos, double* ypos);

@@ -48,11 +48,38 @@ void emu_fft2_ct(std::vector<std::array<float2, E>>& V, float2* buf, const float
     }
 }
 
-template <int N, int T, int E>
+// The three-stage compile-time plan of the alternative radix plans (fft3_ct).
+template <int N, int T, int E, int RA, int RB, int RC>
+void emu_fft3_ct(std::vector<std::array<float2, E>>& V, float2* buf, const float2* twsB, const float2* twsC)
+{
+    for (int t = 0; t < T; t++) stage_dft<E, RA, -1>(V[t].data());
+    for (int t = 0; t < T; t++) stage_store<N, T, E, RA, 1>(V[t].data(), buf, t);
+    for (int t = 0; t < T; t++) {
+        stage_load<N, T, E, RB>(V[t].data(), buf, t);
+        stage_twiddle_rt<N, T, E, RB>(V[t].data(), t, twsB, RA);
+        stage_dft<E, RB, -1>(V[t].data());
+    }
+    for (int t = 0; t < T; t++) stage_store<N, T, E, RB, RA>(V[t].data(), buf, t);
+    for (int t = 0; t < T; t++) {
+        stage_load<N, T, E, RC>(V[t].data(), buf, t);
+        stage_twiddle_rt<N, T, E, RC>(V[t].data(), t, twsC, RA * RB);
+        stage_dft<E, RC, -1>(V[t].data());
+    }
+}
+
+template <int N, int T, int E, int PV = 0>
 void emu_fft_rt(std::vector<std::array<float2, E>>& V, float2* buf, const float2* tw, float ds, int rev)
 {
     if (ds > 0.0f)
         for (int t = 0; t < T; t++) conj_all<E>(V[t].data());
+    if constexpr (PV != 0 && Stages<N, PV>::S == 3) {
+        constexpr int R0 = Stages<N, PV>::R0, R1 = Stages<N, PV>::R1, R2 = Stages<N, PV>::R2;
+        if (rev) emu_fft3_ct<N, T, E, R2, R1, R0>(V, buf, tw + tw_offset<N, PV>(1, 1), tw + tw_offset<N, PV>(1, 2));
+        else emu_fft3_ct<N, T, E, R0, R1, R2>(V, buf, tw + tw_offset<N, PV>(0, 1), tw + tw_offset<N, PV>(0, 2));
+        if (ds > 0.0f)
+            for (int t = 0; t < T; t++) conj_all<E>(V[t].data());
+        return;
+    }
     if constexpr (Stages<N>::S == 2) {
         constexpr int R0 = Stages<N>::R0, R1 = Stages<N>::R1;
         if (rev) emu_fft2_ct<N, T, E, R1, R0>(V, buf, tw + tw_offset<N>(1, 1));
@@ -93,21 +120,22 @@ static std::vector<cd> dft(const std::vector<cd>& x, int sign)
     return X;
 }
 
-template <int N>
+template <int N, int PV = 0>
 void check_fft()
 {
-    constexpr int T = Plan<N>::T, E = Plan<N>::E;
-    std::vector<float2> tw(tw_total<N>() + 1);
-    build_twiddles<N>(tw.data());
+    constexpr int T = Plan<N, PV>::T, E = Plan<N, PV>::E;
+    std::vector<float2> tw(tw_total<N, PV>() + 1);
+    build_twiddles<N, PV>(tw.data());
     std::vector<float2> buf(padi(N) + 64);
     std::vector<cd> x(N);
     for (int i = 0; i < N; i++) x[i] = cd(urand() - 0.5, urand() - 0.5);
-    constexpr int RL = last_radix<N>();
+    constexpr int RL = last_radix<N, PV>();
+    const char* sfx = PV == 0 ? "" : "v1";
     for (int D : {-1, +1}) {
         std::vector<std::array<float2, E>> V(T);
         for (int t = 0; t < T; t++)
             for (int e = 0; e < E; e++) V[t][e] = make_float2((float)x[t + e * T].real(), (float)x[t + e * T].imag());
-        emu_fft_rt<N, T, E>(V, buf.data(), tw.data(), (float)D, 0);
+        emu_fft_rt<N, T, E, PV>(V, buf.data(), tw.data(), (float)D, 0);
         std::vector<cd> X = dft(x, D);
         double err = 0, nrm = 0;
         std::vector<int> seen(N, 0);
@@ -119,8 +147,8 @@ void check_fft()
                 nrm = fmax(nrm, std::abs(X[k]));
             }
         for (int k = 0; k < N; k++)
-            if (seen[k] != 1) { printf("fft%s_%d_coverage 1e9\n", D < 0 ? "fwd" : "inv", N); return; }
-        printf("fft%s_%d %.3e\n", D < 0 ? "fwd" : "inv", N, err / nrm);
+            if (seen[k] != 1) { printf("fft%s_%d%s_coverage 1e9\n", D < 0 ? "fwd" : "inv", N, sfx); return; }
+        printf("fft%s_%d%s %.3e\n", D < 0 ? "fwd" : "inv", N, sfx, err / nrm);
     }
     // propagation: forward, multiply by a unit-modulus table, inverse
     std::vector<float2> h(N);
@@ -133,10 +161,10 @@ void check_fft()
     std::vector<std::array<float2, E>> V(T);
     for (int t = 0; t < T; t++)
         for (int e = 0; e < E; e++) V[t][e] = make_float2((float)x[t + e * T].real(), (float)x[t + e * T].imag());
-    emu_fft_rt<N, T, E>(V, buf.data(), tw.data(), -1.0f, 0);
+    emu_fft_rt<N, T, E, PV>(V, buf.data(), tw.data(), -1.0f, 0);
     for (int t = 0; t < T; t++)
         for (int s = 0; s < E; s++) V[t][s] = cmul(V[t][s], h[last_index<N, T, RL>(t, s)]);
-    emu_fft_rt<N, T, E>(V, buf.data(), tw.data(), 1.0f, 1);
+    emu_fft_rt<N, T, E, PV>(V, buf.data(), tw.data(), 1.0f, 1);
     std::vector<cd> X = dft(x, -1);
     for (int k = 0; k < N; k++) X[k] *= hd[k];
     std::vector<cd> y = dft(X, +1);
@@ -146,7 +174,7 @@ void check_fft()
             err = fmax(err, std::abs(cd(V[t][e].x, V[t][e].y) - y[t + e * T]));
             nrm = fmax(nrm, std::abs(y[t + e * T]));
         }
-    printf("prop_%d %.3e\n", N, err / nrm);
+    printf("prop_%d%s %.3e\n", N, sfx, err / nrm);
 }
 
 // ---------------------------------------------------------------------------
@@ -280,6 +308,7 @@ int main()
     check_fft<256>();
     check_fft<512>();
     check_fft<1024>();
+    check_fft<1024, 1>();  // alternative radix plan 16 x 8 x 8
     check_fft<2048>();
     check_fft<4096>();   // whole-row plans of the large 2-D transforms
     check_fft<8192>();

@@ -1,5 +1,5 @@
 """CPU emulation of the kernels' in-CTA building blocks (same template code):
-Stockham FFT stages for every supported grid, the transfer-table row
+Stockham FFT stages for every supported grid and radix plan, the transfer-table row
 propagation, the TMA tile geometry of the bicubic screen gather, and the
 FP32-only atan2 of the science unwrap."""
 import shutil
@@ -23,7 +23,7 @@ def emul_output(tmp_path_factory):
     return dict((l.split()[0], float(l.split()[1])) for l in out.strip().splitlines())
 
 
-@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, 2048, 4096, 8192])
+@pytest.mark.parametrize("n", [64, 128, 256, 512, 1024, "1024v1", 2048, 4096, 8192])
 def test_fft_stages(emul_output, n):
     assert emul_output[f"fftfwd_{n}"] < 5e-7
     assert emul_output[f"fftinv_{n}"] < 5e-7

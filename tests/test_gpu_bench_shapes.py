@@ -60,14 +60,67 @@ def test_one_context_mixing_grid_classes(lib, oracle64):
     _report("mixed 256/512/1024", ms)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_w1024_every_tile_configuration(lib, oracle64, monkeypatch, cfg):
     """The 1024^2 passes (gather, both propagations, epilogue, science bins on
-    51 x 51 bins) in each compiled tile configuration."""
+    51 x 51 bins) in each compiled configuration: the 32 x 32 radix plan in
+    three tile shapes (0-2) and the 16 x 8 x 8 plan in two (3, 4)."""
     monkeypatch.setenv("ATMWFS_TILE_CFG", str(cfg))
     case = bench_case(W=1024, Wout=1024, sci=[(0.5e-6, 0.0, 0.0), (1.6e-6, TEN, -TEN), (2.4e-6, -TEN, 0.0)])
     ms = compare(case, oracle64, 2)
     _report(f"W=1024 tile configuration {cfg}", ms)
+
+
+@pytest.mark.parametrize("cfg", [3, 4])
+def test_w1024_alternative_plan_grouped_layers(lib, oracle64, monkeypatch, cfg):
+    """The 16 x 8 x 8 plan on a plane of two layers (0 and 50 m share a
+    super-layer: the second layer's window rows come from global memory), a
+    crop and a lambda-ref instance."""
+    monkeypatch.setenv("ATMWFS_TILE_CFG", str(cfg))
+    case = Case(alt=[0.0, 50.0, 5000.0, 12000.0], cn2=[0.4, 0.2, 0.3, 0.1], speed=[8.0, 12.0, 25.0, 30.0],
+                direction=[0.1, 1.0, 3.0, 5.5], M=2048, W=1024, Wout=1000, fresnel_bin=100.0,
+                sci=[(1.25e-6, 0.0, 0.0), (2.2e-6, TEN, -TEN)])
+    ms = compare(case, oracle64, 2)
+    _report(f"W=1024 configuration {cfg}, grouped layers", ms)
+
+
+def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
+    """The autotuner times every configuration compiled for a grid size --
+    at 1024 the 32 x 32 plan in three tile shapes and the 16 x 8 x 8 plan in
+    two -- and reports the one it keeps; a forced configuration is taken as
+    given."""
+    from atmosphericturbulencesimul_gb300 import Series
+    from series_case import instances, make_screens
+
+    case = bench_case(W=1024, Wout=1024, sci=[(1.6e-6, 0.0, 0.0), (0.8e-6, 0.0, 0.0, 512, 512)])
+    screens = make_screens(case, oracle64)
+
+    def classes():
+        s = Series(case.alt, case.cn2, case.speed, case.direction, master_size=case.M, instances=instances(case),
+                   pupil_scale=case.pupil, time_step=case.dt, fresnel_bin=case.fresnel_bin, zangle=case.zangle,
+                   amplitude=case.amplitude, fresnel=case.fresnel)
+        for l, sc in enumerate(screens):
+            s.load_screen(l, sc)
+        s.run_frames(1)
+        info = {ci["n"]: ci for ci in (s.class_info(c) for c in range(s.num_classes()))}
+        s.close()
+        return info
+
+    monkeypatch.delenv("ATMWFS_TILE_CFG", raising=False)
+    info = classes()
+    assert set(info) == {512, 1024}
+    assert all(t > 0 for t in info[1024]["tuned_ms"])          # five configurations timed at 1024
+    assert info[512]["tuned_ms"][3:] == [0.0, 0.0]             # no alternative plan at 512
+    for n, ci in info.items():
+        assert int(np.prod(ci["radices"])) == n
+        timed = [t for t in ci["tuned_ms"] if t > 0]
+        assert ci["tuned_ms"][ci["cfg"]] == min(timed)
+    print("\nautotuner:", json.dumps({n: {k: ci[k] for k in ("cfg", "radices", "rows_per_cta", "tuned_ms")}
+                                      for n, ci in info.items()}))
+    monkeypatch.setenv("ATMWFS_TILE_CFG", "3")
+    info = classes()
+    assert info[1024]["cfg"] == 3 and info[1024]["radices"] == [16, 8, 8] and info[1024]["rows_per_cta"] == 4
+    assert info[512]["cfg"] == 0 and info[512]["radices"] == [32, 16]
 
 
 def test_w2048_step(lib, oracle64):
