@@ -272,6 +272,8 @@ __global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __rest
     for (int jj = blockIdx.x; jj < Nout; jj += gridDim.x) {
         const int bj = nb > 0 ? binx[jj] * nb : 0;
         const size_t ro = (size_t)jj * Nout;
+        const float2* __restrict__ gs = I.gsum ? I.gsum + (size_t)(jj + I.off) * I.wstride + I.off : nullptr;
+        const float sc = I.scoeff[0];
         auto one = [&](float p, float s, int ii) {
             const float peak = nb > 0 ? peakv[bj + binx[ii]] : 0.0f;
             float d1, e1, d2, e2;
@@ -283,12 +285,20 @@ __global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __rest
             for (int i4 = threadIdx.x; i4 < Nout / 4; i4 += blockDim.x) {
                 const int ii = 4 * i4;
                 const float4 p = *reinterpret_cast<const float4*>(pha + ro + ii);
-                const float4 s = *reinterpret_cast<const float4*>(psum + ro + ii);
+                float4 s;
+                if (gs) {
+                    const float2 g0 = gs[ii], g1 = gs[ii + 1], g2 = gs[ii + 2], g3 = gs[ii + 3];
+                    s = make_float4(fmaf(sc, g0.x, sc * g0.y), fmaf(sc, g1.x, sc * g1.y), fmaf(sc, g2.x, sc * g2.y),
+                                    fmaf(sc, g3.x, sc * g3.y));
+                } else {
+                    s = *reinterpret_cast<const float4*>(psum + ro + ii);
+                }
                 *reinterpret_cast<float4*>(pha + ro + ii) =
                     make_float4(one(p.x, s.x, ii), one(p.y, s.y, ii + 1), one(p.z, s.z, ii + 2), one(p.w, s.w, ii + 3));
             }
         } else {
-            for (int ii = threadIdx.x; ii < Nout; ii += blockDim.x) pha[ro + ii] = one(pha[ro + ii], psum[ro + ii], ii);
+            for (int ii = threadIdx.x; ii < Nout; ii += blockDim.x)
+                pha[ro + ii] = one(pha[ro + ii], gs ? fmaf(sc, gs[ii].x, sc * gs[ii].y) : psum[ro + ii], ii);
         }
     }
 }
@@ -298,6 +308,48 @@ cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxno
     if (nsci <= 0) return cudaSuccess;
     const int bx = maxnout < 256 ? maxnout : 256;
     k_sci_apply<<<dim3(bx, nsci), 256, 0, st>>>(insts, list, d_step);
+    return cudaGetLastError();
+}
+
+// Layer sum of one window group, from the top layer down with a two-sum
+// (the order of the reference's accumulation, AtmosphericTurbulence.c:2909-2916,
+// without the per-layer Scoeff that factors out of the sum): four pixels per
+// thread as 16-byte vectors, every layer requested before the sums.
+__global__ void __launch_bounds__(256) k_group_sum(const GroupSumJob* __restrict__ jobs, int L)
+{
+    const GroupSumJob& J = jobs[blockIdx.y];
+    const long n4 = (long)J.side * J.side / 4;
+    for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (long)gridDim.x * blockDim.x) {
+        float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        float4 w[kMaxLayers];
+#pragma unroll
+        for (int l = 0; l < kMaxLayers; l++)
+            if (l < L) w[l] = __ldg(reinterpret_cast<const float4*>(J.win[l]) + k);
+#pragma unroll
+        for (int l = kMaxLayers - 1; l >= 0; l--) {
+            if (l >= L) continue;
+            const float wv[4] = {w[l].x, w[l].y, w[l].z, w[l].w};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float s = __fadd_rn(hi[j], wv[j]);
+                const float bp = __fsub_rn(s, hi[j]);
+                const float e = __fadd_rn(__fsub_rn(hi[j], __fsub_rn(s, bp)), __fsub_rn(wv[j], bp));
+                hi[j] = s;
+                lo[j] = __fadd_rn(lo[j], e);
+            }
+        }
+        float4* o = reinterpret_cast<float4*>(J.out) + 2 * k;
+        o[0] = make_float4(hi[0], lo[0], hi[1], lo[1]);
+        o[1] = make_float4(hi[2], lo[2], hi[3], lo[3]);
+    }
+}
+
+cudaError_t group_sums(const GroupSumJob* jobs, int njobs, int L, int maxside, cudaStream_t st)
+{
+    if (njobs <= 0) return cudaSuccess;
+    const long n4 = (long)maxside * maxside / 4;
+    const long b = (n4 + 255) / 256;
+    k_group_sum<<<dim3((unsigned)(b < 1024 ? b : 1024), (unsigned)njobs), 256, 0, st>>>(jobs, L);
     return cudaGetLastError();
 }
 

@@ -12,6 +12,9 @@ cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int max
                         const float2* atan_tab, cudaStream_t st);
 cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxnout, const int* d_step, cudaStream_t st);
 cudaError_t step_advance(int* d_step, cudaStream_t st);
+// Compensated layer sums of the window groups with a layer-independent
+// Scoeff (one job per group, maxside the largest side).
+cudaError_t group_sums(const GroupSumJob* jobs, int njobs, int L, int maxside, cudaStream_t st);
 // Frame copy-out by a small grid of copy CTAs (16-byte aligned pointers,
 // counts in float4): dst0 = src0, dst1 = src1 (either pair may be absent).
 cudaError_t copy_out(const float4* src0, float4* dst0, long n0, const float4* src1, float4* dst1, long n1,

@@ -290,6 +290,11 @@ struct Class {
     // owns the TMA maps of that size computes them), tile configuration 0
     std::vector<WinJob> jobs;
     WinJob* d_jobs = nullptr;
+    // layer sums of the same groups (those with a factoring Scoeff), and
+    // whether any member still needs its own phase sum (k_phasum)
+    std::vector<GroupSumJob> gjobs;
+    GroupSumJob* d_gjobs = nullptr;
+    bool need_phasum = true;
 };
 
 }  // namespace atmwfs
@@ -332,6 +337,9 @@ struct atmwfs_ctx {
     std::vector<int> group_of;           // global instance -> group
     std::vector<int> group_leader, wg;
     std::vector<float*> d_win[2];        // [orient][group * L + layer], or null
+    // per group: its layer sum (k_group_sum) when every member's Scoeff is
+    // the same for all layers, else null
+    std::vector<float2*> d_gsum;
     std::vector<InstDev> hinst;          // class order
     std::vector<int> slot_of;            // global index -> class-order slot
     InstDev* d_inst = nullptr;
@@ -487,8 +495,18 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
     const int Q = (int)c->plane_lo.size();
     const int P = Q - 1;
     if (k == 0) {
-        // geometric phase sum of all layers over the crop (k_phasum), from
-        // the step's windows
+        // geometric phase sums: the layer sums of the window groups this class
+        // computes (instances whose Scoeff factors out), then the per-instance
+        // sums of the others (k_phasum), from the step's windows
+        double b = 0;
+        if (!cl.gjobs.empty()) {
+            AW_CUDA(group_sums(cl.d_gjobs, (int)cl.gjobs.size(), c->L, cl.N, st));
+            b += (4.0 * c->L + 8.0) * (double)cl.N * cl.N * cl.gjobs.size();
+        }
+        if (!cl.need_phasum) {
+            if (bytes) *bytes = b;
+            return ATMWFS_OK;
+        }
         PassArgs a;
         memset(&a, 0, sizeof a);
         a.inst = c->d_inst + cl.base;
@@ -497,7 +515,9 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
         a.L = c->L;
         a.ninst_total = c->ninst;
         a.poscap = c->poscap;
-        if (bytes) *bytes = (4.0 * c->L + 4.0) * cl.Nout * cl.Nout * cl.members.size();
+        int own = 0;
+        for (int i : cl.members) own += c->d_gsum[c->group_of[i]] == nullptr;
+        if (bytes) *bytes = b + (4.0 * c->L + 4.0) * cl.Nout * cl.Nout * own;
         AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarPhasum, dim3(phasum_blocks(cl.Nout), (unsigned)cl.members.size()), a,
                                         nullptr, nullptr, st));
         return ATMWFS_OK;
@@ -745,8 +765,40 @@ atmwfs_status commit(atmwfs_ctx* c)
         if (!cl.d_jobs) AW_TRY(dalloc(c, (void**)&cl.d_jobs, sizeof(WinJob) * cl.jobs.size()));
         AW_CUDA(cudaMemcpyAsync(cl.d_jobs, cl.jobs.data(), sizeof(WinJob) * cl.jobs.size(), cudaMemcpyHostToDevice, c->st));
     }
+    // Phase-sum factoring per group (ATMWFS_GROUP_PHASE_SUM=0 turns it off):
+    // every member's Scoeff equal on all layers (bit for bit)
+    const char* gps = getenv("ATMWFS_GROUP_PHASE_SUM");
+    const bool factor = !(gps && atoi(gps) == 0);
+    c->d_gsum.resize(G, nullptr);
+    for (int g = 0; g < G; g++) {
+        bool ok = factor && c->L <= kMaxLayers;
+        for (int i = 0; i < c->ninst && ok; i++)
+            if (c->group_of[i] == g)
+                for (int l = 1; l < c->L && ok; l++) ok = c->scoeff[i][l] == c->scoeff[i][0];
+        if (ok && !c->d_gsum[g]) AW_TRY(dalloc(c, (void**)&c->d_gsum[g], sizeof(float2) * (size_t)c->wg[g] * c->wg[g]));
+    }
+    for (Class& cl : c->classes) {
+        cl.gjobs.clear();
+        for (const WinJob& j : cl.jobs) {
+            const int g = c->group_of[j.gidx];
+            if (j.orient != 0 || j.layer != 0 || !c->d_gsum[g]) continue;
+            GroupSumJob gj;
+            memset(&gj, 0, sizeof gj);
+            gj.out = c->d_gsum[g];
+            gj.side = c->wg[g];
+            for (int l = 0; l < c->L; l++) gj.win[l] = c->d_win[0][(size_t)g * c->L + l];
+            cl.gjobs.push_back(gj);
+        }
+        cl.need_phasum = false;
+        for (int i : cl.members) cl.need_phasum = cl.need_phasum || !c->d_gsum[c->group_of[i]];
+        if (cl.gjobs.empty()) continue;
+        if (!cl.d_gjobs) AW_TRY(dalloc(c, (void**)&cl.d_gjobs, sizeof(GroupSumJob) * cl.gjobs.size()));
+        AW_CUDA(cudaMemcpyAsync(cl.d_gjobs, cl.gjobs.data(), sizeof(GroupSumJob) * cl.gjobs.size(),
+                                cudaMemcpyHostToDevice, c->st));
+    }
     for (InstDev& d : c->hinst) {
         const int g = c->group_of[d.gidx];
+        d.gsum = c->d_gsum[g];
         d.wstride = c->wg[g];
         for (int o = 0; o < 2; o++)
             for (int l = 0; l < c->L; l++) d.win[o][l] = c->d_win[o][(size_t)g * c->L + l];

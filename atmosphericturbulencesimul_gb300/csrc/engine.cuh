@@ -53,6 +53,20 @@ struct InstDev {
     // samples: the pass multiplies by scoeff.
     const float* win[2][kMaxLayers];
     int wstride;
+    // Geometric phase sum by factoring: when every member of the window
+    // group has one Scoeff for all its layers, the group's compensated layer
+    // sum sum_l window_l is formed once per step (k_group_sum; (hi, lo) pairs,
+    // wstride x wstride, pass coordinates) and this instance's phase sum is
+    // scoeff[0] * (hi + lo).  Null: the per-instance sum in phisum.
+    const float2* gsum;
+};
+
+// One window group's layer sum (k_group_sum): its L windows in the screen
+// orientation, side x side, and the (hi, lo) output.
+struct GroupSumJob {
+    float2* out;
+    const float* win[kMaxLayers];
+    int side;
 };
 
 // One window of the per-step window kernel: layer `layer` of group leader

@@ -9,6 +9,7 @@
 // gather + phasor, 1-D propagation]: a frame with P hops costs P + 1 passes.
 #pragma once
 #include "engine.cuh"
+#include "epi_math.cuh"
 #include "fft_half.cuh"
 #include "gather_core.cuh"
 
@@ -456,15 +457,36 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
         for (int e = 0; e < E; e++) xrow[padi(t + e * T)] = v[e];
         const int ya = max(y0, off), yb = min(y0 + RR, off + Nout);
         if (ya >= yb) return;  // uniform: the CTA has no crop row
-        // prefetch this thread's phase sums
+        // prefetch this thread's phase sums: every load issued before any
+        // is used (one uniform branch between the two sources, predicated
+        // loads inside)
         float ps[RR][CPT];
+        if (const float2* __restrict__ gs = I->gsum) {
+            const float sg = I->scoeff[0];
+            const size_t ws = (size_t)I->wstride;
+            float2 g[RR][CPT];
 #pragma unroll
-        for (int r = 0; r < RR; r++)
+            for (int r = 0; r < RR; r++)
 #pragma unroll
-            for (int c = 0; c < CPT; c++) {
-                const int x = off + tid + c * NT, y = y0 + r;
-                ps[r][c] = (y >= ya && y < yb && x < off + Nout) ? psum[(size_t)(y - off) * Nout + (x - off)] : 0.0f;
-            }
+                for (int c = 0; c < CPT; c++) {
+                    const int x = off + tid + c * NT, y = y0 + r;
+                    const bool in = y >= ya && y < yb && x < off + Nout;
+                    g[r][c] = in ? __ldg(gs + (size_t)y * ws + x) : make_float2(0.0f, 0.0f);
+                }
+#pragma unroll
+            for (int r = 0; r < RR; r++)
+#pragma unroll
+                for (int c = 0; c < CPT; c++) ps[r][c] = fmaf(sg, g[r][c].x, sg * g[r][c].y);
+        } else {
+#pragma unroll
+            for (int r = 0; r < RR; r++)
+#pragma unroll
+                for (int c = 0; c < CPT; c++) {
+                    const int x = off + tid + c * NT, y = y0 + r;
+                    const bool in = y >= ya && y < yb && x < off + Nout;
+                    ps[r][c] = in ? psum[(size_t)(y - off) * Nout + (x - off)] : 0.0f;
+                }
+        }
         __syncthreads();
         const int nb = I->nb;
         const bool bins = (mode == kModeSci) && nb > 0;
@@ -472,6 +494,12 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
         const int jb0 = bins ? binx[ya - off] : 0;
         // bins are at least 20 rows tall: RR rows touch at most NJ bin rows
         constexpr int NJ = G::NJ;
+        int jr[RR];  // bin row of each of the CTA's rows, relative to jb0
+#pragma unroll
+        for (int r = 0; r < RR; r++) {
+            const int y = y0 + r;
+            jr[r] = (bins && y >= ya && y < yb) ? binx[y - off] - jb0 : 0;
+        }
         // [NJ][N]: per bin row, per column; clear of the staged rows in xb
         float2* colsum = reinterpret_cast<float2*>(wrows);
 #pragma unroll
@@ -490,8 +518,8 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
                     continue;
                 }
                 const float2 u = xb[r * RS + padi(x)];
-                oamp[o] = sqrtf(u.x * u.x + u.y * u.y);
-                const float pha = atan2f(u.y, u.x);
+                oamp[o] = sqrt_approx(fmaf(u.x, u.x, u.y * u.y));
+                const float pha = atan2_out(u.y, u.x);
                 if (mode == kModeRef) {
                     opha[o] = add_2pi_multiple(pha, round_2pi(ps[r][c], 0.0f));
                 } else {
@@ -500,7 +528,7 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
                         float d, de;
                         two_sum(ps[r][c], -pha, d, de);
                         const float2 z = phasor(d + de);  // exp(i (sum - pha))
-                        const int j = binx[y - off] - jb0;
+                        const int j = jr[r];
                         if (j == 0) {
                             acc0.x += z.x;
                             acc0.y += z.y;
@@ -615,6 +643,7 @@ __global__ void __launch_bounds__(kPhasumThreads, 4) k_phasum(const __grid_const
 {
     constexpr int kChunk = 8;
     const InstDev* I = a.inst + blockIdx.y;
+    if (I->gsum) return;  // this instance's phase sum factors through its group's layer sum
     const int off = I->off, Nout = I->Nout, L = a.L;
     const size_t ws = (size_t)I->wstride;
     const bool v4 = (off % 4) == 0 && (Nout % 4) == 0;

@@ -20,6 +20,7 @@
 #include "fft_core.cuh"
 #include "gather_core.cuh"
 #include "atan_ff.cuh"
+#include "epi_math.cuh"
 
 using namespace atmwfs;
 using cd = std::complex<double>;
@@ -300,9 +301,46 @@ static void check_atan2()
     std::printf("atan2_count %ld\n", n);
 }
 
+// The output epilogue's FP32 atan2 against the double atan2: the largest
+// absolute difference in radians over every quadrant, the octant boundaries,
+// the tan(pi/8) switch, magnitudes spread over many decades, and the axes.
+static void check_atan2_out()
+{
+    double worst = 0;
+    long n = 0;
+    auto one = [&](float y, float x) {
+        const double ref = atan2((double)y, (double)x);
+        double d = fabs((double)atan2_out(y, x) - ref);
+        if (d > M_PI) d = fabs(d - 2 * M_PI);  // +-pi on the negative x axis
+        worst = fmax(worst, d);
+        n++;
+    };
+    for (int i = 0; i < 2000000; i++) {
+        const double ang = (urand() * 2 - 1) * M_PI, mag = pow(10.0, urand() * 12 - 6);
+        one((float)(mag * sin(ang)), (float)(mag * cos(ang)));
+    }
+    const double t8 = tan(M_PI / 8);
+    for (int i = -2000; i <= 2000; i++)
+        for (int q = 0; q < 8; q++) {
+            const double base = q * M_PI / 4, ang = base + i * 1e-7;
+            one((float)sin(ang), (float)cos(ang));
+            const double a2 = atan(t8) + q * M_PI / 2 + i * 1e-7;
+            one((float)(3.0 * sin(a2)), (float)(3.0 * cos(a2)));
+        }
+    for (float v : {1.0f, -1.0f, 1e-30f, -1e30f}) {
+        one(v, 0.0f);
+        one(0.0f, v);
+        one(v, v);
+        one(-v, v);
+    }
+    std::printf("atan2out_count %ld\n", n);
+    std::printf("atan2out_maxerr %.3e\n", worst);
+}
+
 int main()
 {
     check_atan2();
+    check_atan2_out();
     check_fft<64>();
     check_fft<128>();
     check_fft<256>();

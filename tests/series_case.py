@@ -33,6 +33,7 @@ class Case:
     fresnel: int = 1
     seed: int = 7
     air_index: bool = False   # hops with lambda / n(air) (atmwfs_instance.hop_n)
+    flat_scoeff: bool = False  # one Scoeff for all layers (a fixed gas mixture, as refractivity.scoeff)
 
 
 def make_screens(case: Case, o64) -> list[np.ndarray]:
@@ -56,6 +57,9 @@ def scoeff_for(case: Case, lam: float) -> np.ndarray:
     """A deterministic stand-in for CONF_LAMBDA/SLAMBDA * N(h,lam)/N(h,lam_ref):
     the vacuum ratio times a mild altitude-dependent dispersion factor."""
     L = len(case.alt)
+    if case.flat_scoeff:
+        return np.full(L, np.float32(np.float32(case.lam_ref) / lam * (1.0 - 1e-3 * (1.0 - case.lam_ref / lam))),
+                       np.float32)
     disp = 1.0 - 2e-3 * (1.0 - case.lam_ref / lam) * np.exp(-np.asarray(case.alt) / 8000.0)
     return (np.float32(case.lam_ref) / lam * disp).astype(np.float32) * np.ones(L, np.float32)
 
@@ -80,9 +84,9 @@ def instances(case: Case):
     return out
 
 
-def run_gpu(case: Case, screens, nsteps: int, ring: int = 1):
+def run_gpu(case: Case, screens, nsteps: int, ring: int = 1, specs=None):
     from atmosphericturbulencesimul_gb300 import Series
-    inst = instances(case)
+    inst = instances(case) if specs is None else specs
     s = Series(case.alt, case.cn2, case.speed, case.direction, master_size=case.M, instances=inst,
                pupil_scale=case.pupil, time_step=case.dt, fresnel_bin=case.fresnel_bin, zangle=case.zangle,
                amplitude=case.amplitude, fresnel=case.fresnel, ring=ring)
@@ -95,9 +99,9 @@ def run_gpu(case: Case, screens, nsteps: int, ring: int = 1):
     return inst, frames, pos, planes
 
 
-def run_oracle(case: Case, o64, screens, nsteps: int):
+def run_oracle(case: Case, o64, screens, nsteps: int, specs=None):
     """Per step, per instance (pha, amp) from the FP64 oracle."""
-    inst = instances(case)
+    inst = instances(case) if specs is None else specs
     cn2 = np.asarray(case.cn2, float)
     cn2 = cn2 * (1.0 / cn2.sum())
     salt, sidx = o64.superlayers(case.alt, cn2, case.fresnel_bin)
@@ -144,9 +148,10 @@ def metrics(pha_g, amp_g, pha_o, amp_o, lam):
 
 
 def compare(case: Case, o64, nsteps: int, wrapped_nm: float = 0.05, flip: float = 2e-3, amp_var: float = 1e-3,
-            screens=None):
+            screens=None, specs=None):
     """Run `case` for `nsteps` on the GPU and in the FP64 oracle from the same
-    screens and assert the parity bars on every frame:
+    screens (and instance list `specs`, default instances(case)) and assert
+    the parity bars on every frame:
       * layer positions equal bit for bit (the reference's sequential update);
       * wrapped phase error < `wrapped_nm` nm rms, amplitude error < 2e-3;
       * a 2 pi jump of the unwrapped phase on fewer than `flip` of the pixels;
@@ -155,8 +160,8 @@ def compare(case: Case, o64, nsteps: int, wrapped_nm: float = 0.05, flip: float 
     Returns the metrics of every frame, with the instance's grid and step."""
     if screens is None:
         screens = make_screens(case, o64)
-    inst_g, frames, pos_g, _ = run_gpu(case, screens, nsteps)
-    inst_o, res, pos_o, _ = run_oracle(case, o64, screens, nsteps)
+    inst_g, frames, pos_g, _ = run_gpu(case, screens, nsteps, specs=specs)
+    inst_o, res, pos_o, _ = run_oracle(case, o64, screens, nsteps, specs=specs)
     for (xg, yg), (xo, yo) in zip(pos_g, pos_o):
         assert np.array_equal(xg, xo) and np.array_equal(yg, yo)
     out = []

@@ -47,3 +47,11 @@ def test_atan2_fp32_only(emul_output):
     assert emul_output["atan2_count"] > 3_000_000
     assert emul_output["atan2_diff"] == 0
     assert emul_output["atan2_maxulp"] == 0
+
+
+def test_atan2_output_epilogue(emul_output):
+    """The last pass's FP32 atan2 (octant reduction and a degree-9 odd
+    polynomial) against the double atan2 on about two million inputs: within
+    3e-7 rad everywhere (one or two float roundings of pi near +-pi)."""
+    assert emul_output["atan2out_count"] > 2_000_000
+    assert emul_output["atan2out_maxerr"] < 3e-7

@@ -16,7 +16,7 @@ import json
 import numpy as np
 import pytest
 
-from series_case import Case, compare, worst
+from series_case import Case, compare, worst  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
@@ -58,6 +58,47 @@ def test_one_context_mixing_grid_classes(lib, oracle64):
     ms = compare(case, oracle64, 3)
     assert {m["W"] for m in ms} == {256, 512, 1024}
     _report("mixed 256/512/1024", ms)
+
+
+@pytest.mark.parametrize("factor", ["1", "0"])
+def test_phase_sum_factored_per_window_group(lib, oracle64, monkeypatch, factor):
+    """Scoeff equal on all layers (a fixed gas mixture, the benchmark's
+    case): the phase sum of every instance of a window group is its Scoeff
+    times the group's compensated layer sum, formed once per step; the
+    lambda-ref instance and the science instances of each direction read it
+    in the last pass's epilogue and in the science apply.  A direction whose
+    instances carry layer-dependent Scoeff keeps the per-instance sum in the
+    same context; ATMWFS_GROUP_PHASE_SUM=0 turns the factoring off."""
+    monkeypatch.setenv("ATMWFS_GROUP_PHASE_SUM", factor)
+    case = bench_case(W=1024, Wout=1024, flat_scoeff=True, sci=[
+        (0.5e-6, -TEN, -TEN, 256, 256),
+        (2.2e-6, -TEN, -TEN, 512, 400),
+        (1.25e-6, 0.0, 0.0, 1024, 1000),
+        (2.4e-6, 0.0, 0.0, 512, 512),
+        (0.9e-6, TEN, 0.0, 1024, 1024),
+    ])
+    ms = compare(case, oracle64, 2)
+    _report(f"phase sum factored ({factor})", ms)
+
+
+def test_phase_sum_factored_and_per_instance_groups(lib, oracle64, monkeypatch):
+    """One group whose members' Scoeff factors beside groups whose members'
+    does not (layer-dependent Scoeff): both kinds of phase sum in one step."""
+    monkeypatch.delenv("ATMWFS_GROUP_PHASE_SUM", raising=False)
+    case = bench_case(W=512, Wout=512, ref=False, sci=[
+        (0.7e-6, TEN, TEN, 512, 512),
+        (1.9e-6, TEN, TEN, 256, 200),
+        (1.1e-6, 0.0, 0.0, 512, 500),
+    ])
+    from series_case import instances as inst_of, make_screens
+    screens = make_screens(case, oracle64)
+    flat = Case(**{**case.__dict__, "flat_scoeff": True})
+    specs = inst_of(case)
+    specs_flat = inst_of(flat)
+    specs[2].scoeff = specs_flat[2].scoeff            # the on-axis direction factors
+    assert np.all(specs[2].scoeff == specs[2].scoeff[0]) and not np.all(specs[0].scoeff == specs[0].scoeff[0])
+    ms = compare(case, oracle64, 2, screens=screens, specs=specs)
+    _report("factored and per-instance phase sums", ms)
 
 
 @pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
