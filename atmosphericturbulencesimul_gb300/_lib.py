@@ -16,7 +16,7 @@ OK = 0
 STATUS_NAMES = {0: "OK", 1: "ERR_INVALID", 2: "ERR_NOMEM", 3: "ERR_CUDA", 4: "ERR_IO", 5: "ERR_TIMEOUT",
                 6: "ERR_STATE", 7: "ERR_NODEVICE"}
 MODE_REF, MODE_SCI, MODE_PHASE = 0, 1, 2
-NUM_TILE_CFG = 5  # ATMWFS_NUM_TILE_CFG
+NUM_TILE_CFG = 6  # ATMWFS_NUM_TILE_CFG
 
 
 class AtmwfsError(RuntimeError):

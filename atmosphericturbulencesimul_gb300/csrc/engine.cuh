@@ -149,32 +149,38 @@ typedef cudaError_t (*PassLauncherCfg)(int cfg, int var, dim3 grid, const PassAr
 
 // Pass configurations compiled per grid size: the radix plan (Plan / Stages
 // variant), rows per CTA, the minimum number of resident CTAs per SM the
-// kernel is register-limited to, and whether the screen tile overlays the
-// exchange rows.  Configurations 0-2 use the default plan: 0 is the
-// one-CTA-per-SM shape; 1 trades rows per tile for several resident CTAs
-// per SM; 2 also overlays the tile on the exchange buffer, which cuts shared
-// memory so that one more CTA fits per SM.  Configurations 3 and 4 run the
-// size's alternative radix plan (where it has one; rr = 0 elsewhere) in two
-// tile shapes.  The engine's autotuner times every compiled configuration of
-// a grid class at set-up and keeps the fastest.
+// kernel is register-limited to, whether the screen tile overlays the
+// exchange rows, and whether the hop transfer tables are staged in shared
+// memory.  Configurations 0-2 use the default plan with the tables read
+// through L1: 0 is the one-CTA-per-SM shape; 1 trades rows per tile for
+// several resident CTAs per SM; 2 also overlays the tile on the exchange
+// buffer, which cuts shared memory so that one more CTA fits per SM.
+// Configurations 3 and 4 run the size's alternative radix plan (where it has
+// one; rr = 0 elsewhere) in two tile shapes; configuration 5 is 1 with the
+// transfer tables copied into shared memory by cp.async at kernel start.
+// The engine's autotuner times every compiled configuration of a grid class
+// at set-up and keeps the fastest.
 struct TileCfg {
     int rr, minb;
     bool alias;
     int plan;
+    bool hsm;
 };
 constexpr int kNumTileCfg = ATMWFS_NUM_TILE_CFG;
 constexpr TileCfg tile_cfg(int N, int c)
 {
-    return c == 3 ? (N == 1024 ? TileCfg{4, 3, false, 1} : TileCfg{0, 0, false, 0})
-         : c == 4 ? (N == 1024 ? TileCfg{2, 6, false, 1} : TileCfg{0, 0, false, 0})
-         : c > 4  ? TileCfg{0, 0, false, 0}
-         : N == 64    ? (c == 0 ? TileCfg{32, 1, false, 0} : c == 1 ? TileCfg{16, 2, false, 0} : TileCfg{16, 3, true, 0})
-         : N == 128   ? (c == 0 ? TileCfg{32, 1, false, 0} : c == 1 ? TileCfg{16, 2, false, 0} : TileCfg{16, 3, true, 0})
-         : N == 256   ? (c == 0 ? TileCfg{16, 1, false, 0} : c == 1 ? TileCfg{8, 3, false, 0} : TileCfg{8, 4, true, 0})
-         : N == 512   ? (c == 0 ? TileCfg{16, 1, false, 0} : c == 1 ? TileCfg{8, 3, false, 0} : TileCfg{8, 4, true, 0})
-         : N == 1024  ? (c == 0 ? TileCfg{8, 1, false, 0} : c == 1 ? TileCfg{4, 3, false, 0} : TileCfg{4, 4, true, 0})
-         : N == 2048  ? (c == 0 ? TileCfg{4, 1, false, 0} : c == 1 ? TileCfg{2, 3, false, 0} : TileCfg{2, 3, true, 0})
-                      : TileCfg{0, 0, false, 0};
+    return c == 3 ? (N == 1024 ? TileCfg{4, 3, false, 1, false} : TileCfg{0, 0, false, 0, false})
+         : c == 4 ? (N == 1024 ? TileCfg{2, 6, false, 1, false} : TileCfg{0, 0, false, 0, false})
+         : c == 5 ? (N == 1024 ? TileCfg{4, 3, false, 0, true} : N == 512 ? TileCfg{8, 3, false, 0, true}
+                                                                          : TileCfg{0, 0, false, 0, false})
+         : c > 5  ? TileCfg{0, 0, false, 0, false}
+         : N == 64    ? (c == 0 ? TileCfg{32, 1, false, 0, false} : c == 1 ? TileCfg{16, 2, false, 0, false} : TileCfg{16, 3, true, 0, false})
+         : N == 128   ? (c == 0 ? TileCfg{32, 1, false, 0, false} : c == 1 ? TileCfg{16, 2, false, 0, false} : TileCfg{16, 3, true, 0, false})
+         : N == 256   ? (c == 0 ? TileCfg{16, 1, false, 0, false} : c == 1 ? TileCfg{8, 3, false, 0, false} : TileCfg{8, 4, true, 0, false})
+         : N == 512   ? (c == 0 ? TileCfg{16, 1, false, 0, false} : c == 1 ? TileCfg{8, 3, false, 0, false} : TileCfg{8, 4, true, 0, false})
+         : N == 1024  ? (c == 0 ? TileCfg{8, 1, false, 0, false} : c == 1 ? TileCfg{4, 3, false, 0, false} : TileCfg{4, 4, true, 0, false})
+         : N == 2048  ? (c == 0 ? TileCfg{4, 1, false, 0, false} : c == 1 ? TileCfg{2, 3, false, 0, false} : TileCfg{2, 3, true, 0, false})
+                      : TileCfg{0, 0, false, 0, false};
 }
 
 // Threads of a phase-sum CTA and CTAs per instance of its launch.

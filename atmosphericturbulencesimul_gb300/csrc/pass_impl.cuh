@@ -74,6 +74,8 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src)
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+// every commit group but the most recent one has completed
+__device__ __forceinline__ void cp_async_wait_group1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Every thread polls the barrier with the same time limit; the CTA agrees
 // on the outcome through __syncthreads_or, so a timeout never splits it.
@@ -116,14 +118,20 @@ struct PassGeom {
     static constexpr size_t COLSUM_BYTES = size_t(NJ) * N * 8;        // epilogue column sums, [NJ][N]
     AW_HD static constexpr size_t round128(size_t b) { return (b + 127) / 128 * 128; }
     AW_HD static constexpr size_t mx(size_t a, size_t b) { return a > b ? a : b; }
-    // Layout: [exchange rows | window rows of the plane's first layer]; the
-    // epilogue's column sums reuse the window rows once the phasor is applied.
+    // Layout: [exchange rows | window rows of the plane's first layer |
+    // (staged transfer tables)]; the epilogue's column sums reuse the window
+    // rows once the phasor is applied.
+    static constexpr size_t HBYTES = size_t(2) * N * 8;  // the pass's two hop tables
     AW_HD static constexpr size_t win_offset() { return round128(XBYTES); }
-    AW_HD static constexpr size_t smem(int ops)
+    AW_HD static constexpr size_t h_offset(int ops)
     {
         const bool gather = (ops & (OP_GATHER | OP_EPI)) != 0, epi = (ops & OP_EPI) != 0;
         if (!gather) return round128(XBYTES);
-        return win_offset() + mx(WIN_BYTES, epi ? COLSUM_BYTES : 0);
+        return round128(win_offset() + mx(WIN_BYTES, epi ? COLSUM_BYTES : 0));
+    }
+    AW_HD static constexpr size_t smem(int ops, bool hs = false)
+    {
+        return h_offset(ops) + ((hs && (ops & (OP_PROP1 | OP_PROP2)) != 0) ? HBYTES : 0);
     }
     static_assert(N % (RR) == 0, "rows per CTA must divide N");
 };
@@ -265,7 +273,7 @@ __device__ __forceinline__ void fft_rt(float2* v, float2* xrow, int t, const flo
 
 // 1-D Fresnel propagation (forward FFT, transfer table, inverse FFT) with a
 // single copy of the transform code.
-template <int N, int T, int E, bool RT = false, int V = 0>
+template <int N, int T, int E, bool RT = false, int V = 0, bool HSM = false>
 __device__ __forceinline__ void prop_row_rt(float2* v, float2* xrow, int t, const float2* __restrict__ tw,
                                             const float2* __restrict__ h, const float2* twr = nullptr)
 {
@@ -278,7 +286,8 @@ __device__ __forceinline__ void prop_row_rt(float2* v, float2* xrow, int t, cons
         if (dir == 0) {
 #pragma unroll
             for (int s = 0; s < E; s++) {
-                const float2 a = v[s], b = __ldg(h + last_index<N, T, RL>(t, s));
+                const float2 a = v[s];
+                const float2 b = HSM ? h[last_index<N, T, RL>(t, s)] : __ldg(h + last_index<N, T, RL>(t, s));
                 v[s] = make_float2(a.x * b.x - a.y * b.y, -(a.x * b.y + a.y * b.x));
             }
         }
@@ -333,12 +342,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 // series passes (as opposed to the unit operators, which have no instance)
 #define I_SERIES(ops) (((ops) & (OP_GATHER | OP_EPI)) != 0)
 
-template <int N, int RR, int MINB, int OPS, bool ALIAS, bool HP = false, int V = 0>
+template <int N, int RR, int MINB, int OPS, bool ALIAS, bool HP = false, int V = 0, bool HS = false>
 __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
     k_pass(const __grid_constant__ PassArgs a, const __grid_constant__ TmaSet maps, const float2* __restrict__ tw)
 {
     using G = PassGeom<N, RR, V>;
     static_assert(!HP || V == 0, "FP16 transforms use the default plan");
+    static_assert(!HP || !HS, "FP16 transforms read their tables from global memory");
     constexpr int T = G::T, E = G::E, NT = G::NT, RS = G::RS;
     constexpr bool kEpi = (OPS & OP_EPI) != 0;
     constexpr bool kGather = (OPS & (OP_GATHER | OP_EPI)) != 0;
@@ -357,6 +367,22 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
 
     const int ltop = a.g_hi - 1;
     const int lbot = a.g_lo;
+    // HS: the transfer tables of this pass's hops are copied into shared
+    // memory (cp.async, their own commit group) while the field loads, and
+    // the transfer multiplies read them there
+    constexpr bool kHs = HS && I_SERIES(OPS) && (OPS & (OP_PROP1 | OP_PROP2)) != 0;
+    float2* hsm = reinterpret_cast<float2*>(sm + G::h_offset(OPS));
+    if constexpr (kHs) {
+#pragma unroll
+        for (int hp = 0; hp < 2; hp++) {
+            if (!(hp == 0 ? (OPS & OP_PROP1) != 0 : (OPS & OP_PROP2) != 0)) continue;
+            const float2* src = I->H + (size_t)(hp == 0 ? a.hop1 : a.hop2) * N;
+#pragma unroll 4
+            for (int k = tid; k < N / 2; k += NT) cp_async16(hsm + hp * N + 2 * k, src + 2 * k);
+        }
+        cp_async_commit();
+    }
+    const bool win_copy = kGather && ltop >= lbot;
     if constexpr (kGather) {
         // this CTA's rows of the window of the plane's first layer, copied
         // while the first propagation runs
@@ -429,14 +455,28 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
             const bool run = ph == 0 ? ((OPS & OP_PROP1) != 0) : ((OPS & OP_PROP2) != 0);
             if (!run) continue;
             const int hop = ph == 0 ? a.hop1 : a.hop2;
+            if constexpr (kHs) {
+                if (ph == 0 || (OPS & OP_PROP1) == 0) {
+                    // the tables' group is complete (the window copy may still run)
+                    if (win_copy && ph == 0) cp_async_wait_group1();
+                    else cp_async_wait_all();
+                    __syncthreads();
+                }
+            }
             if constexpr (HP) {
                 // FP16 transforms: tw is the FP16 twiddle table, Hh holds N H
                 prop_row_h<N, T, E>(v, xrow, t, reinterpret_cast<const __half2*>(tw),
                                     reinterpret_cast<const __half2*>(I->Hh) + (size_t)hop * N);
             } else {
-                const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
-                if constexpr (kRegTw) prop_row_rt<N, T, E, true, V>(v, xrow, t, tw, h, twr);
-                else prop_row_rt<N, T, E, false, V>(v, xrow, t, tw, h);
+                if constexpr (kHs) {
+                    const float2* h = hsm + (ph == 0 ? 0 : N);
+                    if constexpr (kRegTw) prop_row_rt<N, T, E, true, V, true>(v, xrow, t, tw, h, twr);
+                    else prop_row_rt<N, T, E, false, V, true>(v, xrow, t, tw, h);
+                } else {
+                    const float2* h = I ? I->H + (size_t)hop * N : (ph == 0 ? a.H1 : a.H2);
+                    if constexpr (kRegTw) prop_row_rt<N, T, E, true, V>(v, xrow, t, tw, h, twr);
+                    else prop_row_rt<N, T, E, false, V>(v, xrow, t, tw, h);
+                }
             }
         }
     }
@@ -502,50 +542,68 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
         }
         // [NJ][N]: per bin row, per column; clear of the staged rows in xb
         float2* colsum = reinterpret_cast<float2*>(wrows);
+        // One loop per output mode with a branch-free body: every pixel of the
+        // thread's columns is computed (rows and columns outside the crop read
+        // a valid staged value) and only the stores and bin sums are
+        // predicated, so the compiler can interleave the pixels.
+        bool rin[RR];
 #pragma unroll
-        for (int c = 0; c < CPT; c++) {
-            const int x = off + tid + c * NT;
-            if (x >= off + Nout) continue;
-            float2 acc0 = make_float2(0.0f, 0.0f), acc1 = acc0, acc2 = acc0;
+        for (int r = 0; r < RR; r++) rin[r] = y0 + r >= ya && y0 + r < yb;
+        if (mode == kModePhase) {
 #pragma unroll
-            for (int r = 0; r < RR; r++) {
-                const int y = y0 + r;
-                if (y < ya || y >= yb) continue;
-                const size_t o = (size_t)(y - off) * Nout + (x - off);
-                if (mode == kModePhase) {
+            for (int c = 0; c < CPT; c++) {
+                const int x = off + tid + c * NT;
+#pragma unroll
+                for (int r = 0; r < RR; r++) {
+                    if (!(rin[r] && x < off + Nout)) continue;
+                    const size_t o = (size_t)(y0 + r - off) * Nout + (x - off);
                     opha[o] = ps[r][c];
                     oamp[o] = 1.0f;
-                    continue;
                 }
-                const float2 u = xb[r * RS + padi(x)];
-                oamp[o] = sqrt_approx(fmaf(u.x, u.x, u.y * u.y));
-                const float pha = atan2_out(u.y, u.x);
-                if (mode == kModeRef) {
-                    opha[o] = add_2pi_multiple(pha, round_2pi(ps[r][c], 0.0f));
-                } else {
-                    opha[o] = pha;
+            }
+        } else {
+            const bool ref = mode == kModeRef;
+#pragma unroll
+            for (int c = 0; c < CPT; c++) {
+                const int x = off + tid + c * NT;
+                const bool xin = x < off + Nout;
+                const int xl = xin ? x : off;
+                float2 accr[RR];
+#pragma unroll
+                for (int r = 0; r < RR; r++) {
+                    const bool in = xin && rin[r];
+                    const size_t o = (size_t)(y0 + r - off) * Nout + (x - off);
+                    const float2 u = xb[r * RS + padi(xl)];
+                    const float amp = sqrt_approx(fmaf(u.x, u.x, u.y * u.y));
+                    const float pha = atan2_out(u.y, u.x);
+                    const float out = ref ? add_2pi_multiple(pha, round_2pi(ps[r][c], 0.0f)) : pha;
+                    if (in) {
+                        oamp[o] = amp;
+                        opha[o] = out;
+                    }
+                    accr[r] = make_float2(0.0f, 0.0f);
                     if (bins) {
                         float d, de;
                         two_sum(ps[r][c], -pha, d, de);
                         const float2 z = phasor(d + de);  // exp(i (sum - pha))
-                        const int j = jr[r];
-                        if (j == 0) {
-                            acc0.x += z.x;
-                            acc0.y += z.y;
-                        } else if (NJ == 2 || j == 1) {
-                            acc1.x += z.x;
-                            acc1.y += z.y;
-                        } else {
-                            acc2.x += z.x;
-                            acc2.y += z.y;
-                        }
+                        accr[r] = in ? z : make_float2(0.0f, 0.0f);
                     }
                 }
-            }
-            if (bins) {
-                colsum[x - off] = acc0;
-                colsum[N + x - off] = acc1;
-                if (NJ == 3) colsum[2 * N + x - off] = acc2;
+                if (bins && xin) {
+#pragma unroll
+                    for (int j = 0; j < NJ; j++) {
+                        float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+                        for (int r = 0; r < RR; r++) {
+                            const bool sel = NJ == 2 ? (j == 0) == (jr[r] == 0) : jr[r] == j;
+                            if (sel) {
+                                acc.x += accr[r].x;
+                                acc.y += accr[r].y;
+                            }
+                        }
+                        colsum[j * N + x - off] = acc;
+                    }
+                }
             }
         }
         if (bins) {
@@ -689,7 +747,7 @@ __global__ void __launch_bounds__(kPhasumThreads, 4) k_phasum(const __grid_const
 
 // host launcher for one (N, configuration); SO: the series passes only (the
 // unit operators, phase sums and windows launch in configuration 0)
-template <int N, int RR, int MINB, bool ALIAS, bool HP = false, int V = 0, bool SO = false>
+template <int N, int RR, int MINB, bool ALIAS, bool HP = false, int V = 0, bool SO = false, bool HS = false>
 cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* maps, const float2* tw, cudaStream_t st)
 {
     using G = PassGeom<N, RR, V>;
@@ -698,17 +756,17 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
     dim3 block(G::NT);
 #define AW_CASE(VAR)                                                                                   \
     case VAR: {                                                                                        \
-        constexpr size_t sm = G::smem(VAR);                                                            \
+        constexpr size_t sm = G::smem(VAR, HS);                                                        \
         static bool attr = false;                                                                      \
         if (!attr) {                                                                                   \
-            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS, HP, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
+            cudaError_t e = cudaFuncSetAttribute(k_pass<N, RR, MINB, VAR, ALIAS, HP, V, HS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm); \
             if (e != cudaSuccess) return e;                                                            \
             attr = true;                                                                               \
         }                                                                                              \
-        k_pass<N, RR, MINB, VAR, ALIAS, HP, V><<<grid, block, sm, st>>>(a, m, tw);                     \
+        k_pass<N, RR, MINB, VAR, ALIAS, HP, V, HS><<<grid, block, sm, st>>>(a, m, tw);                 \
         return cudaGetLastError();                                                                     \
     }
-    if constexpr (HP || V != 0 || SO) {
+    if constexpr (HP || V != 0 || SO || HS) {
         // FP16 transforms, the alternative radix plans and configurations
         // other than 0: the series passes only
         switch (var) {
@@ -768,8 +826,9 @@ cudaError_t launch_pass_nc(int cfg, int var, dim3 grid, const PassArgs& a, const
                            cudaStream_t st)
 {
     constexpr TileCfg c0 = tile_cfg(N, 0), c1 = tile_cfg(N, 1), c2 = tile_cfg(N, 2);
-    constexpr TileCfg c3 = tile_cfg(N, 3), c4 = tile_cfg(N, 4);
-    static_assert(kNumTileCfg == 5, "one branch per configuration");
+    constexpr TileCfg c3 = tile_cfg(N, 3), c4 = tile_cfg(N, 4), c5 = tile_cfg(N, 5);
+    static_assert(kNumTileCfg == 6, "one branch per configuration");
+    if constexpr (c5.rr > 0) if (cfg == 5) return launch_pass_t<N, c5.rr, c5.minb, c5.alias, false, c5.plan, true, c5.hsm>(var, grid, a, maps, tw, st);
     if constexpr (c3.rr > 0) if (cfg == 3) return launch_pass_t<N, c3.rr, c3.minb, c3.alias, false, c3.plan>(var, grid, a, maps, tw, st);
     if constexpr (c4.rr > 0) if (cfg == 4) return launch_pass_t<N, c4.rr, c4.minb, c4.alias, false, c4.plan>(var, grid, a, maps, tw, st);
     if (cfg >= 3) return cudaErrorInvalidValue;  // no such configuration at this size

@@ -181,12 +181,14 @@ atmwfs_status atmwfs_time_pass(atmwfs_ctx* ctx, int k, int c, int reps, double* 
                                int* count);
 int atmwfs_num_classes(const atmwfs_ctx* ctx);
 
-/* Pass configurations (radix plan x tile shape) the engine can compile per
- * grid size: 0-2 the default radix plan in three tile shapes, 3-4 the
- * size's alternative radix plan where it has one (1024: 16 x 8 x 8 against
- * the default 32 x 32).  The autotuner times every configuration compiled
- * for a grid class and keeps the fastest. */
-#define ATMWFS_NUM_TILE_CFG 5
+/* Pass configurations (radix plan x tile shape x table staging) the engine
+ * can compile per grid size: 0-2 the default radix plan in three tile
+ * shapes, 3-4 the size's alternative radix plan where it has one (1024:
+ * 16 x 8 x 8 against the default 32 x 32), 5 configuration 1 with the hop
+ * transfer tables staged in shared memory (512 and 1024).  The autotuner
+ * times every configuration compiled for a grid class and keeps the
+ * fastest. */
+#define ATMWFS_NUM_TILE_CFG 6
 
 /* Grid class ci (instances sharing wf_raw_size and wf_size): sizes, member
  * count, the rows per CTA the autotuner chose, and the mean time [ms] of the

@@ -101,28 +101,29 @@ def test_phase_sum_factored_and_per_instance_groups(lib, oracle64, monkeypatch):
     _report("factored and per-instance phase sums", ms)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4, 5])
 def test_w1024_every_tile_configuration(lib, oracle64, monkeypatch, cfg):
     """The 1024^2 passes (gather, both propagations, epilogue, science bins on
     51 x 51 bins) in each compiled configuration: the 32 x 32 radix plan in
-    three tile shapes (0-2) and the 16 x 8 x 8 plan in two (3, 4)."""
+    three tile shapes (0-2), the 16 x 8 x 8 plan in two (3, 4), and the
+    transfer tables staged in shared memory (5)."""
     monkeypatch.setenv("ATMWFS_TILE_CFG", str(cfg))
     case = bench_case(W=1024, Wout=1024, sci=[(0.5e-6, 0.0, 0.0), (1.6e-6, TEN, -TEN), (2.4e-6, -TEN, 0.0)])
     ms = compare(case, oracle64, 2)
     _report(f"W=1024 tile configuration {cfg}", ms)
 
 
-@pytest.mark.parametrize("cfg", [3, 4])
-def test_w1024_alternative_plan_grouped_layers(lib, oracle64, monkeypatch, cfg):
-    """The 16 x 8 x 8 plan on a plane of two layers (0 and 50 m share a
-    super-layer: the second layer's window rows come from global memory), a
-    crop and a lambda-ref instance."""
+@pytest.mark.parametrize("W,cfg", [(1024, 3), (1024, 4), (1024, 5), (512, 5)])
+def test_alternative_configurations_grouped_layers(lib, oracle64, monkeypatch, W, cfg):
+    """The 16 x 8 x 8 plan and the staged transfer tables on a plane of two
+    layers (0 and 50 m share a super-layer: the second layer's window rows
+    come from global memory), a crop and a lambda-ref instance."""
     monkeypatch.setenv("ATMWFS_TILE_CFG", str(cfg))
     case = Case(alt=[0.0, 50.0, 5000.0, 12000.0], cn2=[0.4, 0.2, 0.3, 0.1], speed=[8.0, 12.0, 25.0, 30.0],
-                direction=[0.1, 1.0, 3.0, 5.5], M=2048, W=1024, Wout=1000, fresnel_bin=100.0,
+                direction=[0.1, 1.0, 3.0, 5.5], M=2048, W=W, Wout=W - 24, fresnel_bin=100.0,
                 sci=[(1.25e-6, 0.0, 0.0), (2.2e-6, TEN, -TEN)])
     ms = compare(case, oracle64, 2)
-    _report(f"W=1024 configuration {cfg}, grouped layers", ms)
+    _report(f"W={W} configuration {cfg}, grouped layers", ms)
 
 
 def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
@@ -150,8 +151,9 @@ def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
     monkeypatch.delenv("ATMWFS_TILE_CFG", raising=False)
     info = classes()
     assert set(info) == {512, 1024}
-    assert all(t > 0 for t in info[1024]["tuned_ms"])          # five configurations timed at 1024
-    assert info[512]["tuned_ms"][3:] == [0.0, 0.0]             # no alternative plan at 512
+    assert all(t > 0 for t in info[1024]["tuned_ms"])          # six configurations timed at 1024
+    assert info[512]["tuned_ms"][3:5] == [0.0, 0.0]            # no alternative plan at 512
+    assert info[512]["tuned_ms"][5] > 0                        # staged tables at 512
     for n, ci in info.items():
         assert int(np.prod(ci["radices"])) == n
         timed = [t for t in ci["tuned_ms"] if t > 0]
