@@ -76,42 +76,50 @@ k_psf_rows(const float* __restrict__ amp, long amp_fstride, const float* __restr
     }
 }
 
-// Column pass over the B fields of G.  mode 0 (exposure): acc[kx][ky] +=
-// |F_b[ky][kx]|^2 for b = 0..B-1 in order, summed in registers from the
-// current value (the accumulator is kept transposed and uncentred so that
-// these updates are coalesced).  mode 1 (chromatic): I[b][kx][ky] =
-// |F_b[ky][kx]|^2.
+// Column pass over the B fields of G: one column per CTA, the fields spread
+// over F frame lanes of the CTA (lane f takes fields f, f + F, ...), so that
+// a batch of fields keeps F transforms of the column in flight per CTA (a
+// column per CTA with the fields in sequence left a 1024-column transform
+// with 1.7 CTAs of four warps per SM).  mode 0 (exposure): acc[kx][ky] +=
+// |F_b[ky][kx]|^2 for b = 0..B-1: each lane sums its fields in order, then
+// the lanes' partial sums are added to the accumulator in lane order (the
+// accumulator is kept transposed and uncentred so that these updates are
+// coalesced).  mode 1 (chromatic): I[b][kx][ky] = |F_b[ky][kx]|^2.
+template <int N> struct PsfLanes { static constexpr int F = Plan<N>::T >= 64 ? 2 : 4; };
+
 template <int N>
-__global__ void __launch_bounds__(Plan<N>::T * PsfRows<N>::RR)
+__global__ void __launch_bounds__(Plan<N>::T * PsfLanes<N>::F, 4)
 k_psf_cols(const float2* __restrict__ G, int B, int W, int off, int mode, float* __restrict__ out,
            const float2* __restrict__ tw)
 {
-    constexpr int RR = PsfRows<N>::RR, T = Plan<N>::T, E = Plan<N>::E, RS = row_stride<N>();
+    constexpr int F = PsfLanes<N>::F, T = Plan<N>::T, E = Plan<N>::E, RS = row_stride<N>();
     constexpr int RL = last_radix<N>();
-    __shared__ __align__(16) float2 xb[RR * RS];
-    const int tid = threadIdx.x, t = tid % T, rr = tid / T;
-    const int kx = blockIdx.x * RR + rr;
-    float2* xrow = xb + rr * RS;
+    static_assert(F * RS * 2 >= F * N, "the lane sums fit the exchange rows");
+    __shared__ __align__(16) float2 xb[F * RS];
+    const int tid = threadIdx.x, t = tid % T, f = tid / T;
+    const int kx = blockIdx.x;
+    float2* xrow = xb + f * RS;
     float s2[E];
-    if (mode == 0) {
 #pragma unroll
-        for (int s = 0; s < E; s++) s2[s] = out[(size_t)kx * N + last_index<N, T, RL>(t, s)];
-    }
+    for (int s = 0; s < E; s++) s2[s] = 0.0f;
+    // the same trip count in every lane (lanes may share a warp when T < 32)
 #pragma unroll 1
-    for (int b = 0; b < B; b++) {
-        const float2* src = G + (size_t)b * N * N + (size_t)kx * N;
+    for (int b0 = 0; b0 < B; b0 += F) {
+        const int b = b0 + f;
+        const bool have = b < B;
+        const float2* src = G + (size_t)(have ? b : 0) * N * N + (size_t)kx * N;
         float2 v[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const int yi = t + e * T - off;
-            v[e] = (yi >= 0 && yi < W) ? src[t + e * T] : make_float2(0.0f, 0.0f);
+            v[e] = (have && yi >= 0 && yi < W) ? src[t + e * T] : make_float2(0.0f, 0.0f);
         }
         fft_rt<N, T, E>(v, xrow, t, tw, -1.0f, 0);
         if (mode == 0) {
 #pragma unroll
             for (int s = 0; s < E; s++)
                 s2[s] = __fadd_rn(s2[s], __fadd_rn(__fmul_rn(v[s].x, v[s].x), __fmul_rn(v[s].y, v[s].y)));
-        } else {
+        } else if (have) {
             float* I = out + (size_t)b * N * N + (size_t)kx * N;
 #pragma unroll
             for (int s = 0; s < E; s++)
@@ -119,8 +127,17 @@ k_psf_cols(const float2* __restrict__ G, int B, int W, int off, int mode, float*
         }
     }
     if (mode == 0) {
+        __syncthreads();  // every lane's last transform is done with its exchange row
+        float* red = reinterpret_cast<float*>(xb);  // [F][N]
 #pragma unroll
-        for (int s = 0; s < E; s++) out[(size_t)kx * N + last_index<N, T, RL>(t, s)] = s2[s];
+        for (int s = 0; s < E; s++) red[f * N + last_index<N, T, RL>(t, s)] = s2[s];
+        __syncthreads();
+        for (int k = tid; k < N; k += T * F) {
+            float p = red[k];
+#pragma unroll
+            for (int g = 1; g < F; g++) p = __fadd_rn(p, red[g * N + k]);
+            out[(size_t)kx * N + k] = __fadd_rn(out[(size_t)kx * N + k], p);
+        }
     }
 }
 
@@ -193,8 +210,7 @@ template <int N>
 static cudaError_t psf_cols_n(const float2* G, int B, int W, int off, int mode, float* out, const float2* tw,
                               cudaStream_t st)
 {
-    constexpr int RR = PsfRows<N>::RR;
-    k_psf_cols<N><<<N / RR, Plan<N>::T * RR, 0, st>>>(G, B, W, off, mode, out, tw);
+    k_psf_cols<N><<<N, Plan<N>::T * PsfLanes<N>::F, 0, st>>>(G, B, W, off, mode, out, tw);
     return cudaGetLastError();
 }
 
