@@ -153,6 +153,7 @@ SIGNATURES = [
     ("atmwfs_num_classes", C.c_int, [_ctx]),
     ("atmwfs_class_info", C.c_int, [_ctx, C.c_int, _ip, _ip, _ip, _ip, _dp]),
     ("atmwfs_class_plan", C.c_int, [_ctx, C.c_int, _ip, _ip]),
+    ("atmwfs_step_kernels", C.c_int, [_ctx]),
     ("atmwfs_time_pass", C.c_int, [_ctx, C.c_int, C.c_int, C.c_int, _dp, _dp, _ip, _ip]),
     ("atmwfs_fresnel", C.c_int, [_fp, _fp, C.c_long, C.c_double, C.c_double, C.c_double]),
     ("atmwfs_fresnel_dev", C.c_int, [C.c_void_p, C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_double,

@@ -359,6 +359,7 @@ struct atmwfs_ctx {
     LayerPos* h_pos[2] = {nullptr, nullptr};
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaGraphExec_t gexec = nullptr;
+    int step_kernels = 0;                // kernel nodes of the captured step graph
     // graph branches: one stream per grid class, one for the phase sums
     std::vector<cudaStream_t> cls_st;
     cudaStream_t sum_st = nullptr;
@@ -488,6 +489,28 @@ atmwfs_status make_tma_map(CUtensorMap* m, float* base, int Wp, int Hp, int box_
 // the screen's own orientation.
 int pass_orient(int k, int Q) { return (Q - k) & 1; }
 
+// The window kernel over jobs [j0, j1) of class cl (the windows of the
+// groups whose side is cl's grid); optionally report its algorithmic bytes.
+atmwfs_status launch_windows(atmwfs_ctx* c, Class& cl, int j0, int j1, double* bytes, cudaStream_t st)
+{
+    if (bytes) *bytes = 0;
+    if (j1 <= j0) return ATMWFS_OK;
+    PassArgs a;
+    memset(&a, 0, sizeof a);
+    a.pos = c->d_pos;
+    a.d_step = c->d_step;
+    a.d_status = c->d_status;
+    a.L = c->L;
+    a.ninst_total = c->ninst;
+    a.poscap = c->poscap;
+    a.jobs = cl.d_jobs + j0;
+    const int RR0 = tile_cfg(cl.N, 0).rr;
+    // screen tiles in (RR0 + 3 rows of the padded width) and windows out
+    if (bytes) *bytes = (4.0 * (RR0 + 3) / RR0 + 4.0) * (double)cl.N * cl.N * (j1 - j0);
+    AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarWindows, dim3(cl.N / RR0, (unsigned)(j1 - j0)), a, &cl.maps[0], nullptr, st));
+    return ATMWFS_OK;
+}
+
 // Launch pass k (1-based) for grid class cl; optionally report the
 // algorithmic bytes of the launch.
 atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaStream_t st)
@@ -536,21 +559,7 @@ atmwfs_status launch_pass(atmwfs_ctx* c, int k, Class& cl, double* bytes, cudaSt
         // the step's windows of the groups this class computes
         if (bytes) *bytes = 0;
         if (cl.jobs.empty()) return ATMWFS_OK;
-        PassArgs a;
-        memset(&a, 0, sizeof a);
-        a.pos = c->d_pos;
-        a.d_step = c->d_step;
-        a.d_status = c->d_status;
-        a.L = c->L;
-        a.ninst_total = c->ninst;
-        a.poscap = c->poscap;
-        a.jobs = cl.d_jobs;
-        const int RR0 = tile_cfg(cl.N, 0).rr;
-        // screen tiles in (RR0 + 3 rows of the padded width) and windows out
-        if (bytes) *bytes = (4.0 * (RR0 + 3) / RR0 + 4.0) * (double)cl.N * cl.N * cl.jobs.size();
-        AW_CUDA(pass_launcher_cfg(cl.N)(0, kVarWindows, dim3(cl.N / RR0, (unsigned)cl.jobs.size()), a, &cl.maps[0],
-                                        nullptr, st));
-        return ATMWFS_OK;
+        return launch_windows(c, cl, 0, (int)cl.jobs.size(), bytes, st);
     }
     {
         {
@@ -617,7 +626,9 @@ atmwfs_status launch_step(atmwfs_ctx* c)
     const int nc = (int)c->classes.size();
     cudaEvent_t fork = c->gev[0], sums = c->gev[1];
     // the step's screen windows, read by the phase sums and by every pass
-    for (Class& cl : c->classes) AW_TRY(launch_pass(c, Q + 1, cl, nullptr, c->st));
+    // (launching those of the later passes beside the first pass measured no
+    // faster: the transforms keep every SM's registers busy)
+    for (Class& cl : c->classes) AW_TRY(launch_windows(c, cl, 0, (int)cl.jobs.size(), nullptr, c->st));
     AW_CUDA(cudaEventRecord(fork, c->st));
     AW_CUDA(cudaStreamWaitEvent(c->sum_st, fork, 0));
     for (Class& cl : c->classes) AW_TRY(launch_pass(c, 0, cl, nullptr, c->sum_st));
@@ -824,6 +835,18 @@ atmwfs_status commit(atmwfs_ctx* c)
         return s;
     }
     AW_CUDA(ec);
+    {
+        size_t nn = 0;
+        AW_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        AW_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+        c->step_kernels = 0;
+        for (cudaGraphNode_t nd : nodes) {
+            cudaGraphNodeType ty;
+            AW_CUDA(cudaGraphNodeGetType(nd, &ty));
+            c->step_kernels += ty == cudaGraphNodeTypeKernel;
+        }
+    }
     AW_CUDA(cudaGraphInstantiate(&c->gexec, g, 0));
     cudaGraphDestroy(g);
     c->committed = true;
@@ -1431,6 +1454,8 @@ atmwfs_status atmwfs_class_plan(const atmwfs_ctx* c, int ci, int* cfg, int* radi
 }
 
 void* atmwfs_stream(atmwfs_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+int atmwfs_step_kernels(const atmwfs_ctx* c) { return c ? c->step_kernels : 0; }
 
 int atmwfs_num_classes(const atmwfs_ctx* c) { return c ? (int)c->classes.size() : 0; }
 

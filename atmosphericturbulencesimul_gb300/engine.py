@@ -190,6 +190,10 @@ class Series:
     def stream(self) -> int:
         return int(self._lib.atmwfs_stream(self._ctx) or 0)
 
+    def step_kernels(self) -> int:
+        """Kernel launches per time step (nodes of the captured step graph)."""
+        return int(self._lib.atmwfs_step_kernels(self._ctx))
+
     def num_classes(self) -> int:
         return int(self._lib.atmwfs_num_classes(self._ctx))
 

@@ -721,8 +721,8 @@ def main():
             "algorithmic_bytes_per_launch": dom["bytes"] / dom["launches"],
             "ms_per_launch": round(dom["ms"] / dom["launches"], 4), "share_of_step": round(dom["ms"] / tot, 3),
             "peak_source": pk["source"]}
-    # per class: phase sum and passes; the window launches; unwrap, apply, step counter
-    launches = (npl + 1) * s.num_classes() + sum(1 for p in passes if p["k"] == npl + 1) + 3
+    # kernel nodes of the engine's captured step graph (windows, phase sums, passes, unwrap, apply, counter)
+    launches = s.step_kernels()
     cfg["tiles"] = {str(ci["n"]): {"cfg": ci["cfg"], "radices": ci["radices"], "rows_per_cta": ci["rows_per_cta"],
                                    "tuned_ms": [round(x, 4) for x in ci["tuned_ms"]]}
                     for ci in (s.class_info(c) for c in range(s.num_classes()))}

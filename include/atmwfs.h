@@ -197,6 +197,10 @@ int atmwfs_num_classes(const atmwfs_ctx* ctx);
 atmwfs_status atmwfs_class_info(const atmwfs_ctx* ctx, int ci, int* n, int* nout, int* count, int* rows_per_cta,
                                 double* tuned_ms);
 
+/* Kernel launches of one time step (the kernel nodes of the step's CUDA
+ * graph, captured at the first run; 0 before it). */
+int atmwfs_step_kernels(const atmwfs_ctx* ctx);
+
 /* The configuration the autotuner chose for grid class ci (0 ..
  * ATMWFS_NUM_TILE_CFG - 1, see above) and the radix sequence of its
  * forward transform (radices[0..2], 0 after the last stage). */

@@ -145,6 +145,10 @@ def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
             s.load_screen(l, sc)
         s.run_frames(1)
         info = {ci["n"]: ci for ci in (s.class_info(c) for c in range(s.num_classes()))}
+        # the step graph: the window kernel (one window group, side 1024), a
+        # phase sum per class (the layer-dependent Scoeff does not factor),
+        # 7 passes per class, unwrap, apply, step counter
+        assert s.step_kernels() == 1 + 2 + 2 * 7 + 3
         s.close()
         return info
 
