@@ -60,6 +60,9 @@ cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const void* X, 
                            float beta, const float* bias, void* act, int a_bf16, unsigned* status, int swap, bool write_c,
                            cudaStream_t st);
 unsigned* umma_status_ptr();
+bool spectral_umma_supported(int o, int c);
+cudaError_t spectral_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, long P, unsigned* status,
+                          int swap, cudaStream_t st);
 }  // namespace atmwfs
 
 struct atmwfs_fno {
@@ -71,8 +74,10 @@ struct atmwfs_fno {
     float* adam_m = nullptr;
     float* adam_v = nullptr;
     long step = 0;
-    // DFT matrices (FP32, rounded to BF16 by the products)
+    // DFT matrices (FP32, rounded to BF16 by the products), and BF16 copies
+    // of the y transforms for the tcgen05 spectral products
     float *Fx = nullptr, *FyAB = nullptr, *GyBig = nullptr, *Gx = nullptr;
+    __nv_bfloat16 *FyAB_bf = nullptr, *GyBig_bf = nullptr;
     // activations for one batch size
     int cap = 0;
     std::vector<float*> h, u, a, z;     // h[0..nl], u[0..nl-1], a/z per layer
@@ -84,6 +89,8 @@ struct atmwfs_fno {
 };
 
 namespace {
+
+bool umma_enabled();
 
 const double kPi = 3.14159265358979323846264338328;
 
@@ -439,6 +446,13 @@ atmwfs_status build_dft(atmwfs_fno* f)
         FN_TRY(dalloc(f, (void**)mm.d, mm.h->size() * sizeof(float)));
         FN_CUDA(cudaMemcpy(*mm.d, mm.h->data(), mm.h->size() * sizeof(float), cudaMemcpyHostToDevice));
     }
+    struct MB { __nv_bfloat16** d; std::vector<float>* h; } bmats[] = {{&f->FyAB_bf, &FyAB}, {&f->GyBig_bf, &GyBig}};
+    for (auto& mm : bmats) {
+        std::vector<__nv_bfloat16> hb(mm.h->size());
+        for (size_t i = 0; i < hb.size(); i++) hb[i] = __float2bfloat16_rn((*mm.h)[i]);
+        FN_TRY(dalloc(f, (void**)mm.d, hb.size() * sizeof(__nv_bfloat16)));
+        FN_CUDA(cudaMemcpy(*mm.d, hb.data(), hb.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
+    }
     return ATMWFS_OK;
 }
 
@@ -517,16 +531,24 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const void* h, int h_bf16, floa
         g.rdiv = G; g.c_lo = Nc; g.c_hi = m; g.cdiv = m; g.cc_hi = (long)G * Nc;
         FN_CUDA(gemm_args(g, 0.0f, st));
     }
-    // z = FyAB a: [2m, 2G] x [2G, Nc]
-    FN_CUDA(gemm(2 * m, (int)Nc, 2 * G, f->FyAB, 2 * G, 0, 0, a, Nc, 0, 0, z, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
+    // z = FyAB a: [2m, 2G] x [2G, Nc], on tcgen05 where compiled
+    const bool tc = umma_enabled() && Nc % 8 == 0;
+    if (tc && spectral_umma_supported(2 * m, 2 * G))
+        FN_CUDA(spectral_umma(f->FyAB_bf, 2 * m, 2 * G, a, z, Nc, umma_status_ptr(), 0, st));
+    else
+        FN_CUDA(gemm(2 * m, (int)Nc, 2 * G, f->FyAB, 2 * G, 0, 0, a, Nc, 0, 0, z, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
     // y = R z per mode
     const size_t smf = sizeof(float) * (2 * B * w + 2 * w * (w + 1));
     if (smf > 227 * 1024) return err(ATMWFS_ERR_INVALID, "batch %d x width %d exceeds the mode-mixing shared memory", B, w);
     if (smf > 48 * 1024) FN_CUDA(cudaFuncSetAttribute(k_modemix, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
     k_modemix<<<m * m, 256, smf, st>>>(f->pbf + f->L.R[l], z, f->y, B, w, m);
     FN_CUDA(cudaGetLastError());
-    // bb = GyBig y: [2G, 2m] x [2m, Nc]
-    FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->GyBig, 2 * m, 0, 0, f->y, Nc, 0, 0, f->bb, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0, st));
+    // bb = GyBig y: [2G, 2m] x [2m, Nc], on tcgen05 where compiled
+    if (tc && spectral_umma_supported(2 * G, 2 * m))
+        FN_CUDA(spectral_umma(f->GyBig_bf, 2 * G, 2 * m, f->y, f->bb, Nc, umma_status_ptr(), 0, st));
+    else
+        FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->GyBig, 2 * m, 0, 0, f->y, Nc, 0, 0, f->bb, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0,
+                     st));
     {   // spec[bo][y][x] = sum_{p,kx} bb[p][y][bo][kx] Gx[p m + kx][x]: rows (bo, y), A read through its maps
         GemmArgs g{};
         g.M = (int)(BW * G); g.N = G; g.K = 2 * m;

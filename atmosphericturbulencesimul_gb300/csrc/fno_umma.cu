@@ -330,7 +330,206 @@ cudaError_t launch_t(const __nv_bfloat16* W, const void* X, int x_bf16, float* C
     return launch<O, C, float, float>(W, (const float*)X, Cm, (float*)act, bias, beta, B, P, status, swap, write_c, st);
 }
 
+// ---------------------------------------------------------------------------
+// The spectral products of the Fourier layers along y, C (o x P) = W (o x c)
+// X (c x P), with a long K or a wide N: the forward DFT z = [FyA | FyB] a
+// (o = 2 modes, c = 2 grid) and its inverse bb = GyBig y (o = 2 grid,
+// c = 2 modes), P = samples x width x modes columns.  The same transposed
+// tile product as k_pointwise (128 columns of X per tile, one TMEM lane
+// each), with K taken in chunks of 64: each chunk's FP32 rows are staged by
+// cp.async while the previous chunk's MMAs run, rounded into the BF16 A tile
+// and accumulated into the same tensor-memory columns; N above 256 is split
+// over two MMAs per K step (tensor-memory columns 0.. and 256..).  The whole
+// W is staged once per CTA.  No bias or activation: C is written.
+// ---------------------------------------------------------------------------
+constexpr int kKch = 64;  // K per staged chunk
+
+// One chunk (kKch rows of 128 columns) of tile `tile` of X, rows [j kKch, ..).
+__device__ __forceinline__ void stage_chunk(float* stage, const float* X, long P, int tile, int j, int tid)
+{
+    const long p0 = (long)tile * kM;
+    const float* xs = X + (size_t)j * kKch * P + p0;
+    constexpr int CH = kM / 4;  // 16-byte chunks per row
+    for (int i = tid; i < kKch * CH; i += kThreads) {
+        const int k = i / CH, ch = i - k * CH;
+        float* dst = stage + k * kM + 4 * ch;
+        if (p0 + 4 * ch < P) cp_async16(dst, xs + (size_t)k * P + 4 * ch);
+        else *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    cp_async_commit();
+}
+
+template <int O, int C>
+__global__ void __launch_bounds__(kThreads, 1) k_chunked(const __nv_bfloat16* __restrict__ W, const float* __restrict__ X,
+                                                         float* __restrict__ Cm, long P, int ntiles, unsigned* status,
+                                                         int swap)
+{
+    constexpr int NKC = C / kKch;                    // K chunks
+    constexpr int KCB = C / 8, KCA = kKch / 8;       // core matrices along K in B / in one A chunk
+    constexpr int NMMA = O > 256 ? 2 : 1, NI = O / NMMA;
+    constexpr uint32_t STAGE_BYTES = kKch * kM * 4, A_BYTES = kM * kKch * 2;
+    constexpr uint32_t kCols = O <= 32 ? 32 : O <= 64 ? 64 : O <= 128 ? 128 : O <= 256 ? 256 : 512;
+    static_assert(C % kKch == 0, "K: whole chunks");
+    static_assert(O % 32 == 0 && O <= 512 && NI % 16 == 0 && NI <= 256, "N per MMA: 16..256");
+    extern __shared__ __align__(1024) unsigned char sm[];
+    float* stage = reinterpret_cast<float*>(sm);     // one chunk of the tile [kKch][128]
+    unsigned char* sa = sm + STAGE_BYTES;            // A chunk (BF16, K-major)
+    unsigned char* sb = sa + A_BYTES;                // W (BF16, K-major)
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (blockIdx.x < ntiles) stage_chunk(stage, X, P, blockIdx.x, 0, tid);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init(&bar);
+    for (int i = tid; i < O * C; i += kThreads) {
+        const int n = i / C, k = i - n * C;
+        *reinterpret_cast<__nv_bfloat16*>(sb + kmajor_off(n, k, KCB)) = W[i];
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t a_addr = smem_addr(sa), b_addr = smem_addr(sb);
+    uint32_t parity = 0;
+    bool failed = false;
+
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const long p0 = (long)tile * kM;
+        for (int j = 0; j < NKC; j++) {
+            cp_async_wait_all();
+            __syncthreads();  // every thread's copies of this chunk have landed
+            for (int i = tid; i < kM * KCA; i += kThreads) {
+                const int kc = i / kM, m = i - kc * kM;
+                const float* f = stage + kc * 8 * kM + m;
+                uint4 v;
+                __nv_bfloat162 h0 = __floats2bfloat162_rn(f[0], f[kM]);
+                __nv_bfloat162 h1 = __floats2bfloat162_rn(f[2 * kM], f[3 * kM]);
+                __nv_bfloat162 h2 = __floats2bfloat162_rn(f[4 * kM], f[5 * kM]);
+                __nv_bfloat162 h3 = __floats2bfloat162_rn(f[6 * kM], f[7 * kM]);
+                v.x = *reinterpret_cast<uint32_t*>(&h0);
+                v.y = *reinterpret_cast<uint32_t*>(&h1);
+                v.z = *reinterpret_cast<uint32_t*>(&h2);
+                v.w = *reinterpret_cast<uint32_t*>(&h3);
+                *reinterpret_cast<uint4*>(sa + kmajor_off(m, kc * 8, KCA)) = v;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            fence_before();
+            __syncthreads();
+            fence_after();
+            // the staging buffer is free: the next chunk (or the next tile's first) comes in
+            if (j + 1 < NKC) stage_chunk(stage, X, P, tile, j + 1, tid);
+            else if (tile + (int)gridDim.x < ntiles) stage_chunk(stage, X, P, tile + gridDim.x, 0, tid);
+            if (tid == 0) {
+                const uint32_t lbo = swap ? KCA * 128 : 128, sbo_a = swap ? 128 : KCA * 128;
+                const uint32_t lbo_b = swap ? KCB * 128 : 128, sbo_b = swap ? 128 : KCB * 128;
+#pragma unroll
+                for (int ks = 0; ks < kKch / 16; ks++) {
+                    const uint64_t da = smem_desc(a_addr + ks * 256, lbo, sbo_a);
+#pragma unroll
+                    for (int h = 0; h < NMMA; h++) {
+                        // B rows h NI.. (8-row groups KCB * 128 B apart), K core
+                        // matrices 8 j + 2 ks.. (128 B apart)
+                        const uint64_t db =
+                            smem_desc(b_addr + (uint32_t)(h * (NI / 8) * KCB * 128) + (uint32_t)((j * KCA + ks * 2) * 128),
+                                      lbo_b, sbo_b);
+                        const uint32_t acc = (j > 0 || ks > 0) ? 1u : 0u;
+                        asm volatile(
+                            "{\n\t.reg .pred p;\n\t"
+                            "setp.ne.b32 p, %4, 0;\n\t"
+                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                            ::"r"(tmem + (uint32_t)(h * NI)), "l"(da), "l"(db), "r"(instr_desc(NI)), "r"(acc)
+                            : "memory");
+                    }
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_addr(&bar))
+                             : "memory");
+            }
+            // the chunk's products complete before A is overwritten (bounded wait)
+            const uint64_t t0 = now_ns();
+            int timed_out = 0;
+            while (!mbar_try_wait(&bar, parity)) {
+                if (now_ns() - t0 > kWaitNs) {
+                    timed_out = 1;
+                    break;
+                }
+            }
+            if (__syncthreads_or(timed_out)) {
+                if (tid == 0 && status) atomicOr(status, 1u);
+                failed = true;
+                break;
+            }
+            parity ^= 1;
+            fence_after();
+        }
+        if (failed) break;
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. and the columns of half w / 4
+        const int g = warp & 3, half = warp >> 2;
+        const long p = p0 + g * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(g * 32) << 16);
+#pragma unroll 1
+        for (int c0 = half * (O / 2); c0 < (half + 1) * (O / 2); c0 += 16) {
+            float r[16];
+            tmem_ld16(trow + c0, r);
+            if (p < P) {
+#pragma unroll
+                for (int jj = 0; jj < 16; jj++) Cm[(size_t)(c0 + jj) * P + p] = r[jj];
+            }
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    }
+}
+
+template <int O, int C>
+cudaError_t launch_chunked(const __nv_bfloat16* W, const float* X, float* Cm, long P, unsigned* status, int swap,
+                           cudaStream_t st)
+{
+    if (P % 8 != 0) return cudaErrorNotSupported;
+    constexpr size_t smem = (size_t)kKch * kM * 4 + (size_t)kM * kKch * 2 + (size_t)O * C * 2;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_chunked<O, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const long tiles = (P + kM - 1) / kM;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // CTAs per SM: two by shared memory; one when a CTA holds all 512 TMEM columns
+    const long per = O > 256 ? 1 : 2;
+    const long grid = tiles < per * sms ? tiles : per * sms;
+    k_chunked<O, C><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, P, (int)tiles, status, swap);
+    return cudaGetLastError();
+}
+
 }  // namespace umma
+
+// The spectral products compiled for tcgen05 (grid 256, 32 modes):
+// o x c = 64 x 512 (the forward DFT along y) and 512 x 64 (its inverse).
+bool spectral_umma_supported(int o, int c) { return (o == 64 && c == 512) || (o == 512 && c == 64); }
+
+cudaError_t spectral_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, long P, unsigned* status,
+                          int swap, cudaStream_t st)
+{
+    if (o == 64 && c == 512) return umma::launch_chunked<64, 512>(W, X, C, P, status, swap, st);
+    if (o == 512 && c == 64) return umma::launch_chunked<512, 64>(W, X, C, P, status, swap, st);
+    return cudaErrorNotSupported;
+}
 
 // The shapes of the surrogate's pointwise products that run on tcgen05:
 // o x c in {64 x 64 (Fourier layers), 128 x 64 (projection 1)}.  Others
@@ -388,6 +587,32 @@ extern "C" atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, c
         return ATMWFS_ERR_CUDA;
     }
     const cudaError_t e = pointwise_umma(w, o, c, X, 0, C, batch, P, beta, bias, act, 0, status, engine == 2, true, st);
+    if (e != cudaSuccess) {
+        set_error_message(cudaGetErrorString(e));
+        return ATMWFS_ERR_CUDA;
+    }
+    return ATMWFS_OK;
+}
+
+extern "C" atmwfs_status atmwfs_fno_spectral_dev(const void* W, int o, int c, const float* X, float* C, long P,
+                                                 int engine, void* stream)
+{
+    using namespace atmwfs;
+    if (!W || !X || !C || o < 1 || c < 1 || P < 1 || engine < 1 || engine > 2) {
+        set_error_message("atmwfs_fno_spectral_dev: bad arguments");
+        return ATMWFS_ERR_INVALID;
+    }
+    if (!spectral_umma_supported(o, c) || P % 8 != 0) {
+        set_error_message("atmwfs_fno_spectral_dev: shape not compiled for the tcgen05 product");
+        return ATMWFS_ERR_INVALID;
+    }
+    unsigned* status = umma_status_ptr();
+    if (!status) {
+        set_error_message("atmwfs_fno_spectral_dev: status symbol");
+        return ATMWFS_ERR_CUDA;
+    }
+    const cudaError_t e = spectral_umma(reinterpret_cast<const __nv_bfloat16*>(W), o, c, X, C, P, status, engine == 2,
+                                        (cudaStream_t)stream);
     if (e != cudaSuccess) {
         set_error_message(cudaGetErrorString(e));
         return ATMWFS_ERR_CUDA;

@@ -91,6 +91,14 @@ atmwfs_status atmwfs_gemm_bf16(int M, int N, int K, const void* A, long lda, int
  * that only engine 1 matches the FP32 product). */
 atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, const float* X, float* C, int batch, long P,
                                        float beta, const float* bias, float* act, int engine, void* stream);
+/* The Fourier layers' spectral product along y on the tcgen05 tensor cores
+ * (no counterpart in the reference): C (o x P) = W (o x c, BF16) X (c x P,
+ * FP32, rounded to BF16), K taken in chunks of 64 accumulated in tensor
+ * memory; compiled for o x c = 64 x 512 (the forward DFT of a 256 grid with
+ * 32 modes) and 512 x 64 (its inverse); P a multiple of 8.  engine as for
+ * atmwfs_fno_pointwise_dev. */
+atmwfs_status atmwfs_fno_spectral_dev(const void* W, int o, int c, const float* X, float* C, long P, int engine,
+                                      void* stream);
 /* Status bits of the tcgen05 products since the last clear (1: a bounded
  * wait for the tensor cores ran out); clear != 0 resets them. */
 unsigned atmwfs_fno_umma_status(int clear);

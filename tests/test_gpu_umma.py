@@ -62,3 +62,32 @@ def test_tcgen05_pointwise_rejects_other_shapes(lib):
     Cm = torch.zeros((1, 2, 256), device="cuda")
     bias = torch.zeros((2,), device="cuda")
     assert _run(lib, W, X, Cm, None, bias, 0.0, 1) == 1
+
+
+@pytest.mark.parametrize("o,c,P", [(64, 512, 32768), (512, 64, 32768), (64, 512, 1000), (512, 64, 1000)])
+def test_tcgen05_spectral_product_matches_fp64(lib, o, c, P):
+    """The Fourier layers' product along y (K = 512 in eight staged chunks of
+    64 accumulated in tensor memory, or N = 512 as two MMAs of 256 per K
+    step): C = W X against an FP64 product of the same BF16-rounded operands.
+    Up to 512 exact BF16 products are summed in FP32, so the result matches
+    to 1e-5 of the largest |C|; exchanging the descriptors' core-matrix
+    strides (engine 2) must break it."""
+    from atmosphericturbulencesimul_gb300 import _lib
+    g = torch.Generator(device="cuda").manual_seed(o + c + P)
+    W = (torch.randn((o, c), device="cuda", generator=g) / 16).to(torch.bfloat16)
+    X = torch.randn((c, P), device="cuda", generator=g)
+    ref = W.double() @ X.to(torch.bfloat16).double()
+    scale = float(ref.abs().max())
+    lib.atmwfs_fno_umma_status(1)
+    errs = {}
+    for engine in (1, 2):
+        Cm = torch.full((o, P), float("nan"), device="cuda")
+        _lib.check(lib.atmwfs_fno_spectral_dev(C.c_void_p(W.data_ptr()), o, c, C.c_void_p(X.data_ptr()),
+                                               C.c_void_p(Cm.data_ptr()), P, engine,
+                                               C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        torch.cuda.synchronize()
+        errs[engine] = float((Cm.double() - ref).abs().nan_to_num(float("inf")).max()) / scale
+    print(f"\no={o} c={c} P={P}: relative error {errs[1]:.3g} (strides as laid out), {errs[2]:.3g} (exchanged)")
+    assert lib.atmwfs_fno_umma_status(1) == 0
+    assert errs[1] < 1e-5, errs
+    assert errs[2] > 1e-2, errs
