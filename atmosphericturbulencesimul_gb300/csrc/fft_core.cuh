@@ -205,21 +205,6 @@ AW_HD void stage_load(float2* v, const float2* buf, int t)
     }
 }
 
-template <int N, int T, int E, int R, int NS, int D>
-AW_HD void stage_twiddle(float2* v, int t, const float2* tw)
-{
-    if (NS == 1) return;
-    AW_UNROLL
-    for (int w = 0; w < E / R; w++) {
-        const int k = (t + T * w) % NS;
-        AW_UNROLL
-        for (int r = 1; r < R; r++) {
-            const float2 w0 = tw[k * r * (N / (NS * R))];
-            v[w * R + r] = D < 0 ? cmul(v[w * R + r], w0) : cmulc(v[w * R + r], w0);
-        }
-    }
-}
-
 template <int E, int R, int D>
 AW_HD void stage_dft(float2* v)
 {
@@ -309,24 +294,6 @@ template <> struct Plan<2048> { static constexpr int E = 32, T = 64; };
 template <> struct Plan<4096> { static constexpr int E = 16, T = 256; };
 template <> struct Plan<8192> { static constexpr int E = 32, T = 256; };
 template <> struct Plan<1024, 1> { static constexpr int E = 16, T = 64; };
-
-template <int... Rs> struct Radices {};
-
-template <int N> struct FwdRadices;
-template <> struct FwdRadices<64>   { using type = Radices<8, 8>; };
-template <> struct FwdRadices<128>  { using type = Radices<16, 8>; };
-template <> struct FwdRadices<256>  { using type = Radices<16, 16>; };
-template <> struct FwdRadices<512>  { using type = Radices<32, 16>; };
-template <> struct FwdRadices<1024> { using type = Radices<32, 32>; };
-template <> struct FwdRadices<2048> { using type = Radices<32, 8, 8>; };
-
-template <int N> struct InvRadices;
-template <> struct InvRadices<64>   { using type = Radices<8, 8>; };
-template <> struct InvRadices<128>  { using type = Radices<8, 16>; };
-template <> struct InvRadices<256>  { using type = Radices<16, 16>; };
-template <> struct InvRadices<512>  { using type = Radices<16, 32>; };
-template <> struct InvRadices<1024> { using type = Radices<32, 32>; };
-template <> struct InvRadices<2048> { using type = Radices<8, 8, 32>; };
 
 // Radix sequence of the forward transform as a runtime-indexable table; the
 // inverse of a propagation walks it backwards.
@@ -428,9 +395,5 @@ AW_HD void stage_exchange_load(float2* v, const float2* buf, int t, int r)
     if constexpr (has_radix<N, V>(16)) if (r == 16) { stage_load<N, T, E, 16>(v, buf, t); return; }
     if constexpr (has_radix<N, V>(8)) if (r == 8) { stage_load<N, T, E, 8>(v, buf, t); return; }
 }
-
-template <int R0, int... Rs> struct LastRadix { static constexpr int value = LastRadix<Rs...>::value; };
-template <int R0> struct LastRadix<R0> { static constexpr int value = R0; };
-template <int R0, int... Rs> struct FirstRadix { static constexpr int value = R0; };
 
 }  // namespace atmwfs
