@@ -220,6 +220,9 @@ SIGNATURES = [
                                            C.c_float, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     ("atmwfs_fno_spectral_dev", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_long, C.c_int,
                                           C.c_void_p]),
+    ("atmwfs_fno_xspectral_dev", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_long, C.c_long,
+                                           C.c_int, C.c_long, C.c_void_p, C.c_long, C.c_long, C.c_long, C.c_int,
+                                           C.c_long, C.c_long, C.c_int, C.c_void_p]),
     ("atmwfs_fno_umma_status", C.c_uint, [C.c_int]),
     ("atmwfs_gemm_bf16", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_int, C.c_int, C.c_void_p,
                                    C.c_long, C.c_int, C.c_int, C.c_void_p, C.c_long, C.c_float, C.c_float, C.c_void_p,

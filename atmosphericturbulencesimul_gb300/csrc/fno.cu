@@ -61,6 +61,10 @@ cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const void* X, 
                            cudaStream_t st);
 unsigned* umma_status_ptr();
 bool spectral_umma_supported(int o, int c);
+bool xspectral_umma_supported(int n, int k);
+cudaError_t xspectral_umma(const __nv_bfloat16* Bt, int n, int k, const float* A, long a_div, long a_lo, long a_hi,
+                           int a_kdiv, long a_khi, float* C, long c_div, long c_lo, long c_hi, int c_ndiv, long c_nhi,
+                           long M, unsigned* status, int swap, cudaStream_t st);
 cudaError_t spectral_umma(const __nv_bfloat16* W, int o, int c, const float* X, float* C, long P, unsigned* status,
                           int swap, cudaStream_t st);
 }  // namespace atmwfs
@@ -78,6 +82,7 @@ struct atmwfs_fno {
     // of the y transforms for the tcgen05 spectral products
     float *Fx = nullptr, *FyAB = nullptr, *GyBig = nullptr, *Gx = nullptr;
     __nv_bfloat16 *FyAB_bf = nullptr, *GyBig_bf = nullptr;
+    __nv_bfloat16 *FxT_bf = nullptr, *GxT_bf = nullptr;  // the x transforms transposed (N x K)
     // activations for one batch size
     int cap = 0;
     std::vector<float*> h, u, a, z;     // h[0..nl], u[0..nl-1], a/z per layer
@@ -446,7 +451,15 @@ atmwfs_status build_dft(atmwfs_fno* f)
         FN_TRY(dalloc(f, (void**)mm.d, mm.h->size() * sizeof(float)));
         FN_CUDA(cudaMemcpy(*mm.d, mm.h->data(), mm.h->size() * sizeof(float), cudaMemcpyHostToDevice));
     }
-    struct MB { __nv_bfloat16** d; std::vector<float>* h; } bmats[] = {{&f->FyAB_bf, &FyAB}, {&f->GyBig_bf, &GyBig}};
+    // transposes of the x transforms: FxT (2m x G) = Fx^T, GxT (G x 2m) = Gx^T
+    std::vector<float> FxT((size_t)2 * m * G), GxT((size_t)G * 2 * m);
+    for (int x = 0; x < G; x++)
+        for (int n = 0; n < 2 * m; n++) {
+            FxT[(size_t)n * G + x] = Fx[(size_t)x * 2 * m + n];
+            GxT[(size_t)x * 2 * m + n] = Gx[(size_t)n * G + x];
+        }
+    struct MB { __nv_bfloat16** d; std::vector<float>* h; } bmats[] = {
+        {&f->FyAB_bf, &FyAB}, {&f->GyBig_bf, &GyBig}, {&f->FxT_bf, &FxT}, {&f->GxT_bf, &GxT}};
     for (auto& mm : bmats) {
         std::vector<__nv_bfloat16> hb(mm.h->size());
         for (size_t i = 0; i < hb.size(); i++) hb[i] = __float2bfloat16_rn((*mm.h)[i]);
@@ -524,12 +537,19 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const void* h, int h_bf16, floa
     const long BW = (long)B * w, Nc = BW * m;
     float* a = f->a[l];
     float* z = f->z[l];
+    const bool tcx = umma_enabled() && xspectral_umma_supported(2 * m, G) && xspectral_umma_supported(G, 2 * m);
     {   // a[p][y][bc][kx] = sum_x h[bc][y][x] Fx[x][p m + kx]
-        GemmArgs g{};
-        g.M = (int)(BW * G); g.N = 2 * m; g.K = G;
-        g.A = h; g.a_bf16 = h_bf16; g.lda = G; g.B = f->Fx; g.ldb = 2 * m; g.C = a; g.ldc = 2 * m;
-        g.rdiv = G; g.c_lo = Nc; g.c_hi = m; g.cdiv = m; g.cc_hi = (long)G * Nc;
-        FN_CUDA(gemm_args(g, 0.0f, st));
+        if (tcx && !h_bf16 &&
+            xspectral_umma(f->FxT_bf, 2 * m, G, (const float*)h, 0, G, 0, G, 0, a, G, Nc, m, m, (long)G * Nc, BW * G,
+                           umma_status_ptr(), 0, st) == cudaSuccess) {
+        } else {
+            cudaGetLastError();
+            GemmArgs g{};
+            g.M = (int)(BW * G); g.N = 2 * m; g.K = G;
+            g.A = h; g.a_bf16 = h_bf16; g.lda = G; g.B = f->Fx; g.ldb = 2 * m; g.C = a; g.ldc = 2 * m;
+            g.rdiv = G; g.c_lo = Nc; g.c_hi = m; g.cdiv = m; g.cc_hi = (long)G * Nc;
+            FN_CUDA(gemm_args(g, 0.0f, st));
+        }
     }
     // z = FyAB a: [2m, 2G] x [2G, Nc], on tcgen05 where compiled
     const bool tc = umma_enabled() && Nc % 8 == 0;
@@ -550,11 +570,16 @@ atmwfs_status spectral_fwd(atmwfs_fno* f, int l, const void* h, int h_bf16, floa
         FN_CUDA(gemm(2 * G, (int)Nc, 2 * m, f->GyBig, 2 * m, 0, 0, f->y, Nc, 0, 0, f->bb, Nc, 0.0f, 1, 0, 0, 0, nullptr, 0,
                      st));
     {   // spec[bo][y][x] = sum_{p,kx} bb[p][y][bo][kx] Gx[p m + kx][x]: rows (bo, y), A read through its maps
-        GemmArgs g{};
-        g.M = (int)(BW * G); g.N = G; g.K = 2 * m;
-        g.A = f->bb; g.lda = m; g.ardiv = G; g.a_lo = Nc; g.a_hi = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
-        g.B = f->Gx; g.ldb = G; g.C = spec; g.ldc = G;
-        FN_CUDA(gemm_args(g, 0.0f, st));
+        if (tcx && xspectral_umma(f->GxT_bf, G, 2 * m, f->bb, G, Nc, m, m, (long)G * Nc, spec, 0, G, 0, G, 0, BW * G,
+                                  umma_status_ptr(), 0, st) == cudaSuccess) {
+        } else {
+            cudaGetLastError();
+            GemmArgs g{};
+            g.M = (int)(BW * G); g.N = G; g.K = 2 * m;
+            g.A = f->bb; g.lda = m; g.ardiv = G; g.a_lo = Nc; g.a_hi = m; g.kdiv = m; g.ka_hi = (long)G * Nc;
+            g.B = f->Gx; g.ldb = G; g.C = spec; g.ldc = G;
+            FN_CUDA(gemm_args(g, 0.0f, st));
+        }
     }
     return ATMWFS_OK;
 }

@@ -517,7 +517,222 @@ cudaError_t launch_chunked(const __nv_bfloat16* W, const float* X, float* Cm, lo
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// The spectral products along x, D = A B with the rows of A contiguous in K:
+// the forward DFT a = h Fx (rows: every (sample, channel, y) line of x
+// values, K = grid, N = 2 modes) and its inverse spec = bb Gx (K = 2 modes,
+// N = grid).  The planar spectra are read and written through the index
+// maps of the mma.sync product: row m of A at (m % a_div) a_lo + (m / a_div)
+// a_hi (a_div = 0: m a_lo) and K index k at (k / a_kdiv) a_khi + k % a_kdiv;
+// row m of C at (m % c_div) c_lo + (m / c_div) c_hi, column n at (n / c_ndiv)
+// c_nhi + n % c_ndiv.  A tile is 128 rows (one TMEM lane each); each row's
+// K chunk of 64 FP32 values is staged by cp.async (16-byte pieces: a_kdiv a
+// multiple of 4), rounded into the BF16 K-major A tile and accumulated in
+// tensor memory; B (N x K, BF16, K-major: the transposed DFT matrix) is
+// staged once per CTA.  The epilogue writes 16 consecutive columns of a row
+// per 16-byte-vector group (c_ndiv a multiple of 16).
+// ---------------------------------------------------------------------------
+struct RowMaps {
+    const float* A;
+    long a_div, a_lo, a_hi;
+    int a_kdiv;
+    long a_khi;
+    float* C;
+    long c_div, c_lo, c_hi;
+    int c_ndiv;
+    long c_nhi;
+    long M;
+};
+
+__device__ __forceinline__ long row_off(long m, long div, long lo, long hi)
+{
+    return div ? (m % div) * lo + (m / div) * hi : m * lo;
+}
+
+template <int K>
+__device__ __forceinline__ void stage_rows(float* stage, const RowMaps& g, long m0, int j, int tid)
+{
+    constexpr int PIECES = kKch / 4;  // 16-byte pieces per row of a chunk
+    for (int i = tid; i < kM * PIECES; i += kThreads) {
+        const int r = i / PIECES, q = i - r * PIECES;
+        float* dst = stage + r * kKch + 4 * q;  // [128][64]
+        const long m = m0 + r;
+        if (m < g.M) {
+            const int k = j * kKch + 4 * q;
+            const long ko = (long)(k / g.a_kdiv) * g.a_khi + k % g.a_kdiv;
+            cp_async16(dst, g.A + row_off(m, g.a_div, g.a_lo, g.a_hi) + ko);
+        } else {
+            *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    cp_async_commit();
+}
+
+template <int N, int K>
+__global__ void __launch_bounds__(kThreads, 1) k_rowprod(const __nv_bfloat16* __restrict__ Bt, const RowMaps g,
+                                                         int ntiles, unsigned* status, int swap)
+{
+    constexpr int NKC = K / kKch;
+    constexpr int KCB = K / 8, KCA = kKch / 8;
+    constexpr uint32_t STAGE_BYTES = kM * kKch * 4, A_BYTES = kM * kKch * 2;
+    constexpr uint32_t kCols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
+    static_assert(K % kKch == 0 && N % 32 == 0 && N <= 256, "K in chunks of 64, N per MMA 32..256");
+    extern __shared__ __align__(1024) unsigned char sm[];
+    float* stage = reinterpret_cast<float*>(sm);   // [128][64] FP32
+    unsigned char* sa = sm + STAGE_BYTES;
+    unsigned char* sb = sa + A_BYTES;
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_base;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (blockIdx.x < ntiles) stage_rows<K>(stage, g, (long)blockIdx.x * kM, 0, tid);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init(&bar);
+    for (int i = tid; i < N * K; i += kThreads) {
+        const int n = i / K, k = i - n * K;
+        *reinterpret_cast<__nv_bfloat16*>(sb + kmajor_off(n, k, KCB)) = Bt[i];
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_base;
+    const uint32_t a_addr = smem_addr(sa), b_addr = smem_addr(sb);
+    uint32_t parity = 0;
+    bool failed = false;
+
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const long m0 = (long)tile * kM;
+        for (int j = 0; j < NKC; j++) {
+            cp_async_wait_all();
+            __syncthreads();
+            // A: 8 consecutive K values of one row per 16-byte store
+            for (int i = tid; i < kM * KCA; i += kThreads) {
+                const int r = i / KCA, kc = i - r * KCA;
+                const float4 f0 = *reinterpret_cast<const float4*>(stage + r * kKch + kc * 8);
+                const float4 f1 = *reinterpret_cast<const float4*>(stage + r * kKch + kc * 8 + 4);
+                uint4 v;
+                __nv_bfloat162 h0 = __floats2bfloat162_rn(f0.x, f0.y);
+                __nv_bfloat162 h1 = __floats2bfloat162_rn(f0.z, f0.w);
+                __nv_bfloat162 h2 = __floats2bfloat162_rn(f1.x, f1.y);
+                __nv_bfloat162 h3 = __floats2bfloat162_rn(f1.z, f1.w);
+                v.x = *reinterpret_cast<uint32_t*>(&h0);
+                v.y = *reinterpret_cast<uint32_t*>(&h1);
+                v.z = *reinterpret_cast<uint32_t*>(&h2);
+                v.w = *reinterpret_cast<uint32_t*>(&h3);
+                *reinterpret_cast<uint4*>(sa + kmajor_off(r, kc * 8, KCA)) = v;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            fence_before();
+            __syncthreads();
+            fence_after();
+            if (j + 1 < NKC) stage_rows<K>(stage, g, m0, j + 1, tid);
+            else if (tile + (int)gridDim.x < ntiles) stage_rows<K>(stage, g, (long)(tile + gridDim.x) * kM, 0, tid);
+            if (tid == 0) {
+                const uint32_t lbo = swap ? KCA * 128 : 128, sbo_a = swap ? 128 : KCA * 128;
+                const uint32_t lbo_b = swap ? KCB * 128 : 128, sbo_b = swap ? 128 : KCB * 128;
+#pragma unroll
+                for (int ks = 0; ks < kKch / 16; ks++) {
+                    const uint64_t da = smem_desc(a_addr + ks * 256, lbo, sbo_a);
+                    const uint64_t db = smem_desc(b_addr + (uint32_t)((j * KCA + ks * 2) * 128), lbo_b, sbo_b);
+                    const uint32_t acc = (j > 0 || ks > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\t"
+                        "setp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                        ::"r"(tmem), "l"(da), "l"(db), "r"(instr_desc(N)), "r"(acc)
+                        : "memory");
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 smem_addr(&bar))
+                             : "memory");
+            }
+            const uint64_t t0 = now_ns();
+            int timed_out = 0;
+            while (!mbar_try_wait(&bar, parity)) {
+                if (now_ns() - t0 > kWaitNs) {
+                    timed_out = 1;
+                    break;
+                }
+            }
+            if (__syncthreads_or(timed_out)) {
+                if (tid == 0 && status) atomicOr(status, 1u);
+                failed = true;
+                break;
+            }
+            parity ^= 1;
+            fence_after();
+        }
+        if (failed) break;
+        // epilogue: warp w reads TMEM lanes 32 (w % 4) .. (its 32 rows) and the
+        // columns of half w / 4; each lane writes 16 consecutive columns of its row
+        const int gq = warp & 3, half = warp >> 2;
+        const long m = m0 + gq * 32 + lane;
+        const uint32_t trow = tmem + ((uint32_t)(gq * 32) << 16);
+        float* crow = m < g.M ? g.C + row_off(m, g.c_div, g.c_lo, g.c_hi) : nullptr;
+#pragma unroll 1
+        for (int c0 = half * (N / 2); c0 < (half + 1) * (N / 2); c0 += 16) {
+            float r[16];
+            tmem_ld16(trow + c0, r);
+            if (crow) {
+                float4* o = reinterpret_cast<float4*>(crow + (long)(c0 / g.c_ndiv) * g.c_nhi + c0 % g.c_ndiv);
+#pragma unroll
+                for (int q = 0; q < 4; q++) o[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+            }
+        }
+        fence_before();
+        __syncthreads();
+        fence_after();
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    }
+}
+
+template <int N, int K>
+cudaError_t launch_rowprod(const __nv_bfloat16* Bt, const RowMaps& g, unsigned* status, int swap, cudaStream_t st)
+{
+    if (g.a_kdiv % 4 || g.c_ndiv % 16 || g.a_lo % 4 || g.a_hi % 4 || g.a_khi % 4 || g.c_lo % 4 || g.c_hi % 4 ||
+        g.c_nhi % 4 || (reinterpret_cast<uintptr_t>(g.A) & 15) || (reinterpret_cast<uintptr_t>(g.C) & 15))
+        return cudaErrorNotSupported;  // 16-byte pieces of A rows and C rows
+    constexpr size_t smem = (size_t)kM * kKch * 4 + (size_t)kM * kKch * 2 + (size_t)N * K * 2;
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_rowprod<N, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const long tiles = (g.M + kM - 1) / kM;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long grid = tiles < 2L * sms ? tiles : 2L * sms;
+    k_rowprod<N, K><<<(unsigned)grid, kThreads, smem, st>>>(Bt, g, (int)tiles, status, swap);
+    return cudaGetLastError();
+}
+
 }  // namespace umma
+
+// The spectral products along x compiled for tcgen05 (grid 256, 32 modes):
+// N x K = 64 x 256 (the forward DFT) and 256 x 64 (its inverse).
+bool xspectral_umma_supported(int n, int k) { return (n == 64 && k == 256) || (n == 256 && k == 64); }
+
+cudaError_t xspectral_umma(const __nv_bfloat16* Bt, int n, int k, const float* A, long a_div, long a_lo, long a_hi,
+                           int a_kdiv, long a_khi, float* C, long c_div, long c_lo, long c_hi, int c_ndiv, long c_nhi,
+                           long M, unsigned* status, int swap, cudaStream_t st)
+{
+    const umma::RowMaps g{A, a_div, a_lo, a_hi, a_kdiv, a_khi, C, c_div, c_lo, c_hi, c_ndiv, c_nhi, M};
+    if (n == 64 && k == 256) return umma::launch_rowprod<64, 256>(Bt, g, status, swap, st);
+    if (n == 256 && k == 64) return umma::launch_rowprod<256, 64>(Bt, g, status, swap, st);
+    return cudaErrorNotSupported;
+}
 
 // The spectral products compiled for tcgen05 (grid 256, 32 modes):
 // o x c = 64 x 512 (the forward DFT along y) and 512 x 64 (its inverse).
@@ -616,6 +831,35 @@ extern "C" atmwfs_status atmwfs_fno_spectral_dev(const void* W, int o, int c, co
     if (e != cudaSuccess) {
         set_error_message(cudaGetErrorString(e));
         return ATMWFS_ERR_CUDA;
+    }
+    return ATMWFS_OK;
+}
+
+extern "C" atmwfs_status atmwfs_fno_xspectral_dev(const void* Bt, int n, int k, const float* A, long a_div, long a_lo,
+                                                  long a_hi, int a_kdiv, long a_khi, float* C, long c_div, long c_lo,
+                                                  long c_hi, int c_ndiv, long c_nhi, long M, int engine, void* stream)
+{
+    using namespace atmwfs;
+    if (!Bt || !A || !C || M < 1 || a_kdiv < 1 || c_ndiv < 1 || engine < 1 || engine > 2) {
+        set_error_message("atmwfs_fno_xspectral_dev: bad arguments");
+        return ATMWFS_ERR_INVALID;
+    }
+    if (!xspectral_umma_supported(n, k)) {
+        set_error_message("atmwfs_fno_xspectral_dev: shape not compiled for the tcgen05 product");
+        return ATMWFS_ERR_INVALID;
+    }
+    unsigned* status = umma_status_ptr();
+    if (!status) {
+        set_error_message("atmwfs_fno_xspectral_dev: status symbol");
+        return ATMWFS_ERR_CUDA;
+    }
+    const cudaError_t e = xspectral_umma(reinterpret_cast<const __nv_bfloat16*>(Bt), n, k, A, a_div, a_lo, a_hi, a_kdiv,
+                                         a_khi, C, c_div, c_lo, c_hi, c_ndiv, c_nhi, M, status, engine == 2,
+                                         (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        set_error_message(e == cudaErrorNotSupported ? "atmwfs_fno_xspectral_dev: maps break 16-byte pieces"
+                                                     : cudaGetErrorString(e));
+        return e == cudaErrorNotSupported ? ATMWFS_ERR_INVALID : ATMWFS_ERR_CUDA;
     }
     return ATMWFS_OK;
 }

@@ -99,6 +99,19 @@ atmwfs_status atmwfs_fno_pointwise_dev(const void* W, int o, int c, const float*
  * atmwfs_fno_pointwise_dev. */
 atmwfs_status atmwfs_fno_spectral_dev(const void* W, int o, int c, const float* X, float* C, long P, int engine,
                                       void* stream);
+/* The Fourier layers' spectral products along x on the tcgen05 tensor cores
+ * (no counterpart in the reference): C = A Bt^T with A (M x k, FP32, rounded
+ * to BF16) and Bt (n x k, BF16, the transposed DFT matrix), K taken in
+ * chunks of 64.  Row m of A starts at (m % a_div) a_lo + (m / a_div) a_hi
+ * (a_div = 0: m a_lo) and its column j at (j / a_kdiv) a_khi + j % a_kdiv;
+ * row m of C at (m % c_div) c_lo + (m / c_div) c_hi, column j at
+ * (j / c_ndiv) c_nhi + j % c_ndiv (the planar spectrum layouts of the
+ * network).  Compiled for n x k = 64 x 256 (forward DFT of a 256 grid with 32
+ * modes) and 256 x 64 (its inverse); a_kdiv and the strides multiples of 4,
+ * c_ndiv of 16.  engine as for atmwfs_fno_pointwise_dev. */
+atmwfs_status atmwfs_fno_xspectral_dev(const void* Bt, int n, int k, const float* A, long a_div, long a_lo, long a_hi,
+                                       int a_kdiv, long a_khi, float* C, long c_div, long c_lo, long c_hi, int c_ndiv,
+                                       long c_nhi, long M, int engine, void* stream);
 /* Status bits of the tcgen05 products since the last clear (1: a bounded
  * wait for the tensor cores ran out); clear != 0 resets them. */
 unsigned atmwfs_fno_umma_status(int clear);

@@ -91,3 +91,56 @@ def test_tcgen05_spectral_product_matches_fp64(lib, o, c, P):
     assert lib.atmwfs_fno_umma_status(1) == 0
     assert errs[1] < 1e-5, errs
     assert errs[2] > 1e-2, errs
+
+
+def _xspec(lib, Bt, A, maps, Cm, M, engine):
+    n, k = Bt.shape
+    return lib.atmwfs_fno_xspectral_dev(C.c_void_p(Bt.data_ptr()), n, k, C.c_void_p(A.data_ptr()), *maps[:5],
+                                        C.c_void_p(Cm.data_ptr()), *maps[5:], M, engine,
+                                        C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
+@pytest.mark.parametrize("direction", ["forward", "inverse"])
+def test_tcgen05_x_spectral_products_match_fp64(lib, direction):
+    """The Fourier layers' products along x through the network's planar
+    layouts: the forward DFT reads lines of x values (K = 256 in four staged
+    chunks) and writes the planar spectrum [2][G][B w][m]; the inverse reads
+    that layout (two 32-value runs per row) and writes lines of 256 values.
+    Against an FP64 product of the same BF16-rounded operands on the same
+    index maps (1e-5 of the largest |C|); exchanged descriptor strides must
+    break it."""
+    from atmosphericturbulencesimul_gb300 import _lib
+    G, m, BW = 256, 32, 6           # grid, modes, samples x width
+    Nc = BW * m
+    M = BW * G
+    g = torch.Generator(device="cuda").manual_seed(11 if direction == "forward" else 12)
+    if direction == "forward":
+        n, k = 2 * m, G
+        A = torch.randn((BW, G, G), device="cuda", generator=g)          # h[bc][y][x]
+        Ad = A.reshape(M, G)
+        maps = (0, G, 0, G, 0, G, Nc, m, m, G * Nc)
+        Cm = torch.full((2, G, BW, m), float("nan"), device="cuda")      # a[p][y][bc][kx]
+    else:
+        n, k = G, 2 * m
+        A = torch.randn((2, G, BW, m), device="cuda", generator=g)       # bb[p][y][bo][kx]
+        Ad = A.permute(2, 1, 0, 3).reshape(M, 2 * m)                     # rows (bo, y), K (p, kx)
+        maps = (G, Nc, m, m, G * Nc, 0, G, 0, G, 0)
+        Cm = torch.full((BW, G, G), float("nan"), device="cuda")         # spec[bo][y][x]
+    Bt = (torch.randn((n, k), device="cuda", generator=g) / 16).to(torch.bfloat16)
+    ref = Ad.to(torch.bfloat16).double() @ Bt.double().t()              # (M, n)
+    if direction == "forward":
+        ref = ref.reshape(BW, G, 2, m).permute(2, 1, 0, 3)               # -> [p][y][bc][kx]
+    else:
+        ref = ref.reshape(BW, G, G)
+    scale = float(ref.abs().max())
+    lib.atmwfs_fno_umma_status(1)
+    errs = {}
+    for engine in (1, 2):
+        Cm.fill_(float("nan"))
+        _lib.check(_xspec(lib, Bt, A, maps, Cm, M, engine))
+        torch.cuda.synchronize()
+        errs[engine] = float((Cm.double() - ref).abs().nan_to_num(float("inf")).max()) / scale
+    print(f"\nx {direction}: relative error {errs[1]:.3g} (strides as laid out), {errs[2]:.3g} (exchanged)")
+    assert lib.atmwfs_fno_umma_status(1) == 0
+    assert errs[1] < 1e-5, errs
+    assert errs[2] > 1e-2, errs
