@@ -721,6 +721,17 @@ def main():
             "algorithmic_bytes_per_launch": dom["bytes"] / dom["launches"],
             "ms_per_launch": round(dom["ms"] / dom["launches"], 4), "share_of_step": round(dom["ms"] / tot, 3),
             "peak_source": pk["source"]}
+    # the whole step against the path's per-frame byte model W^2 (4 L + 4 e P + 8) (layer windows read once,
+    # two field round trips per hop, outputs written once; e = 8 B per complex element), summed over the
+    # step's instances; this engine does one field round trip per hop, so the model overstates its bytes
+    hops = num_hops(wl)
+    e_el = 4 if args.fft_fp16 else 8
+    model_step = sum(float(I["W"]) ** 2 * (4 * L + 4 * e_el * hops + 8) for I in wl["inst"])
+    ms_step = 1e3 * t / args.steps
+    roof["path_model"] = {"bytes_per_step": model_step, "ms_per_step": round(ms_step, 4),
+                          "achieved": round(model_step / (ms_step * 1e-3) / 1e9, 1),
+                          "frac": round(model_step / (ms_step * 1e-3) / 1e9 / pk["hbm_gbs"], 4),
+                          "bytes_per_frame_1024": 1024.0 ** 2 * (4 * L + 4 * e_el * hops + 8)}
     # kernel nodes of the engine's captured step graph (windows, phase sums, passes, unwrap, apply, counter)
     launches = s.step_kernels()
     cfg["tiles"] = {str(ci["n"]): {"cfg": ci["cfg"], "radices": ci["radices"], "rows_per_cta": ci["rows_per_cta"],
