@@ -878,8 +878,6 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
     if (!pow2_in(p->master_size, 64, 1 << 16)) return fail(ATMWFS_ERR_INVALID, "master_size must be a power of two >= 64");
     if (p->ninst < 1 || !p->inst) return fail(ATMWFS_ERR_INVALID, "no instances");
     if (!(p->pupil_scale > 0)) return fail(ATMWFS_ERR_INVALID, "pupil_scale must be > 0");
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(ATMWFS_ERR_NODEVICE, "no CUDA device");
     for (int i = 0; i < p->ninst; i++) {
         const atmwfs_instance& I = p->inst[i];
         if (!pow2_in(I.wf_raw_size, 64, 2048)) return fail(ATMWFS_ERR_INVALID, "instance %d: wf_raw_size must be a power of two in 64..2048", i);
@@ -887,6 +885,9 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
         if (I.mode < 0 || I.mode > 2) return fail(ATMWFS_ERR_INVALID, "instance %d: bad mode", i);
         if (!(I.lambda > 0)) return fail(ATMWFS_ERR_INVALID, "instance %d: lambda must be > 0", i);
     }
+    // the arguments are checked before any CUDA call
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(ATMWFS_ERR_NODEVICE, "no CUDA device");
     atmwfs_ctx* c = new atmwfs_ctx();
     c->L = p->nlayers;
     c->ninst = p->ninst;

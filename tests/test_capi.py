@@ -80,3 +80,35 @@ def test_errors_are_status_codes(lib):
     ctx = C.c_void_p()
     assert lib.atmwfs_create(C.byref(p), C.byref(ctx)) == 1
     assert lib.atmwfs_layer_planes(None, None, 0, 0.0, 1, 1, 0.0, None, None, None, None, None, None, None) == 1
+
+
+@pytest.mark.parametrize("field,value,words", [
+    ("wf_raw_size", 100, "power of two"),      # not a power of two
+    ("wf_raw_size", 4096, "power of two"),     # above the largest propagation grid
+    ("wf_size", 300, "wf_size"),               # crop larger than the grid
+    ("wf_size", 0, "wf_size"),                 # empty crop
+    ("mode", 3, "mode"),
+    ("lambda_", 0.0, "lambda"),
+])
+def test_bad_instances_are_rejected_before_device_work(lib, field, value, words):
+    """Instance geometry the engine cannot run is refused with
+    ATMWFS_ERR_INVALID and a message (the reference would index out of its
+    arrays or exit), before any CUDA call: this runs without a GPU."""
+    from atmosphericturbulencesimul_gb300 import _lib
+    alt = (C.c_double * 2)(0.0, 5000.0)
+    cn2 = (C.c_double * 2)(0.5, 0.5)
+    spd = (C.c_double * 2)(10.0, 20.0)
+    drc = (C.c_double * 2)(0.1, 1.0)
+    inst = (_lib.Instance * 1)()
+    inst[0].lambda_ = 1.6e-6
+    inst[0].mode = 1
+    inst[0].wf_raw_size = 256
+    inst[0].wf_size = 256
+    setattr(inst[0], field, value)
+    p = _lib.Params()
+    p.nlayers, p.alt, p.cn2, p.speed, p.dir = 2, alt, cn2, spd, drc
+    p.fresnel_bin, p.pupil_scale, p.time_step, p.master_size = 100.0, 0.01, 0.001, 512
+    p.amplitude, p.fresnel, p.ninst, p.inst, p.ring = 1, 1, 1, inst, 1
+    ctx = C.c_void_p()
+    assert lib.atmwfs_create(C.byref(p), C.byref(ctx)) == 1
+    assert words in lib.atmwfs_last_error().decode()

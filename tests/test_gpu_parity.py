@@ -151,3 +151,37 @@ def test_normalize_matches_oracle(lib, oracle32):
                              np.array([0.7, 0.3]), np.float32(0.0))
     assert np.allclose(r0g, r0o, rtol=1e-6)
     s.close()
+
+
+def test_series_odd_crops(lib, oracle64):
+    """Crops that break the 16-byte vectors (129 of 256, 257 of 512, 75 of 128):
+    the phase sum, the epilogue and the science apply take their one-column
+    paths; science bins of 21-22 pixels (nb = Wout / 20 rounded down)."""
+    case = Case(alt=[0.0, 3000.0, 9000.0], cn2=[0.5, 0.3, 0.2], speed=[9.0, 17.0, 26.0], direction=[0.4, 2.1, 4.0],
+                M=512, W=256, Wout=129, fresnel_bin=100.0,
+                sci=[(1.25e-6, 0.0, 0.0), (2.2e-6, 4.85e-5, 0.0, 512, 257), (0.7e-6, 0.0, 4.85e-5, 128, 75)])
+    _compare(case, oracle64, 2)
+
+
+def test_zero_steps_then_steps(lib, oracle64):
+    """A run of zero steps is a no-op that returns OK; the steps after it give
+    the same frames as a context that never ran it."""
+    case = Case(alt=[0.0, 4000.0], cn2=[0.6, 0.4], speed=[10.0, 20.0], direction=[0.3, 2.0], M=256, W=128, Wout=128)
+    screens = make_screens(case, oracle64)
+    from atmosphericturbulencesimul_gb300 import Series
+    from series_case import instances
+
+    def frames(zero_first):
+        s = Series(case.alt, case.cn2, case.speed, case.direction, master_size=case.M, instances=instances(case),
+                   pupil_scale=case.pupil, time_step=case.dt, fresnel_bin=case.fresnel_bin)
+        for l, sc in enumerate(screens):
+            s.load_screen(l, sc)
+        if zero_first:
+            z = s.run_frames(0)
+            assert all(p.shape[0] == 0 and a.shape[0] == 0 for p, a in z)
+        out = s.run_frames(2)
+        s.close()
+        return out
+
+    for (p0, a0), (p1, a1) in zip(frames(False), frames(True)):
+        assert np.array_equal(p0, p1) and np.array_equal(a0, a1)
