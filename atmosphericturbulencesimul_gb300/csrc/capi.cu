@@ -284,6 +284,9 @@ struct Class {
     int cfg = 0;               // tile configuration (tile_cfg), chosen by the autotuner
     std::vector<int> members;  // global instance indices
     int base = 0;              // first slot in the class-ordered InstDev array
+    // this class's science instances: entries [sci0, sci0 + nsci) of the
+    // context's science list, their largest bin grid and crop
+    int sci0 = 0, nsci = 0, maxnb = 0, maxnout = 0;
     TmaSet maps[kNumTileCfg];  // per configuration: the box height is RR + 3
     double tuned_ms[kNumTileCfg] = {};
     // windows of the groups whose side is this class's N (the class that
@@ -640,12 +643,16 @@ atmwfs_status launch_step(atmwfs_ctx* c)
             if (k == Q) AW_CUDA(cudaStreamWaitEvent(cs, sums, 0));
             AW_TRY(launch_pass(c, k, c->classes[ci], nullptr, cs));
         }
+        // the class's science unwrap and apply on its own branch: a class that
+        // finishes early unwraps beside the passes of the larger grids
+        const Class& cl = c->classes[ci];
+        if (cl.nsci > 0) {
+            AW_CUDA(unwrap_bins(c->d_inst, c->d_sci + cl.sci0, cl.nsci, cl.maxnb, c->d_status, c->d_iters,
+                                c->d_atan_tab, cs));
+            AW_CUDA(sci_apply(c->d_inst, c->d_sci + cl.sci0, cl.nsci, cl.maxnout, c->d_step, cs));
+        }
         AW_CUDA(cudaEventRecord(c->gev[2 + ci], cs));
         AW_CUDA(cudaStreamWaitEvent(c->st, c->gev[2 + ci], 0));
-    }
-    if (c->nsci > 0) {
-        AW_CUDA(unwrap_bins(c->d_inst, c->d_sci, c->nsci, c->maxnb, c->d_status, c->d_iters, c->d_atan_tab, c->st));
-        AW_CUDA(sci_apply(c->d_inst, c->d_sci, c->nsci, c->maxnout, c->d_step, c->st));
     }
     AW_CUDA(step_advance(c->d_step, c->st));
     return ATMWFS_OK;
@@ -1050,7 +1057,11 @@ atmwfs_status atmwfs_create(const atmwfs_params* p, atmwfs_ctx** out)
                     CKC(cudaMemcpy(dbx + No, b0.data(), sizeof(short) * (d.nb + 2), cudaMemcpyHostToDevice));
                     d.binx = dbx;
                     d.binx0 = dbx + No;
+                    if (cl.nsci == 0) cl.sci0 = (int)sci.size();
                     sci.push_back(slot);
+                    cl.nsci++;
+                    cl.maxnb = cl.maxnb > d.nb ? cl.maxnb : d.nb;
+                    cl.maxnout = cl.maxnout > No ? cl.maxnout : No;
                     c->maxnb = c->maxnb > d.nb ? c->maxnb : d.nb;
                     c->maxnout = c->maxnout > No ? c->maxnout : No;
                 }

@@ -147,8 +147,8 @@ def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
         info = {ci["n"]: ci for ci in (s.class_info(c) for c in range(s.num_classes()))}
         # the step graph: the window kernel (one window group, side 1024), a
         # phase sum per class (the layer-dependent Scoeff does not factor),
-        # 7 passes per class, unwrap, apply, step counter
-        assert s.step_kernels() == 1 + 2 + 2 * 7 + 3
+        # 7 passes, the unwrap and the apply per class, the step counter
+        assert s.step_kernels() == 1 + 2 + 2 * (7 + 2) + 1
         s.close()
         return info
 
