@@ -672,7 +672,7 @@ atmwfs_status forward(atmwfs_fno* f, const float* x, float* out, int B, cudaStre
                     pointwise_umma_supported(c.proj, c.width))
                        ? 1
                        : 0;
-    FN_CUDA(pointwise(pb + f->L.lift_W, c.width, c.nin, x, f->h[0], B, P, 0.0f, pf + f->L.lift_b, st));
+    FN_CUDA(pointwise_fwd(pb + f->L.lift_W, c.width, c.nin, x, 0, f->h[0], B, P, 0.0f, pf + f->L.lift_b, st));
     for (int l = 0; l < c.layers; l++) {
         // u = S_l(h) + W_l h + b_l; h' = gelu(u) from the same epilogue
         // (the last layer has no activation: its u is the projection's input)

@@ -118,19 +118,20 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // The pixels of one tile (C channel rows of 128 pixels, FP32 or BF16 as
 // stored) copied into the staging buffer with 16-byte asynchronous copies;
-// pixels past P are zeros.
-template <int C, typename TX>
+// pixels past P are zeros, and so are the channel rows from CR on (X holds
+// CR channels per sample; K is padded to the MMA's multiple of 16).
+template <int C, int CR, typename TX>
 __device__ __forceinline__ void stage_tile(TX* stage, const TX* X, long P, int tile, long tiles_per_sample, int tid)
 {
     constexpr int EPC = 16 / sizeof(TX);  // elements per 16-byte chunk
     const long b = tile / tiles_per_sample;
     const long p0 = (tile - b * tiles_per_sample) * kM;
-    const TX* xs = X + (size_t)b * C * P + p0;
+    const TX* xs = X + (size_t)b * CR * P + p0;
     constexpr int CH = kM / EPC;  // chunks per channel row
     for (int i = tid; i < C * CH; i += kThreads) {
         const int k = i / CH, ch = i - k * CH;
         TX* dst = stage + k * kM + EPC * ch;
-        if (p0 + EPC * ch < P) cp_async16(dst, xs + (size_t)k * P + EPC * ch);
+        if (k < CR && p0 + EPC * ch < P) cp_async16(dst, xs + (size_t)k * P + EPC * ch);
         else *reinterpret_cast<uint4*>(dst) = make_uint4(0u, 0u, 0u, 0u);
     }
     cp_async_commit();
@@ -145,7 +146,7 @@ __device__ __forceinline__ void put(__nv_bfloat16* p, float v) { *p = __float2bf
 // tile; the next tile's copies start; one thread issues the MMAs; all wait
 // for their commit; the eight warps read D (warp w: lanes 32 (w % 4) ..,
 // columns of half w / 4) and write C while the next tile's pixels arrive.
-template <int O, int C, typename TX, typename TA>
+template <int O, int C, typename TX, typename TA, int CR = C>
 __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* __restrict__ W, const TX* __restrict__ X,
                                                            float* __restrict__ Cm, TA* __restrict__ act,
                                                            const float* __restrict__ bias, float beta, long P, int ntiles,
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const long tiles_per_sample = (P + kM - 1) / kM;
-    if (blockIdx.x < ntiles) stage_tile<C, TX>(stage, X, P, blockIdx.x, tiles_per_sample, tid);
+    if (blockIdx.x < ntiles) stage_tile<C, CR, TX>(stage, X, P, blockIdx.x, tiles_per_sample, tid);
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
                      "r"(kCols)
@@ -173,11 +174,12 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) mbar_init(&bar);
-    // weights: W is o x c, row-major (K contiguous), element loads (the
-    // parameter blocks carry no alignment guarantee)
+    // weights: W is o x CR, row-major (K contiguous), element loads (the
+    // parameter blocks carry no alignment guarantee); zeros for k >= CR
     for (int i = tid; i < O * C; i += kThreads) {
         const int n = i / C, k = i - n * C;
-        *reinterpret_cast<__nv_bfloat16*>(sb + kmajor_off(n, k, KC)) = W[i];
+        *reinterpret_cast<__nv_bfloat16*>(sb + kmajor_off(n, k, KC)) =
+            k < CR ? W[n * CR + k] : __float2bfloat16_rn(0.0f);
     }
     fence_before();
     __syncthreads();
@@ -212,7 +214,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
         __syncthreads();
         fence_after();
         // the staging buffer is free: the next tile's pixels come in now
-        if (tile + (int)gridDim.x < ntiles) stage_tile<C, TX>(stage, X, P, tile + gridDim.x, tiles_per_sample, tid);
+        if (tile + (int)gridDim.x < ntiles) stage_tile<C, CR, TX>(stage, X, P, tile + gridDim.x, tiles_per_sample, tid);
         if (tid == 0) {
 #pragma unroll
             for (int ks = 0; ks < C / 16; ks++) {
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_pointwise(const __nv_bfloat16* 
     }
 }
 
-template <int O, int C, typename TX, typename TA>
+template <int O, int C, typename TX, typename TA, int CR = C>
 cudaError_t launch(const __nv_bfloat16* W, const TX* X, float* Cm, TA* act, const float* bias, float beta, int B, long P,
                    unsigned* status, int swap, int write_c, cudaStream_t st)
 {
@@ -299,7 +301,7 @@ cudaError_t launch(const __nv_bfloat16* W, const TX* X, float* Cm, TA* act, cons
     constexpr size_t smem = (size_t)C * kM * sizeof(TX) + (size_t)kM * C * 2 + (size_t)O * C * 2;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_pointwise<O, C, TX, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_pointwise<O, C, TX, TA, CR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
         attr = true;
@@ -309,8 +311,8 @@ cudaError_t launch(const __nv_bfloat16* W, const TX* X, float* Cm, TA* act, cons
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long grid = tiles < 3L * sms ? tiles : 3L * sms;
-    k_pointwise<O, C, TX, TA><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles, status,
-                                                                        swap, write_c);
+    k_pointwise<O, C, TX, TA, CR><<<(unsigned)grid, kThreads, smem, st>>>(W, X, Cm, act, bias, beta, P, (int)tiles,
+                                                                            status, swap, write_c);
     return cudaGetLastError();
 }
 
@@ -747,10 +749,10 @@ cudaError_t spectral_umma(const __nv_bfloat16* W, int o, int c, const float* X, 
 }
 
 // The shapes of the surrogate's pointwise products that run on tcgen05:
-// o x c in {64 x 64 (Fourier layers), 128 x 64 (projection 1)}.  Others
-// (the 8-channel lift, the 2-channel output) return cudaErrorNotSupported
-// and stay on the mma.sync product.
-bool pointwise_umma_supported(int o, int c) { return (o == 64 && c == 64) || (o == 128 && c == 64); }
+// o x c in {64 x 64 (Fourier layers), 128 x 64 (projection 1), 64 x 8 (the
+// lift: K padded to 16 with zero channels)}.  Others (the 2-channel output)
+// return cudaErrorNotSupported and stay on the mma.sync product.
+bool pointwise_umma_supported(int o, int c) { return (o == 64 && c == 64) || (o == 128 && c == 64) || (o == 64 && c == 8); }
 
 cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const void* X, int x_bf16, float* C, int B, long P,
                            float beta, const float* bias, void* act, int a_bf16, unsigned* status, int swap, bool write_c,
@@ -761,6 +763,9 @@ cudaError_t pointwise_umma(const __nv_bfloat16* W, int o, int c, const void* X, 
         return umma::launch_t<64, 64>(W, X, x_bf16, C, act, a_bf16, bias, beta, B, P, status, swap, wc, st);
     if (o == 128 && c == 64)
         return umma::launch_t<128, 64>(W, X, x_bf16, C, act, a_bf16, bias, beta, B, P, status, swap, wc, st);
+    if (o == 64 && c == 8 && !x_bf16 && !act)
+        return umma::launch<64, 16, float, float, 8>(W, (const float*)X, C, nullptr, bias, beta, B, P, status, swap, wc,
+                                                     st);
     return cudaErrorNotSupported;
 }
 

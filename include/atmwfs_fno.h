@@ -85,7 +85,8 @@ atmwfs_status atmwfs_gemm_bf16(int M, int N, int K, const void* A, long lda, int
  * counterpart in the reference, whose path has no network):
  * C[b] (o x P) = W (o x c, BF16) X[b] (c x P, FP32) + bias[o] + beta C[b],
  * act[b] = gelu(C[b]) if act is not NULL, on the tcgen05 tensor cores
- * (accumulator in tensor memory), compiled for o x c = 64 x 64 and 128 x 64.
+ * (accumulator in tensor memory), compiled for o x c = 64 x 64 and 128 x 64, and
+ * 64 x 8 without act (the lift: K padded to 16 with zero channels).
  * engine 1: the product the network uses; 2: the same with the two
  * core-matrix strides of its shared-memory descriptors exchanged (a check
  * that only engine 1 matches the FP32 product). */
