@@ -674,8 +674,23 @@ atmwfs_status clear_bins(atmwfs_ctx* c)
 // (a middle pass when there is one) in each configuration compiled for its
 // size -- radix plan and tile shape (tile_cfg) -- and keep the fastest.
 // ATMWFS_TILE_CFG=<k> forces configuration k (ignored where the size has
-// none).  Science bins are cleared afterwards (a timed last pass
-// accumulates into them).
+// none); ATMWFS_TILE_CFG=<N>:<k>[,<N>:<k>...] forces it for the listed grid
+// sizes only and tunes the others.  Science bins are cleared afterwards (a
+// timed last pass accumulates into them).
+int forced_cfg(const char* force, int N)
+{
+    if (!force || !*force) return -1;
+    if (!strchr(force, ':')) return atoi(force);
+    for (const char* p = force; p && *p;) {
+        char* end = nullptr;
+        const long n = strtol(p, &end, 10);
+        if (end && *end == ':' && n == N) return atoi(end + 1);
+        p = strchr(p, ',');
+        if (p) p++;
+    }
+    return -1;
+}
+
 atmwfs_status autotune(atmwfs_ctx* c)
 {
     const int Q = (int)c->plane_lo.size();
@@ -688,9 +703,9 @@ atmwfs_status autotune(atmwfs_ctx* c)
     for (Class& cl : c->classes) {
         if (c->fp16) {
             cl.cfg = 2;  // the FP16-transform passes are compiled for configuration 2
-        } else if (force) {
-            const int g = atoi(force);
-            cl.cfg = (g >= 0 && g < kNumTileCfg && tile_cfg(cl.N, g).rr > 0) ? g : 0;
+        } else if (forced_cfg(force, cl.N) >= 0) {
+            const int g = forced_cfg(force, cl.N);
+            cl.cfg = (g < kNumTileCfg && tile_cfg(cl.N, g).rr > 0) ? g : 0;
         } else {
             // two interleaved rounds over the configurations; each keeps its
             // fastest reading, so one disturbed reading does not decide

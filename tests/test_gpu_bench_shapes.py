@@ -130,7 +130,7 @@ def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
     """The autotuner times every configuration compiled for a grid size --
     at 1024 the 32 x 32 plan in three tile shapes and the 16 x 8 x 8 plan in
     two -- and reports the one it keeps; a forced configuration is taken as
-    given."""
+    given, for every size or for the sizes listed as N:k."""
     from atmosphericturbulencesimul_gb300 import Series
     from series_case import instances, make_screens
 
@@ -168,6 +168,12 @@ def test_autotuner_reports_its_radix_plan(lib, oracle64, monkeypatch):
     info = classes()
     assert info[1024]["cfg"] == 3 and info[1024]["radices"] == [16, 8, 8] and info[1024]["rows_per_cta"] == 4
     assert info[512]["cfg"] == 0 and info[512]["radices"] == [32, 16]
+    # per-size form: 512 forced to the staged tables, 1024 tuned
+    monkeypatch.setenv("ATMWFS_TILE_CFG", "512:5")
+    info = classes()
+    assert info[512]["cfg"] == 5 and all(t == 0 for t in info[512]["tuned_ms"])
+    assert all(t > 0 for t in info[1024]["tuned_ms"])
+    assert info[1024]["tuned_ms"][info[1024]["cfg"]] == min(info[1024]["tuned_ms"])
 
 
 def test_w2048_step(lib, oracle64):
