@@ -166,6 +166,7 @@ __device__ float bin_votes(const float* pb, const float* ppf, int nb, int bx, in
 __global__ void k_unwrap(const InstDev* __restrict__ insts, const int* __restrict__ list, unsigned* status,
                          int* iters_out, const float2* __restrict__ atan_tab)
 {
+    pdl_gate();
     const InstDev& I = insts[list[blockIdx.x]];
     const int nb = I.nb;
     if (nb <= 0) return;
@@ -250,14 +251,14 @@ cudaError_t unwrap_bins(const InstDev* insts, const int* list, int nsci, int max
         cudaError_t e = cudaFuncSetAttribute(k_unwrap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (e != cudaSuccess) return e;
     }
-    k_unwrap<<<nsci, 512, sm, st>>>(insts, list, status, iters, atan_tab);
-    return cudaGetLastError();
+    return launch_gated(k_unwrap, dim3(nsci), dim3(512), sm, st, insts, list, status, iters, atan_tab);
 }
 
 // final science phase: pha + 2 pi round((phasum - pha - peak[bin]) / 2 pi)
 // (AtmosphericTurbulence.c:3918-3941)
 __global__ void k_sci_apply(const InstDev* __restrict__ insts, const int* __restrict__ list, const int* d_step)
 {
+    pdl_gate();
     const InstDev& I = insts[list[blockIdx.y]];
     const int Nout = I.Nout, nb = I.nb;
     const int step = d_step ? *d_step : 0;
@@ -307,8 +308,7 @@ cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxno
 {
     if (nsci <= 0) return cudaSuccess;
     const int bx = maxnout < 256 ? maxnout : 256;
-    k_sci_apply<<<dim3(bx, nsci), 256, 0, st>>>(insts, list, d_step);
-    return cudaGetLastError();
+    return launch_gated(k_sci_apply, dim3(bx, nsci), dim3(256), 0, st, insts, list, d_step);
 }
 
 // Layer sum of one window group, from the top layer down with a two-sum
@@ -317,6 +317,7 @@ cudaError_t sci_apply(const InstDev* insts, const int* list, int nsci, int maxno
 // thread as 16-byte vectors, every layer requested before the sums.
 __global__ void __launch_bounds__(256) k_group_sum(const GroupSumJob* __restrict__ jobs, int L)
 {
+    pdl_gate();
     const GroupSumJob& J = jobs[blockIdx.y];
     const long n4 = (long)J.side * J.side / 4;
     for (long k = (long)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += (long)gridDim.x * blockDim.x) {
@@ -349,16 +350,18 @@ cudaError_t group_sums(const GroupSumJob* jobs, int njobs, int L, int maxside, c
     if (njobs <= 0) return cudaSuccess;
     const long n4 = (long)maxside * maxside / 4;
     const long b = (n4 + 255) / 256;
-    k_group_sum<<<dim3((unsigned)(b < 1024 ? b : 1024), (unsigned)njobs), 256, 0, st>>>(jobs, L);
-    return cudaGetLastError();
+    return launch_gated(k_group_sum, dim3((unsigned)(b < 1024 ? b : 1024), (unsigned)njobs), dim3(256), 0, st, jobs, L);
 }
 
-__global__ void k_step_advance(int* d_step) { *d_step += 1; }
+__global__ void k_step_advance(int* d_step)
+{
+    pdl_gate();
+    *d_step += 1;
+}
 
 cudaError_t step_advance(int* d_step, cudaStream_t st)
 {
-    k_step_advance<<<1, 1, 0, st>>>(d_step);
-    return cudaGetLastError();
+    return launch_gated(k_step_advance, dim3(1), dim3(1), 0, st, d_step);
 }
 
 // ---------------------------------------------------------------------------

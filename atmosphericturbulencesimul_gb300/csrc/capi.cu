@@ -696,6 +696,11 @@ atmwfs_status autotune(atmwfs_ctx* c)
     const int Q = (int)c->plane_lo.size();
     const char* force = getenv("ATMWFS_TILE_CFG");
     const int k = Q >= 3 ? 2 : 1;
+    // the candidates are timed with plain launches (see pdl_hold)
+    struct Hold {
+        Hold() { pdl_hold() = 1; }
+        ~Hold() { pdl_hold() = 0; }
+    } hold;
     cudaEvent_t e0, e1;
     AW_CUDA(cudaEventCreate(&e0));
     AW_CUDA(cudaEventCreate(&e1));

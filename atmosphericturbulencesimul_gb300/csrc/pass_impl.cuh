@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(Plan<N, V>::T* RR, MINB)
     extern __shared__ __align__(1024) unsigned char sm[];
     float2* xb = reinterpret_cast<float2*>(sm);
     float* wrows = reinterpret_cast<float*>(sm + G::win_offset());  // [RR][N]
+    pdl_gate();
 
     const int tid = threadIdx.x;
     const int t = tid % T;
@@ -668,6 +669,7 @@ __global__ void __launch_bounds__(PassGeom<N, RR>::NT)
     extern __shared__ __align__(1024) unsigned char sm[];
     float* tile = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sm) + 127) & ~uintptr_t(127));
     __shared__ __align__(8) uint64_t bar;
+    pdl_gate();
     const WinJob J = a.jobs[blockIdx.y];
     const int tid = threadIdx.x;
     const int y0 = blockIdx.x * RR;
@@ -700,6 +702,7 @@ template <int N>
 __global__ void __launch_bounds__(kPhasumThreads, 4) k_phasum(const __grid_constant__ PassArgs a)
 {
     constexpr int kChunk = 8;
+    pdl_gate();
     const InstDev* I = a.inst + blockIdx.y;
     if (I->gsum) return;  // this instance's phase sum factors through its group's layer sum
     const int off = I->off, Nout = I->Nout, L = a.L;
@@ -763,8 +766,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
             if (e != cudaSuccess) return e;                                                            \
             attr = true;                                                                               \
         }                                                                                              \
-        k_pass<N, RR, MINB, VAR, ALIAS, HP, V, HS><<<grid, block, sm, st>>>(a, m, tw);                 \
-        return cudaGetLastError();                                                                     \
+        return launch_gated(k_pass<N, RR, MINB, VAR, ALIAS, HP, V, HS>, grid, block, sm, st, a, m, tw); \
     }
     if constexpr (HP || V != 0 || SO || HS) {
         // FP16 transforms, the alternative radix plans and configurations
@@ -786,8 +788,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
         AW_CASE(kVarUnitFwd)
         AW_CASE(kVarUnitInv)
         case kVarPhasum: {
-            k_phasum<N><<<grid, kPhasumThreads, 0, st>>>(a);
-            return cudaGetLastError();
+            return launch_gated(k_phasum<N>, grid, dim3(kPhasumThreads), 0, st, a);
         }
         case kVarWindows: {
             constexpr size_t sm = G::TILE_BYTES + 128;
@@ -797,8 +798,7 @@ cudaError_t launch_pass_t(int var, dim3 grid, const PassArgs& a, const TmaSet* m
                 if (e != cudaSuccess) return e;
                 attr = true;
             }
-            k_layer_windows<N, RR><<<grid, dim3(G::NT), sm, st>>>(a, m);
-            return cudaGetLastError();
+            return launch_gated(k_layer_windows<N, RR>, grid, dim3(G::NT), sm, st, a, m);
         }
         default: return cudaErrorInvalidValue;
     }
